@@ -1,0 +1,343 @@
+#!/usr/bin/env python
+"""Headline benchmark: D2Q9 BGK channel 4096 x 1024, FP32, in MLUPS.
+
+Workload (one bench step = one whole solve): periodic in x, walls on rows 0 and 1023, Guo body
+force 1e-6 in x, tau 0.55, 64 non-overlapping disks (centres uniform, radius uniform in [8, 24],
+seed 20261203), 10,000 time steps.  MLUPS counts all 4,194,304 cells per time step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mine|reference]
+
+Arm "mine" (default) prints one JSON line with
+  value      device-resident throughput (state in HBM before the timed region), CUDA events on the
+             library's stream, max over ranks, summed over ranks (replicas: each rank solves its own
+             domain, no data-path collective)
+  e2e        the same solve through the C ABI from pinned host buffers: flags + initial populations
+             host->device, 10,000 steps, density/velocity device->host, every step
+  roofline   step kernel: algorithmic bytes per launch (72 B x cells) / average launch duration
+  cpu_baseline  the CPU oracle (OpenMP, all host cores) on a bounded sample of the same workload
+Arm "reference" times the CPU restatement of the step on the host cores (the reference has no CPU
+implementation of its own) on the same workload and prints the same kind of line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX, NY, NDISKS, RMIN, RMAX = 4096, 1024, 64, 8.0, 24.0
+TAU, FORCE, SEED, LBM_STEPS = 0.55, 1e-6, 20261203, 10000
+W9 = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4, dtype=np.float32)
+WORKLOAD = (f"D2Q9 BGK channel {NX}x{NY} FP32: periodic x, walls y=0 and y={NY - 1}, Guo force {FORCE} in x, "
+            f"tau {TAU}, {NDISKS} non-overlapping disks r in [{RMIN:g},{RMAX:g}] (seed {SEED}), "
+            f"{LBM_STEPS} steps per bench step")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
+    ap.add_argument("--lbm-steps", type=int, default=LBM_STEPS)
+    ap.add_argument("--dtype", default="f32", choices=["f32", "f16s", "bf16s"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------- helpers
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel_key: str):
+    """Per-launch DRAM bytes (read + write) of the step kernel from the committed ncu summary."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for name in sorted(os.listdir(pdir)):
+        if not name.endswith((".md", ".txt")) or kernel_key not in name:
+            continue
+        with open(os.path.join(pdir, name)) as fh:
+            m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", fh.read())
+        if m:
+            return float(m.group(1))
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def channel_flags():
+    import latticeboltzmanncuda_gb300 as lbm
+    flags, _ = lbm.gen_channel(NX, NY, NDISKS, RMIN, RMAX, SEED)
+    return flags
+
+
+def cpu_port_mlups(flags, seconds, threads=None):
+    """The CPU oracle's FP32 step (OpenMP over all host cores) on the same channel; the number of
+    time steps is sized to about `seconds` of work.  Returns (MLUPS, steps, threads)."""
+    import oracle
+    if threads:
+        oracle.set_num_threads(threads)
+    nthreads = oracle.num_threads()
+    f = np.ascontiguousarray(np.broadcast_to(W9[:, None, None], (9, NY, NX)), dtype=np.float32)
+    out = np.empty_like(f)
+    t0 = time.perf_counter()
+    oracle.d2q9_step(f, flags, np.float32(TAU), periodic=1, force=(np.float32(FORCE), np.float32(0)), out=out)
+    t1 = time.perf_counter()
+    steps = int(max(2, min(5000, math.ceil(seconds / max(t1 - t0, 1e-6)))))
+    a, b = f, out
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        oracle.d2q9_step(a, flags, np.float32(TAU), periodic=1, force=(np.float32(FORCE), np.float32(0)), out=b)
+        a, b = b, a
+    dt = time.perf_counter() - t0
+    return NX * NY * steps / dt / 1e6, steps, nthreads
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ----------------------------------------------------------------------------- arms
+def run_reference(args):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    import oracle
+    flags = channel_flags()
+    per = max(args.cpu_seconds / max(args.steps + args.warmup, 1), 0.5)
+    # each bench step is a bounded sample of the solve: the same steps count every time
+    _, steps, threads = cpu_port_mlups(flags, per)
+    f = np.ascontiguousarray(np.broadcast_to(W9[:, None, None], (9, NY, NX)), dtype=np.float32)
+    out = np.empty_like(f)
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        a, b = f, out
+        for _ in range(steps):
+            oracle.d2q9_step(a, flags, np.float32(TAU), periodic=1, force=(np.float32(FORCE), np.float32(0)), out=b)
+            a, b = b, a
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    t = sum(times)
+    value = args.steps * steps * NX * NY / t / 1e6
+    sample = f"{NX}x{NY} channel, {steps} time steps per bench step (of {args.lbm_steps})"
+    line = {
+        "impl": "reference", "metric": "MLUPS", "value": round(value, 3), "unit": "MLUPS", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * t / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": sample, "l2": "inputs (302 MB state) larger than L2"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference has no CPU step; this is the CPU restatement of the step (oracle/) on all host cores",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_mine(args):
+    import torch
+    import latticeboltzmanncuda_gb300 as lbm
+
+    ws, rank, local = dist_setup()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    flags = channel_flags()
+    cells = NX * NY
+    stream = torch.cuda.Stream(device=dev)
+    L = lbm.Lattice(NX, NY, dtype=args.dtype, tau=TAU, periodic=1, body_force=(FORCE, 0.0, 0.0),
+                    device=local, stream=stream.cuda_stream)
+    L.set_flags(flags)
+    L.init_equilibrium()
+    info = L.info()
+    bpu = info["bytes_per_update"]
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---------------- device-resident
+    for _ in range(args.warmup):
+        L.step(args.lbm_steps)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for _ in range(args.steps):
+            L.step(args.lbm_steps)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier()
+    t = max_over_ranks(e0.elapsed_time(e1) / 1000.0)
+    launches = args.steps * args.lbm_steps
+    value = ws * args.steps * args.lbm_steps * cells / t / 1e6
+    avg_launch = t / launches
+    achieved = bpu * cells / avg_launch / 1e9
+    peak, peak_kind = peaks()
+    cons = L.conservation()
+
+    # ---------------- end to end through the C ABI, pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        flags_h = torch.from_numpy(flags).pin_memory().numpy()
+        f0 = torch.empty((9, NY, NX), dtype=torch.float32).pin_memory().numpy()
+        f0[:] = W9[:, None, None]
+        outs = [torch.empty((NY, NX), dtype=torch.float32).pin_memory().numpy() for _ in range(3)]
+        def one():
+            L.set_flags(flags_h)
+            L.load_populations(f0)
+            L.step(args.lbm_steps)
+            L.moments(out=outs)
+        for _ in range(args.warmup):
+            one()
+        torch.cuda.synchronize(dev)
+        barrier()
+        x0, x1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        w0 = time.perf_counter()
+        x0.record(stream)
+        for _ in range(args.steps):
+            one()
+        x1.record(stream)
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - w0
+        barrier()
+        te = max_over_ranks(max(x0.elapsed_time(x1) / 1000.0, 0.0))
+        te = max(te, max_over_ranks(wall))
+        e2e = {"value": round(ws * args.steps * args.lbm_steps * cells / te / 1e6, 3), "unit": "MLUPS",
+               "h2d_bytes_per_step": int(flags_h.nbytes + f0.nbytes), "d2h_bytes_per_step": int(sum(o.nbytes for o in outs)),
+               "ms_per_step": round(1000 * te / args.steps, 3)}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        mlups, steps, threads = cpu_port_mlups(flags, args.cpu_seconds)
+        cpu = {"value": round(mlups, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
+               "sample": f"{NX}x{NY} channel, {steps} FP32 time steps (of {args.lbm_steps}), OpenMP"}
+
+    if rank == 0:
+        traffic = ncu_traffic(f"d2q9_step_{args.dtype}")
+        line = {
+            "metric": "MLUPS", "value": round(value, 3), "unit": "MLUPS", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1000 * t / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells": cells, "fluid_cells": info["fluid_cells"],
+                       "lbm_steps_per_bench_step": args.lbm_steps, "parallelism": f"replicas x{ws}",
+                       "l2": "inputs larger than L2: 2 x 151 MB population buffers (129 MB L2)"},
+            "mflups": round(value * info["fluid_cells"] / cells, 3),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                         "bytes_per_update": bpu, "traffic": traffic,
+                         "kernel": f"step_kernel<{args.dtype}>", "avg_launch_us": round(avg_launch * 1e6, 3)},
+            "gpu_launches": launches,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "mass": cons[0],
+        }
+        print(json.dumps(line), flush=True)
+    L.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_mine(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

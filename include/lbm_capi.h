@@ -1,0 +1,204 @@
+/*
+ * lbm_capi.h -- C ABI of the GB300 lattice Boltzmann library (liblbm_gb300.so).
+ *
+ * This is the drop-in boundary for the reference's collide-stream path.  The reference exposes
+ * that path as the C++ class Lattice (simulation/include/Lattice.h:40-106) on top of the launch
+ * wrappers RunCudaFunctions::run_* (simulation/include/SimCalcFuncs.cuh:13-25); a C++
+ * compatibility layer with those names is built on this ABI (see the package's simulation/
+ * directory), and other languages bind these functions directly (ctypes, cgo, JNI).
+ *
+ * Conventions
+ *   - Every function returns an lbm_status; lbm_last_error() gives the message of the last
+ *     failure on a context (or, for a NULL context, of the calling thread).
+ *   - Plain pointers and sizes only.  Pointers named host_* are host memory owned by the caller;
+ *     the context owns all device memory it allocates and frees it in lbm_destroy().
+ *   - One context per host thread at a time.  Each context works on its own CUDA stream (the one
+ *     given in lbm_desc.stream, or a non-blocking stream it creates).  Functions that read results
+ *     back to the host synchronise that stream; lbm_step() only enqueues work.
+ *   - Two lattice modes share the API:
+ *       LBM_D2Q9      standard D2Q9 BGK: pull streaming, half-way bounce-back, moving walls,
+ *                     periodic edges, Guo body force; populations stored shifted (f_i - w_i) in
+ *                     FP32, FP16, BF16 or FP64.
+ *       LBM_D3Q27_REF the reference's own D3Q27 step (SimCalcFuncs.cu:79-215): zero-fill pull
+ *                     streaming, mesh "reflections", SPLIT-weighted velocity, FP64-evaluated
+ *                     equilibrium, mass-source flow; FP32 populations.
+ */
+#ifndef LBM_CAPI_H
+#define LBM_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define LBM_API __attribute__((visibility("default")))
+#else
+#define LBM_API
+#endif
+
+typedef enum lbm_status {
+    LBM_OK = 0,
+    LBM_ERR_INVALID = 1,     /* bad argument or size */
+    LBM_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    LBM_ERR_OOM = 3,         /* device allocation failed */
+    LBM_ERR_UNSUPPORTED = 4, /* call not available in this mode / dtype */
+    LBM_ERR_STATE = 5,       /* call out of order (e.g. step before flags) */
+    LBM_ERR_BUDGET = 6,      /* request does not fit the server's memory budget */
+    LBM_ERR_TIMEOUT = 7      /* a bounded wait gave up */
+} lbm_status;
+
+typedef enum lbm_mode { LBM_D2Q9 = 0, LBM_D3Q27_REF = 1 } lbm_mode;
+
+typedef enum lbm_dtype {
+    LBM_F32 = 0,   /* FP32 storage (D2Q9: shifted f_i - w_i) */
+    LBM_F16S = 1,  /* FP16 storage of f_i - w_i, FP32 arithmetic (D2Q9 only) */
+    LBM_BF16S = 2, /* BF16 storage of f_i - w_i, FP32 arithmetic (D2Q9 only) */
+    LBM_F64 = 3    /* FP64 storage and arithmetic: the GPU oracle run (D2Q9 only) */
+} lbm_dtype;
+
+/* D2Q9 cell flags (one byte per cell, row-major [ny][nx]) */
+enum { LBM_FLUID = 0, LBM_WALL = 1, LBM_MOVING_WALL = 2 };
+
+/* D3Q27_REF cell flag bits (one byte per cell, reference index z + Z*(y + Y*x)):
+ * LatticePoint::isInternal, LatticePoint::isReflected (LatticePoint.h:13-14) and the flow
+ * criterion of FlowData (FlowSurface.h:9-46) evaluated once per cell. */
+enum { LBM_INTERNAL = 1, LBM_REFLECTED = 2, LBM_SOURCE = 4 };
+
+/* D3Q27_REF step orders for lbm_step():
+ *   LBM_ORDER_STREAM_COLLIDE  Lattice::simulateLattice (Lattice.cpp:222-226)
+ *   LBM_ORDER_CLI             stream, reflect, collide, flow (LatticeBoltzmannCuda.cpp:85-93) */
+enum { LBM_ORDER_STREAM_COLLIDE = 0, LBM_ORDER_CLI = 1 };
+
+/* D3Q27_REF single passes for lbm_apply(), one flag per call (Lattice::simulateStreaming,
+ * simulateReflections, simulateCollision, simulateFlow; Lattice.cpp:115-220) */
+enum { LBM_OP_STREAM = 1, LBM_OP_REFLECT = 2, LBM_OP_COLLIDE = 4, LBM_OP_FLOW = 8 };
+
+/* D3Q27_REF momentum-exchange force convention (SimCalcFuncs.cu:179-184):
+ *   LBM_FORCE_REFERENCE          the reference's slot-indexed term c_s*SPLIT[s] (slots >= 27,
+ *                                undefined in the reference, contribute no incoming term)
+ *   LBM_FORCE_MOMENTUM_EXCHANGE  the arriving population's term c_{s/3}*SPLIT[s/3] */
+enum { LBM_FORCE_REFERENCE = 0, LBM_FORCE_MOMENTUM_EXCHANGE = 1 };
+
+typedef struct lbm_desc {
+    int32_t mode;             /* lbm_mode */
+    int32_t dtype;            /* lbm_dtype */
+    int32_t nx, ny, nz;       /* D2Q9: nx x ny (nz = 1); D3Q27_REF: X, Y, Z of Lattice(x, y, z, ...) */
+    int32_t periodic;         /* D2Q9: bit0 periodic in x, bit1 periodic in y; other edges are walls */
+    float tau;                /* relaxation time (FluidData::m_characteristicTimescale) */
+    float body_force[3];      /* D2Q9: Guo body force per cell (x, y) */
+    float wall_velocity[3];   /* D2Q9: velocity of LBM_MOVING_WALL cells (x, y) */
+    int32_t order;            /* D3Q27_REF: LBM_ORDER_* used by lbm_step() */
+    int32_t force_mode;       /* D3Q27_REF: LBM_FORCE_* */
+    int32_t device;           /* CUDA device ordinal */
+    void *stream;             /* cudaStream_t to work on, or NULL for a private stream */
+} lbm_desc;
+
+typedef struct lbm_ctx lbm_ctx;
+
+typedef struct lbm_info {
+    int64_t cells;            /* nx*ny*nz */
+    int64_t fluid_cells;      /* D2Q9: cells with LBM_FLUID after lbm_set_flags() */
+    int64_t row_pitch;        /* D2Q9: elements per stored row (nx rounded up) */
+    int64_t state_bytes;      /* device bytes of both population buffers */
+    int64_t device_bytes;     /* all device bytes owned by the context */
+    int64_t bytes_per_update; /* algorithmic bytes per cell update: 2 * Q * sizeof(storage) */
+    int64_t steps_done;
+    int32_t block_threads;    /* launch shape of the step kernel */
+    int32_t cells_per_thread;
+} lbm_info;
+
+/* ---------------------------------------------------------------- context life cycle */
+LBM_API void lbm_desc_init(lbm_desc *desc);
+LBM_API lbm_status lbm_create(const lbm_desc *desc, lbm_ctx **out);
+LBM_API lbm_status lbm_destroy(lbm_ctx *ctx);
+LBM_API const char *lbm_last_error(const lbm_ctx *ctx);
+LBM_API const char *lbm_status_string(lbm_status s);
+LBM_API lbm_status lbm_get_info(lbm_ctx *ctx, lbm_info *out);
+LBM_API lbm_status lbm_get_stream(lbm_ctx *ctx, void **stream);
+LBM_API lbm_status lbm_synchronize(lbm_ctx *ctx);
+/* change tau / body force / wall velocity between steps */
+LBM_API lbm_status lbm_set_params(lbm_ctx *ctx, float tau, const float body_force[3],
+                                  const float wall_velocity[3]);
+
+/* ---------------------------------------------------------------- geometry and state */
+/* Cell flags, host_flags[cells] (layout per mode, see enums above).  Replaces
+ * Lattice::insertModel's isInternal output (Lattice.cpp:228-260) for D3Q27_REF. */
+LBM_API lbm_status lbm_set_flags(lbm_ctx *ctx, const uint8_t *host_flags);
+LBM_API lbm_status lbm_get_flags(lbm_ctx *ctx, uint8_t *host_flags);
+
+/* D2Q9: populations = equilibrium of (rho, ux, uy) per cell; NULL arrays mean rho = 1, u = 0. */
+LBM_API lbm_status lbm_init_equilibrium(lbm_ctx *ctx, const float *host_rho, const float *host_ux,
+                                        const float *host_uy);
+
+/* Raw populations, unshifted, as float (host_dtype LBM_F32) or double (LBM_F64).
+ *   D2Q9:      host[q][ny][nx], q in the order (0,0),(1,0),(0,1),(-1,0),(0,-1),(1,1),(-1,1),
+ *              (-1,-1),(1,-1)
+ *   D3Q27_REF: host[cell][27] in the reference's particle_distribution order (SimCalcFuncs.cu:12) */
+LBM_API lbm_status lbm_load_populations(lbm_ctx *ctx, const void *host, int32_t host_dtype);
+LBM_API lbm_status lbm_retrieve_populations(lbm_ctx *ctx, void *host, int32_t host_dtype);
+
+/* Reference AoS records (struct LatticePoint, LatticePoint.h:9-17, 144 bytes each), count =
+ * cells, record index z + Z*(y + Y*x); 2-D lattices use X = nx, Y = ny, Z = 1 and the in-plane
+ * slots {0,6,5,1,2,18,10,7,15} for the D2Q9 populations.  Replaces Lattice::load_data /
+ * retrieve_data (Lattice.cpp:73-113).  Loading takes particle_distribution and, in D3Q27_REF,
+ * isInternal / isReflected; retrieving writes x, y, z, particle_distribution and the flags and
+ * sets both reflection pointers to NULL. */
+LBM_API lbm_status lbm_load_aos(lbm_ctx *ctx, const void *host_points, int64_t count);
+LBM_API lbm_status lbm_retrieve_aos(lbm_ctx *ctx, void *host_points, int64_t count);
+
+/* D3Q27_REF reflection tables: records[i] (struct ReflectionValues, LatticePoint.h:3-7,
+ * 380 bytes) belongs to cell cells[i] (reference index).  Replaces the device upload of
+ * Lattice::preProcessModel (Lattice.cpp:417-423).  count = 0 clears the tables. */
+LBM_API lbm_status lbm_set_reflection_tables(lbm_ctx *ctx, int64_t count, const int32_t *host_cells,
+                                             const void *host_records);
+
+/* D3Q27_REF flow source (FlowData, FlowSurface.h:9-46; Lattice::setFlowData, Lattice.cpp:428-436):
+ * host_mask[cells] != 0 marks cells where the criterion holds (NULL keeps the current mask),
+ * host_induced[27] the populations added there each step (NULL disables flow). */
+LBM_API lbm_status lbm_set_flow(lbm_ctx *ctx, const uint8_t *host_mask, const float *host_induced);
+
+/* D3Q27_REF accumulated momentum-exchange force (ReflectionData, Lattice.h:33-38).
+ * lbm_set_force starts accumulation from host_in (Lattice::setReflectionData, Lattice.cpp:61-71);
+ * enabled = 0 stops accumulating.  lbm_get_force reads the running sum
+ * (Lattice::retrieve_reflection_data, Lattice.cpp:438-443). */
+LBM_API lbm_status lbm_set_force(lbm_ctx *ctx, const float host_in[3], int32_t enabled);
+LBM_API lbm_status lbm_get_force(lbm_ctx *ctx, float host_out[3]);
+
+/* ---------------------------------------------------------------- stepping */
+/* Advance nsteps fused time steps (one read and one write of the populations per step). */
+LBM_API lbm_status lbm_step(lbm_ctx *ctx, int32_t nsteps);
+/* D3Q27_REF: one separate pass (LBM_OP_*), as the reference's Lattice::simulate* methods. */
+LBM_API lbm_status lbm_apply(lbm_ctx *ctx, int32_t op);
+
+/* ---------------------------------------------------------------- results */
+/* Density and velocity per cell (host arrays of cells floats, any may be NULL).
+ * D2Q9: moments of the streamed populations with the half-force shift (solid cells: rho = 1,
+ * u = 0).  D3Q27_REF: density and the reference's SPLIT-weighted velocity of the stored
+ * populations (SimCalcFuncs.cu:107-120). */
+LBM_API lbm_status lbm_moments(lbm_ctx *ctx, float *host_rho, float *host_ux, float *host_uy,
+                               float *host_uz);
+/* FP64 sums over non-solid cells of the stored populations: mass, momentum x, y, z. */
+LBM_API lbm_status lbm_conservation(lbm_ctx *ctx, double host_out[4]);
+
+/* ---------------------------------------------------------------- seeded geometry generators */
+/* Channel of nx x ny: walls on rows 0 and ny-1, ndisks non-overlapping disks (x-periodic
+ * distance), centres uniform in [0,nx) x [0,ny), radius uniform in [rmin, rmax]; a cell is
+ * solid when its centre (x+0.5, y+0.5) lies inside a disk.  Returns the disks placed as
+ * (cx, cy, r) triples in host_disks (may be NULL, else room for 3*ndisks floats). */
+LBM_API lbm_status lbm_gen_channel(int32_t nx, int32_t ny, int32_t ndisks, float rmin, float rmax,
+                                   uint64_t seed, uint8_t *host_flags, float *host_disks);
+/* Lid-driven cavity: moving lid on row ny-1, walls on row 0 and columns 0 and nx-1. */
+LBM_API lbm_status lbm_gen_cavity(int32_t nx, int32_t ny, uint8_t *host_flags);
+/* Random disks (radius in [rmin, rmax], overlap allowed) added until at least solid_fraction of
+ * the cells are solid; existing flags are kept.  Returns the achieved fraction. */
+LBM_API lbm_status lbm_gen_disks_fraction(int32_t nx, int32_t ny, float solid_fraction, float rmin,
+                                          float rmax, uint64_t seed, uint8_t *host_flags,
+                                          float *achieved);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBM_CAPI_H */

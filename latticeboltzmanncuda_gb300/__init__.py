@@ -1,0 +1,219 @@
+"""GB300-native lattice Boltzmann collide-stream step.
+
+The compute path is liblbm_gb300.so (hand-written sm_103a CUDA kernels behind the C ABI of
+include/lbm_capi.h).  This package is the Python host side over that ABI: ``Lattice`` owns one
+library context; the generators produce seeded flag masks.  A C++ layer with the reference's own
+class names (Lattice, RunCudaFunctions, ... of simulation/include) sits on the same ABI in
+``simulation/``.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import capi
+from .capi import (BF16S, D2Q9, D3Q27_REF, F16S, F32, F64, FLUID, FORCE_MOMENTUM_EXCHANGE,
+                   FORCE_REFERENCE, INTERNAL, LATTICE_POINT, MOVING_WALL, OP_COLLIDE, OP_FLOW,
+                   OP_REFLECT, OP_STREAM, ORDER_CLI, ORDER_STREAM_COLLIDE, REFLECTED,
+                   REFLECTION_VALUES, SOURCE, WALL, LBMError, check, ptr)
+
+__all__ = ["Lattice", "gen_channel", "gen_cavity", "gen_disks_fraction", "LBMError", "capi"]
+
+
+def _mode(mode):
+    return capi.MODES[mode] if isinstance(mode, str) else int(mode)
+
+
+def _dtype(dtype):
+    return capi.DTYPES[dtype] if isinstance(dtype, str) else int(dtype)
+
+
+class Lattice:
+    """One library context: a D2Q9 domain or a D3Q27_REF lattice resident on one GPU."""
+
+    def __init__(self, nx, ny, nz=1, *, mode="d2q9", dtype="f32", tau=1.0, periodic=0,
+                 body_force=(0.0, 0.0, 0.0), wall_velocity=(0.0, 0.0, 0.0), order=ORDER_STREAM_COLLIDE,
+                 force_mode=FORCE_REFERENCE, device=0, stream=None):
+        L = capi.lib()
+        d = capi.Desc()
+        L.lbm_desc_init(ctypes.byref(d))
+        d.mode, d.dtype = _mode(mode), _dtype(dtype)
+        d.nx, d.ny, d.nz = int(nx), int(ny), int(nz)
+        d.periodic = int(periodic)
+        d.tau = float(tau)
+        for k in range(3):
+            d.body_force[k] = float(body_force[k]) if k < len(body_force) else 0.0
+            d.wall_velocity[k] = float(wall_velocity[k]) if k < len(wall_velocity) else 0.0
+        d.order, d.force_mode, d.device = int(order), int(force_mode), int(device)
+        d.stream = stream
+        self.desc = d
+        self._ctx = ctypes.c_void_p()
+        check(L.lbm_create(ctypes.byref(d), ctypes.byref(self._ctx)))
+        self.mode = d.mode
+        self.shape = (int(nx), int(ny), int(nz))
+        self.cells = int(nx) * int(ny) * int(nz)
+        self.q = 9 if d.mode == D2Q9 else 27
+
+    # ------------------------------------------------------------------ life cycle
+    def close(self):
+        if getattr(self, "_ctx", None) and self._ctx.value:
+            capi.lib().lbm_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _call(self, name, *args):
+        check(getattr(capi.lib(), name)(self._ctx, *args), self._ctx)
+
+    @property
+    def handle(self):
+        return self._ctx
+
+    def info(self) -> dict:
+        i = capi.Info()
+        self._call("lbm_get_info", ctypes.byref(i))
+        return {k: getattr(i, k) for k, _ in capi.Info._fields_}
+
+    @property
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        self._call("lbm_get_stream", ctypes.byref(s))
+        return s.value or 0
+
+    def synchronize(self):
+        self._call("lbm_synchronize")
+
+    def set_params(self, tau, body_force=None, wall_velocity=None):
+        bf = None if body_force is None else np.array(list(body_force) + [0.0] * (3 - len(body_force)), np.float32)
+        wv = None if wall_velocity is None else np.array(list(wall_velocity) + [0.0] * (3 - len(wall_velocity)), np.float32)
+        self._call("lbm_set_params", float(tau), ptr(bf), ptr(wv))
+
+    # ------------------------------------------------------------------ geometry and state
+    def _host_shape(self):
+        nx, ny, nz = self.shape
+        return (ny, nx) if self.mode == D2Q9 else (self.cells,)
+
+    def set_flags(self, flags):
+        a = np.ascontiguousarray(flags, dtype=np.uint8).reshape(-1)
+        if a.size != self.cells:
+            raise LBMError(capi.ERR_INVALID, f"flags need {self.cells} cells, got {a.size}")
+        self._call("lbm_set_flags", ptr(a))
+
+    def get_flags(self):
+        a = np.empty(self.cells, np.uint8)
+        self._call("lbm_get_flags", ptr(a))
+        return a.reshape(self._host_shape())
+
+    def init_equilibrium(self, rho=None, ux=None, uy=None):
+        arrs = [None if v is None else np.ascontiguousarray(v, dtype=np.float32).reshape(-1) for v in (rho, ux, uy)]
+        for v in arrs:
+            if v is not None and v.size != self.cells:
+                raise LBMError(capi.ERR_INVALID, "field size mismatch")
+        self._call("lbm_init_equilibrium", *[ptr(v) for v in arrs])
+
+    def _pop_shape(self):
+        nx, ny, nz = self.shape
+        return (9, ny, nx) if self.mode == D2Q9 else (self.cells, 27)
+
+    def load_populations(self, f):
+        f = np.asarray(f)
+        dt = F64 if f.dtype == np.float64 else F32
+        a = np.ascontiguousarray(f, dtype=np.float64 if dt == F64 else np.float32)
+        if a.size != self.cells * self.q:
+            raise LBMError(capi.ERR_INVALID, f"populations need {self.cells * self.q} values, got {a.size}")
+        self._call("lbm_load_populations", ptr(a), dt)
+
+    def retrieve_populations(self, dtype=np.float32, out=None):
+        dtype = np.dtype(dtype)
+        a = np.empty(self._pop_shape(), dtype) if out is None else out
+        self._call("lbm_retrieve_populations", ptr(a), F64 if dtype == np.float64 else F32)
+        return a
+
+    def load_aos(self, points):
+        a = np.ascontiguousarray(points, dtype=LATTICE_POINT)
+        self._call("lbm_load_aos", ptr(a), int(a.size))
+
+    def retrieve_aos(self):
+        a = np.zeros(self.cells, LATTICE_POINT)
+        self._call("lbm_retrieve_aos", ptr(a), int(a.size))
+        return a
+
+    def set_reflection_tables(self, cells, records):
+        c = np.ascontiguousarray(cells, dtype=np.int32)
+        r = np.ascontiguousarray(records, dtype=REFLECTION_VALUES)
+        self._call("lbm_set_reflection_tables", int(c.size), ptr(c), ptr(r))
+
+    def set_flow(self, mask=None, induced=None):
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8).reshape(-1)
+        i = None if induced is None else np.ascontiguousarray(induced, dtype=np.float32)
+        self._call("lbm_set_flow", ptr(m), ptr(i))
+
+    def set_force(self, value=(0.0, 0.0, 0.0), enabled=True):
+        v = np.ascontiguousarray(value, dtype=np.float32)
+        self._call("lbm_set_force", ptr(v), int(bool(enabled)))
+
+    def get_force(self):
+        v = np.zeros(3, np.float32)
+        self._call("lbm_get_force", ptr(v))
+        return v
+
+    # ------------------------------------------------------------------ stepping
+    def step(self, n=1):
+        self._call("lbm_step", int(n))
+
+    def apply(self, op):
+        self._call("lbm_apply", int(op))
+
+    # ------------------------------------------------------------------ results
+    def moments(self, out=None):
+        """(rho, ux, uy) for D2Q9, (rho, ux, uy, uz) for D3Q27_REF; `out` may give float32 arrays
+        (for example pinned host memory) to write into."""
+        shp = self._host_shape()
+        n = 4 if self.mode == D3Q27_REF else 3
+        if out is None:
+            out = [np.empty(shp, np.float32) for _ in range(n)]
+        for o in out:
+            if o is not None and (o.dtype != np.float32 or o.size != self.cells or not o.flags.c_contiguous):
+                raise LBMError(capi.ERR_INVALID, "moment outputs must be contiguous float32 arrays of one value per cell")
+        args = [ptr(o) for o in out] + [None] * (4 - len(out))
+        self._call("lbm_moments", *args)
+        return tuple(out)
+
+    def conservation(self):
+        out = np.zeros(4, np.float64)
+        self._call("lbm_conservation", ptr(out))
+        return out
+
+
+def gen_channel(nx, ny, ndisks, rmin, rmax, seed):
+    flags = np.empty((ny, nx), np.uint8)
+    disks = np.empty((max(ndisks, 1), 3), np.float32)
+    check(capi.lib().lbm_gen_channel(int(nx), int(ny), int(ndisks), float(rmin), float(rmax),
+                                     ctypes.c_uint64(int(seed)), ptr(flags), ptr(disks)))
+    return flags, disks[:ndisks]
+
+
+def gen_cavity(nx, ny):
+    flags = np.empty((ny, nx), np.uint8)
+    check(capi.lib().lbm_gen_cavity(int(nx), int(ny), ptr(flags)))
+    return flags
+
+
+def gen_disks_fraction(flags, solid_fraction, rmin, rmax, seed):
+    flags = np.ascontiguousarray(flags, dtype=np.uint8).copy()
+    ny, nx = flags.shape
+    ach = ctypes.c_float()
+    check(capi.lib().lbm_gen_disks_fraction(int(nx), int(ny), float(solid_fraction), float(rmin), float(rmax),
+                                            ctypes.c_uint64(int(seed)), ptr(flags), ctypes.byref(ach)))
+    return flags, float(ach.value)

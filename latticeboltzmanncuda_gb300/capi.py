@@ -1,0 +1,133 @@
+"""ctypes binding of the C ABI (include/lbm_capi.h) over liblbm_gb300.so.
+
+Every call goes through the C ABI; there is no other code path.  If the library cannot be loaded
+the import of this module's ``lib()`` raises: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "liblbm_gb300.so")
+
+# enums (lbm_capi.h)
+OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_UNSUPPORTED, ERR_STATE, ERR_BUDGET, ERR_TIMEOUT = range(8)
+D2Q9, D3Q27_REF = 0, 1
+F32, F16S, BF16S, F64 = 0, 1, 2, 3
+FLUID, WALL, MOVING_WALL = 0, 1, 2
+INTERNAL, REFLECTED, SOURCE = 1, 2, 4
+ORDER_STREAM_COLLIDE, ORDER_CLI = 0, 1
+OP_STREAM, OP_REFLECT, OP_COLLIDE, OP_FLOW = 1, 2, 4, 8
+FORCE_REFERENCE, FORCE_MOMENTUM_EXCHANGE = 0, 1
+
+DTYPES = {"f32": F32, "f16s": F16S, "bf16s": BF16S, "f64": F64}
+MODES = {"d2q9": D2Q9, "d3q27_ref": D3Q27_REF}
+
+# struct LatticePoint (LatticePoint.h:9-17), 144 bytes
+LATTICE_POINT = np.dtype({
+    "names": ["x", "y", "z", "f", "isReflected", "isInternal", "reflections", "d_reflections"],
+    "formats": [np.int32, np.int32, np.int32, (np.float32, (27,)), np.bool_, np.bool_, np.uint64, np.uint64],
+    "offsets": [0, 4, 8, 12, 120, 121, 128, 136],
+    "itemsize": 144,
+})
+# struct ReflectionValues (LatticePoint.h:3-7), 380 bytes
+REFLECTION_VALUES = np.dtype([("dirs", np.int32, (14,)), ("w", np.float32, (81,))])
+assert REFLECTION_VALUES.itemsize == 380
+
+# D2Q9 population order used by the library
+CX9 = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1], dtype=np.int32)
+CY9 = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1], dtype=np.int32)
+W9 = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
+AOS_SLOTS_D2Q9 = np.array([0, 6, 5, 1, 2, 18, 10, 7, 15], dtype=np.int32)
+
+
+class Desc(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int32), ("dtype", ctypes.c_int32), ("nx", ctypes.c_int32),
+                ("ny", ctypes.c_int32), ("nz", ctypes.c_int32), ("periodic", ctypes.c_int32),
+                ("tau", ctypes.c_float), ("body_force", ctypes.c_float * 3),
+                ("wall_velocity", ctypes.c_float * 3), ("order", ctypes.c_int32),
+                ("force_mode", ctypes.c_int32), ("device", ctypes.c_int32), ("stream", ctypes.c_void_p)]
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("cells", ctypes.c_int64), ("fluid_cells", ctypes.c_int64), ("row_pitch", ctypes.c_int64),
+                ("state_bytes", ctypes.c_int64), ("device_bytes", ctypes.c_int64),
+                ("bytes_per_update", ctypes.c_int64), ("steps_done", ctypes.c_int64),
+                ("block_threads", ctypes.c_int32), ("cells_per_thread", ctypes.c_int32)]
+
+
+# exported symbols and their signatures: (name, restype, argtypes)
+_P, _I32, _I64, _U64, _F = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64, ctypes.c_float
+_S = ctypes.c_int
+SIGNATURES = [
+    ("lbm_desc_init", None, [_P]),
+    ("lbm_create", _S, [_P, _P]),
+    ("lbm_destroy", _S, [_P]),
+    ("lbm_last_error", ctypes.c_char_p, [_P]),
+    ("lbm_status_string", ctypes.c_char_p, [_S]),
+    ("lbm_get_info", _S, [_P, _P]),
+    ("lbm_get_stream", _S, [_P, _P]),
+    ("lbm_synchronize", _S, [_P]),
+    ("lbm_set_params", _S, [_P, _F, _P, _P]),
+    ("lbm_set_flags", _S, [_P, _P]),
+    ("lbm_get_flags", _S, [_P, _P]),
+    ("lbm_init_equilibrium", _S, [_P, _P, _P, _P]),
+    ("lbm_load_populations", _S, [_P, _P, _I32]),
+    ("lbm_retrieve_populations", _S, [_P, _P, _I32]),
+    ("lbm_load_aos", _S, [_P, _P, _I64]),
+    ("lbm_retrieve_aos", _S, [_P, _P, _I64]),
+    ("lbm_set_reflection_tables", _S, [_P, _I64, _P, _P]),
+    ("lbm_set_flow", _S, [_P, _P, _P]),
+    ("lbm_set_force", _S, [_P, _P, _I32]),
+    ("lbm_get_force", _S, [_P, _P]),
+    ("lbm_step", _S, [_P, _I32]),
+    ("lbm_apply", _S, [_P, _I32]),
+    ("lbm_moments", _S, [_P, _P, _P, _P, _P]),
+    ("lbm_conservation", _S, [_P, _P]),
+    ("lbm_gen_channel", _S, [_I32, _I32, _I32, _F, _F, _U64, _P, _P]),
+    ("lbm_gen_cavity", _S, [_I32, _I32, _P]),
+    ("lbm_gen_disks_fraction", _S, [_I32, _I32, _F, _F, _F, _U64, _P, _P]),
+]
+
+_lib = None
+
+
+class LBMError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+def lib(build: bool = True):
+    """Load liblbm_gb300.so (building it with nvcc first when it is missing or stale)."""
+    global _lib
+    if _lib is None:
+        if build:
+            from . import build as _b
+            _b.build()
+        if not os.path.exists(LIB_PATH):
+            raise LBMError(ERR_STATE, f"{LIB_PATH} is missing: build it with python -m latticeboltzmanncuda_gb300.build")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def ptr(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def check(status, ctx=None):
+    if status != OK:
+        msg = lib().lbm_last_error(ctx)
+        raise LBMError(status, (msg or b"").decode() or lib().lbm_status_string(status).decode())
+
+
+def last_thread_error() -> str:
+    return (lib().lbm_last_error(None) or b"").decode()

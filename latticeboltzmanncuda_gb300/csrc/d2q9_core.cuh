@@ -1,0 +1,163 @@
+// D2Q9 device building blocks shared by the single-domain and the batched kernels.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "lbm_internal.h"
+
+namespace lbm {
+namespace d2q9 {
+
+// population order: 0:(0,0) 1:(1,0) 2:(0,1) 3:(-1,0) 4:(0,-1) 5:(1,1) 6:(-1,1) 7:(-1,-1) 8:(1,-1)
+__host__ __device__ constexpr int cx(int q) { return q == 1 || q == 5 || q == 8 ? 1 : (q == 3 || q == 6 || q == 7 ? -1 : 0); }
+__host__ __device__ constexpr int cy(int q) { return q == 2 || q == 5 || q == 6 ? 1 : (q == 4 || q == 7 || q == 8 ? -1 : 0); }
+__host__ __device__ constexpr int opp(int q) { return q == 0 ? 0 : (q < 5 ? ((q + 1) & 3) + 1 : ((q - 3) & 3) + 5); }
+template <class R>
+__host__ __device__ constexpr R w(int q) {
+    return q == 0 ? (R)(4.0 / 9.0) : (q < 5 ? (R)(1.0 / 9.0) : (R)(1.0 / 36.0));
+}
+
+static_assert(opp(1) == 3 && opp(2) == 4 && opp(3) == 1 && opp(4) == 2, "opp faces");
+static_assert(opp(5) == 7 && opp(6) == 8 && opp(7) == 5 && opp(8) == 6, "opp diagonals");
+
+template <class R>
+struct Vec2 {
+    R x, y;
+};
+
+// storage traits: S is the stored type, R the arithmetic type
+template <class S>
+struct Store;
+template <>
+struct Store<float> {
+    using R = float;
+    static __device__ __forceinline__ R ld(const float *p) { return __ldg(p); }
+    static __device__ __forceinline__ void st(float *p, R v) { *p = v; }
+};
+template <>
+struct Store<double> {
+    using R = double;
+    static __device__ __forceinline__ R ld(const double *p) { return __ldg(p); }
+    static __device__ __forceinline__ void st(double *p, R v) { *p = v; }
+};
+template <>
+struct Store<__half> {
+    using R = float;
+    static __device__ __forceinline__ R ld(const __half *p) { return __half2float(__ldg(p)); }
+    static __device__ __forceinline__ void st(__half *p, R v) { *p = __float2half_rn(v); }
+};
+template <>
+struct Store<__nv_bfloat16> {
+    using R = float;
+    static __device__ __forceinline__ R ld(const __nv_bfloat16 *p) { return __bfloat162float(__ldg(p)); }
+    static __device__ __forceinline__ void st(__nv_bfloat16 *p, R v) { *p = __float2bfloat16_rn(v); }
+};
+
+template <class R, class P>
+__device__ __forceinline__ R omega(const P &p);
+template <>
+__device__ __forceinline__ float omega<float>(const lbm::D2Q9Params &p) { return p.omega; }
+template <>
+__device__ __forceinline__ double omega<double>(const lbm::D2Q9Params &p) { return p.omega_d; }
+template <class R, class P>
+__device__ __forceinline__ Vec2<R> force(const P &p);
+template <>
+__device__ __forceinline__ Vec2<float> force<float>(const lbm::D2Q9Params &p) { return {p.fx, p.fy}; }
+template <>
+__device__ __forceinline__ Vec2<double> force<double>(const lbm::D2Q9Params &p) { return {p.fx_d, p.fy_d}; }
+template <class R, class P>
+__device__ __forceinline__ Vec2<R> wall_u(const P &p);
+template <>
+__device__ __forceinline__ Vec2<float> wall_u<float>(const lbm::D2Q9Params &p) { return {p.uwx, p.uwy}; }
+template <>
+__device__ __forceinline__ Vec2<double> wall_u<double>(const lbm::D2Q9Params &p) { return {p.uwx_d, p.uwy_d}; }
+
+// Streamed populations of fluid cell (x, y): population q is pulled from (x - cx_q, y - cy_q)
+// (periodic wrap, or clamped when the link bit says the value is not used), and replaced by the
+// half-way bounce-back of the cell's own opposite population when link bit q-1 is set, plus the
+// moving-wall term 6 w_q (c_q . u_w) when bit q+7 is set.
+template <class S, class R>
+__device__ __forceinline__ void gather(const S *__restrict__ src, uint32_t L, int x, int y, int nx, int ny,
+                                       int64_t pitch, int64_t plane, int periodic, Vec2<R> uw, R g[9]) {
+    int xm = x - 1, xp = x + 1, ym = y - 1, yp = y + 1;
+    if (xm < 0) xm = (periodic & 1) ? nx - 1 : 0;
+    if (xp >= nx) xp = (periodic & 1) ? 0 : nx - 1;
+    if (ym < 0) ym = (periodic & 2) ? ny - 1 : 0;
+    if (yp >= ny) yp = (periodic & 2) ? 0 : ny - 1;
+    const int64_t r0 = (int64_t)y * pitch, rm = (int64_t)ym * pitch, rp = (int64_t)yp * pitch;
+    g[0] = Store<S>::ld(src + r0 + x);
+    g[1] = Store<S>::ld(src + 1 * plane + r0 + xm);
+    g[2] = Store<S>::ld(src + 2 * plane + rm + x);
+    g[3] = Store<S>::ld(src + 3 * plane + r0 + xp);
+    g[4] = Store<S>::ld(src + 4 * plane + rp + x);
+    g[5] = Store<S>::ld(src + 5 * plane + rm + xm);
+    g[6] = Store<S>::ld(src + 6 * plane + rm + xp);
+    g[7] = Store<S>::ld(src + 7 * plane + rp + xp);
+    g[8] = Store<S>::ld(src + 8 * plane + rp + xm);
+    if (L) {
+#pragma unroll
+        for (int q = 1; q < 9; ++q) {
+            if (L & (1u << (q - 1))) {
+                R v = Store<S>::ld(src + opp(q) * plane + r0 + x);
+                if (L & (1u << (q + 7))) v += (R)6 * w<R>(q) * ((R)cx(q) * uw.x + (R)cy(q) * uw.y);
+                g[q] = v;
+            }
+        }
+    }
+}
+
+template <class R>
+__device__ __forceinline__ void moments(const R g[9], R &drho, R &mx, R &my) {
+    drho = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
+    mx = (g[1] - g[3]) + (g[5] - g[6]) + (g[8] - g[7]);
+    my = (g[2] - g[4]) + (g[5] + g[6]) - (g[7] + g[8]);
+}
+
+// shifted equilibrium geq_q = feq_q - w_q = w_q (drho + rho (3 cu + 4.5 cu^2 - 1.5 u^2))
+template <class R>
+__device__ __forceinline__ void equilibrium_shifted(R drho, R rho, R ux, R uy, R g[9]) {
+    const R usq = (R)1.5 * (ux * ux + uy * uy);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const R cu = (R)cx(q) * ux + (R)cy(q) * uy;
+        g[q] = w<R>(q) * (drho + rho * ((R)3 * cu + (R)4.5 * cu * cu - usq));
+    }
+}
+
+// BGK collision with Guo forcing on shifted populations, in place
+template <class R, bool FORCE>
+__device__ __forceinline__ void collide(R g[9], R om, Vec2<R> F) {
+    R drho, mx, my;
+    moments(g, drho, mx, my);
+    const R rho = (R)1 + drho;
+    const R inv = (R)1 / rho;
+    R ux, uy;
+    if (FORCE) {
+        ux = (mx + (R)0.5 * F.x) * inv;
+        uy = (my + (R)0.5 * F.y) * inv;
+    } else {
+        ux = mx * inv;
+        uy = my * inv;
+    }
+    const R usq = (R)1.5 * (ux * ux + uy * uy);
+    const R pre = (R)1 - (R)0.5 * om;
+    const R uF = ux * F.x + uy * F.y;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const R cu = (R)cx(q) * ux + (R)cy(q) * uy;
+        const R geq = w<R>(q) * (drho + rho * ((R)3 * cu + (R)4.5 * cu * cu - usq));
+        R v = g[q] + om * (geq - g[q]);
+        if (FORCE) {
+            const R cF = (R)cx(q) * F.x + (R)cy(q) * F.y;
+            v += pre * w<R>(q) * ((R)3 * (cF - uF) + (R)9 * cu * cF);
+        }
+        g[q] = v;
+    }
+}
+
+}  // namespace d2q9
+}  // namespace lbm

@@ -1,0 +1,450 @@
+// D3Q27_REF kernels: the reference's step (simulation/source/SimCalcFuncs.cu) re-designed as
+// structure-of-arrays passes.
+//
+// State: f[q * cells + cell], q in the reference's particle_distribution order, cell index
+// z + Z*(y + Y*x) (Lattice.cpp:254).  FP32 populations; the equilibrium is evaluated in FP64 and
+// rounded to FP32, as the reference's double literals make it (SimCalcFuncs.cu:125-154).
+//
+// The reference runs four kernels per CLI step with a full-lattice malloc + device copy before the
+// streaming and reflection kernels (Lattice.cpp:115-210) and float atomics on every population.
+// Here one step is one pass over the populations (one read, one write):
+//   fused_kernel   all cells that receive no reflection: zero-fill pull streaming, zeroing of
+//                  internal cells, collision, flow source.
+//   gather_kernel  the (few) fluid cells next to reflecting cells: the same, plus the reflected
+//                  populations pulled through precomputed gather lists (the reference's atomic
+//                  scatter of SimCalcFuncs.cu:164-186 turned into a pull with a fixed order), plus
+//                  the momentum-exchange force reduced per block without atomics.
+// lbm_apply() runs the reference's single passes (stream / reflect / collide / flow) separately.
+#include <cuda_runtime.h>
+
+#include "lbm_internal.h"
+#include "reduce.cuh"
+
+namespace lbm {
+namespace {
+
+constexpr uint8_t F_INTERNAL = LBM_INTERNAL, F_SOURCE = LBM_SOURCE;
+constexpr uint8_t F_GATHER = 8;  // cell receives reflected populations (set by the library)
+
+// SimCalcFuncs.cu:12-14
+__constant__ int c_dir[27][3] = {
+    {0, 0, 0},   {-1, 0, 0},  {0, -1, 0},  {0, 0, -1},  {0, 0, 1},    {0, 1, 0},    {1, 0, 0},
+    {-1, -1, 0}, {-1, 0, -1}, {-1, 0, 1},  {-1, 1, 0},  {0, -1, -1},  {0, -1, 1},   {0, 1, -1},
+    {0, 1, 1},   {1, -1, 0},  {1, 0, -1},  {1, 0, 1},   {1, 1, 0},    {-1, -1, -1}, {-1, -1, 1},
+    {-1, 1, -1}, {-1, 1, 1},  {1, -1, -1}, {1, -1, 1},  {1, 1, -1},   {1, 1, 1}};
+__constant__ float c_split[27] = {0.0f,        1.0f,        1.0f,        1.0f,        1.0f,        1.0f,
+                                  1.0f,        0.5f,        0.5f,        0.5f,        0.5f,        0.5f,
+                                  0.5f,        0.5f,        0.5f,        0.5f,        0.5f,        0.5f,
+                                  0.5f,        1.0f / 3.0f, 1.0f / 3.0f, 1.0f / 3.0f, 1.0f / 3.0f, 1.0f / 3.0f,
+                                  1.0f / 3.0f, 1.0f / 3.0f, 1.0f / 3.0f};
+
+struct Dims {
+    int X, Y, Z;
+    int64_t n;
+};
+
+__device__ __forceinline__ void decode(const Dims &d, int64_t c, int &x, int &y, int &z) {
+    z = (int)(c % d.Z);
+    int64_t t = c / d.Z;
+    y = (int)(t % d.Y);
+    x = (int)(t / d.Y);
+}
+
+// pull streaming with zero fill (SimCalcFuncs.cu:79-96): v[j] = f_j(x - c_j), 0 outside
+__device__ __forceinline__ void pull(const float *__restrict__ src, const Dims &d, int64_t c, int x, int y, int z,
+                                     float v[27]) {
+#pragma unroll
+    for (int j = 0; j < 27; ++j) {
+        const int sx = x - c_dir[j][0], sy = y - c_dir[j][1], sz = z - c_dir[j][2];
+        const bool in = sx >= 0 && sy >= 0 && sz >= 0 && sx < d.X && sy < d.Y && sz < d.Z;
+        const int64_t s = c - (int64_t)c_dir[j][2] - (int64_t)d.Z * ((int64_t)c_dir[j][1] + (int64_t)d.Y * c_dir[j][0]);
+        v[j] = in ? __ldg(src + (int64_t)j * d.n + s) : 0.0f;
+    }
+}
+
+// calculate_collision (SimCalcFuncs.cu:98-156): FP32 density and SPLIT-weighted velocity, FP64
+// equilibrium rounded to FP32, f += (eq - f) / tau in FP32.
+__device__ __forceinline__ void collide(float v[27], float tau) {
+    float density = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 27; ++i) {
+        density += v[i];
+        ux += v[i] * (float)c_dir[i][0] * c_split[i];
+        uy += v[i] * (float)c_dir[i][1] * c_split[i];
+        uz += v[i] * (float)c_dir[i][2] * c_split[i];
+    }
+    if (density != 0.0f) {
+        ux /= density;
+        uy /= density;
+        uz /= density;
+    }
+    const float usq = (ux * ux) + (uy * uy) + (uz * uz);
+#pragma unroll
+    for (int i = 0; i < 27; ++i) {
+        const double wgt = i == 0 ? (8.0 / 27.0) : (i < 7 ? (2.0 / 27.0) : (i < 19 ? (1.0 / 54.0) : (1.0 / 216.0)));
+        const float ct = ((float)c_dir[i][0] * ux) + ((float)c_dir[i][1] * uy) + ((float)c_dir[i][2] * uz);
+        const float eq = (float)(wgt * density * (1 + (3.0 * ct) + (4.5 * ct * ct) - (1.5 * usq)));
+        v[i] = v[i] + (eq - v[i]) / tau;
+    }
+}
+
+struct StepArgs {
+    const float *src;
+    float *dst;
+    const uint8_t *flags;
+    Dims d;
+    float tau;
+    const float *induced;  // nullptr: no flow
+    int cli;               // 1: stream, reflect, collide, flow; 0: stream, collide
+};
+
+__global__ void __launch_bounds__(256) fused_kernel(StepArgs a) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= a.d.n) return;
+    const uint8_t fl = a.flags[c];
+    if (a.cli && (fl & F_GATHER)) return;  // written by gather_kernel
+    int x, y, z;
+    decode(a.d, c, x, y, z);
+    float v[27];
+    pull(a.src, a.d, c, x, y, z, v);
+    if (a.cli && (fl & F_INTERNAL)) {
+#pragma unroll
+        for (int j = 0; j < 27; ++j) v[j] = 0.0f;
+    }
+    collide(v, a.tau);
+    if (a.cli && a.induced && (fl & F_SOURCE)) {
+#pragma unroll
+        for (int j = 0; j < 27; ++j) v[j] = v[j] + __ldg(a.induced + j);
+    }
+#pragma unroll
+    for (int j = 0; j < 27; ++j) a.dst[(int64_t)j * a.d.n + c] = v[j];
+}
+
+struct GatherArgs {
+    const int32_t *tgt;
+    const int32_t *off;
+    const GatherEntry *ent;
+    int64_t ntgt;
+    double *partials;  // 3 per block, or nullptr when no force is accumulated
+    int force_mode;
+};
+
+// force contribution m * (c_d SPLIT[d] - c_k SPLIT[k]) (SimCalcFuncs.cu:181-183)
+__device__ __forceinline__ void force_term(float m, const GatherEntry &e, int mode, double acc[3]) {
+    const int k = mode == LBM_FORCE_MOMENTUM_EXCHANGE ? e.slot / 3 : e.slot;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float kin = k < 27 ? (float)c_dir[k][a] * c_split[k] : 0.0f;
+        const float coef = ((float)c_dir[e.dst_pop][a] * c_split[e.dst_pop]) - kin;
+        acc[a] += (double)(m * coef);
+    }
+}
+
+// mode 0: fused step (values of the reflecting cells are their streamed populations);
+// mode 1: the reference's separate reflection pass (values read in place, no collision).
+template <int MODE>
+__global__ void __launch_bounds__(128) gather_kernel(StepArgs a, GatherArgs g) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double facc[3] = {0.0, 0.0, 0.0};
+    if (i < g.ntgt) {
+        const int64_t c = g.tgt[i];
+        const uint8_t fl = a.flags[c];
+        float v[27];
+        if (MODE == 0) {
+            int x, y, z;
+            decode(a.d, c, x, y, z);
+            pull(a.src, a.d, c, x, y, z, v);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 27; ++j) v[j] = __ldg(a.src + (int64_t)j * a.d.n + c);
+        }
+        for (int k = g.off[i]; k < g.off[i + 1]; ++k) {
+            const GatherEntry e = g.ent[k];
+            const int64_t s = MODE == 0 ? (int64_t)e.src_stream : (int64_t)e.src_cell;
+            const float val = s >= 0 ? __ldg(a.src + (int64_t)e.src_pop * a.d.n + s) : 0.0f;
+            const float m = val * e.w;
+            // v[e.dst_pop] += m, one add per contribution as the reference's atomicAdd
+            // (SimCalcFuncs.cu:177), selected over the register-resident array
+#pragma unroll
+            for (int j = 1; j < 27; ++j)
+                if (j == e.dst_pop) v[j] = v[j] + m;
+            if (g.partials) force_term(m, e, g.force_mode, facc);
+        }
+        if (fl & F_INTERNAL) {
+#pragma unroll
+            for (int j = 0; j < 27; ++j) v[j] = 0.0f;
+        }
+        if (MODE == 0) {
+            collide(v, a.tau);
+            if (a.induced && (fl & F_SOURCE)) {
+#pragma unroll
+                for (int j = 0; j < 27; ++j) v[j] = v[j] + __ldg(a.induced + j);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 27; ++j) a.dst[(int64_t)j * a.d.n + c] = v[j];
+    }
+    if (g.partials) block_sum<3>(facc, g.partials + 3 * blockIdx.x);
+}
+
+// ------------------------------------------------------------------------- separate passes
+__global__ void stream_kernel(const float *__restrict__ src, float *__restrict__ dst, Dims d) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= d.n) return;
+    int x, y, z;
+    decode(d, c, x, y, z);
+    float v[27];
+    pull(src, d, c, x, y, z, v);
+#pragma unroll
+    for (int j = 0; j < 27; ++j) dst[(int64_t)j * d.n + c] = v[j];
+}
+
+// reflection pass for cells that receive nothing: copy, internal cells zeroed
+__global__ void reflect_copy_kernel(const float *__restrict__ src, float *__restrict__ dst,
+                                    const uint8_t *__restrict__ flags, Dims d) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= d.n) return;
+    const uint8_t fl = flags[c];
+    if (fl & F_GATHER) return;
+    const bool zero = fl & F_INTERNAL;
+#pragma unroll
+    for (int j = 0; j < 27; ++j) dst[(int64_t)j * d.n + c] = zero ? 0.0f : __ldg(src + (int64_t)j * d.n + c);
+}
+
+__global__ void collide_kernel(float *__restrict__ f, Dims d, float tau) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= d.n) return;
+    float v[27];
+#pragma unroll
+    for (int j = 0; j < 27; ++j) v[j] = f[(int64_t)j * d.n + c];
+    collide(v, tau);
+#pragma unroll
+    for (int j = 0; j < 27; ++j) f[(int64_t)j * d.n + c] = v[j];
+}
+
+__global__ void flow_kernel(float *__restrict__ f, const uint8_t *__restrict__ flags, Dims d,
+                            const float *__restrict__ induced) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= d.n || !(flags[c] & F_SOURCE)) return;
+#pragma unroll
+    for (int j = 0; j < 27; ++j) f[(int64_t)j * d.n + c] = f[(int64_t)j * d.n + c] + induced[j];
+}
+
+// ------------------------------------------------------------------------- results and I/O
+__global__ void moments_kernel(const float *__restrict__ f, Dims d, float *rho, float *ux, float *uy, float *uz) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= d.n) return;
+    float density = 0.0f, vx = 0.0f, vy = 0.0f, vz = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 27; ++i) {
+        const float v = f[(int64_t)i * d.n + c];
+        density += v;
+        vx += v * (float)c_dir[i][0] * c_split[i];
+        vy += v * (float)c_dir[i][1] * c_split[i];
+        vz += v * (float)c_dir[i][2] * c_split[i];
+    }
+    if (density != 0.0f) {
+        vx /= density;
+        vy /= density;
+        vz /= density;
+    }
+    if (rho) rho[c] = density;
+    if (ux) ux[c] = vx;
+    if (uy) uy[c] = vy;
+    if (uz) uz[c] = vz;
+}
+
+__global__ void conservation_kernel(const float *__restrict__ f, const uint8_t *__restrict__ flags, Dims d,
+                                    double *partials) {
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < d.n; c += (int64_t)gridDim.x * blockDim.x) {
+        if (flags[c] & F_INTERNAL) continue;
+#pragma unroll
+        for (int i = 0; i < 27; ++i) {
+            const double v = f[(int64_t)i * d.n + c];
+            acc[0] += v;
+            acc[1] += v * c_dir[i][0];
+            acc[2] += v * c_dir[i][1];
+            acc[3] += v * c_dir[i][2];
+        }
+    }
+    block_sum<4>(acc, partials + 4 * blockIdx.x);
+}
+
+// host layouts: cell-major [cell][27] float/double, or LatticePoint records (144 bytes; floats
+// from byte 12, flags at 120 / 121, pointers at 128 / 136)
+template <class H>
+__global__ void load_kernel(float *__restrict__ f, const H *__restrict__ host, Dims d, int aos) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= d.n) return;
+    for (int j = 0; j < 27; ++j) {
+        float v;
+        if (aos)
+            v = reinterpret_cast<const float *>(reinterpret_cast<const char *>(host) + c * 144 + 12)[j];
+        else
+            v = (float)host[c * 27 + j];
+        f[(int64_t)j * d.n + c] = v;
+    }
+}
+
+template <class H>
+__global__ void store_kernel(const float *__restrict__ f, H *__restrict__ host, const uint8_t *__restrict__ flags,
+                             Dims d, int aos) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= d.n) return;
+    if (aos) {
+        char *rec = reinterpret_cast<char *>(host) + c * 144;
+        int x, y, z;
+        decode(d, c, x, y, z);
+        int *xyz = reinterpret_cast<int *>(rec);
+        xyz[0] = x;
+        xyz[1] = y;
+        xyz[2] = z;
+        float *p = reinterpret_cast<float *>(rec + 12);
+        for (int j = 0; j < 27; ++j) p[j] = f[(int64_t)j * d.n + c];
+        const uint8_t fl = flags[c];
+        rec[120] = (fl & LBM_REFLECTED) ? 1 : 0;
+        rec[121] = (fl & LBM_INTERNAL) ? 1 : 0;
+        rec[122] = rec[123] = 0;
+        *reinterpret_cast<int *>(rec + 124) = 0;
+        *reinterpret_cast<unsigned long long *>(rec + 128) = 0ull;
+        *reinterpret_cast<unsigned long long *>(rec + 136) = 0ull;
+    } else {
+        for (int j = 0; j < 27; ++j) host[c * 27 + j] = (H)f[(int64_t)j * d.n + c];
+    }
+}
+
+inline Dims dims(const lbm_ctx *ctx) {
+    return Dims{ctx->desc.nx, ctx->desc.ny, ctx->desc.nz, ctx->cells};
+}
+
+inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+float *cur(lbm_ctx *ctx) { return static_cast<float *>(ctx->f[ctx->cur]); }
+float *nxt(lbm_ctx *ctx) { return static_cast<float *>(ctx->f[ctx->cur ^ 1]); }
+
+GatherArgs gather_args(lbm_ctx *ctx) {
+    GatherArgs g;
+    g.tgt = ctx->tgt_cells_d;
+    g.off = ctx->tgt_off_d;
+    g.ent = ctx->entries_d;
+    g.ntgt = ctx->ntgt;
+    g.partials = ctx->force_on ? ctx->scratch.partials : nullptr;
+    g.force_mode = ctx->desc.force_mode;
+    return g;
+}
+
+cudaError_t launch_gather(lbm_ctx *ctx, const StepArgs &a, int mode) {
+    if (ctx->ntgt == 0) return cudaSuccess;
+    GatherArgs g = gather_args(ctx);
+    const int threads = 128;
+    const unsigned nb = blocks_for(ctx->ntgt, threads);
+    if (mode == 0)
+        gather_kernel<0><<<nb, threads, 0, ctx->stream>>>(a, g);
+    else
+        gather_kernel<1><<<nb, threads, 0, ctx->stream>>>(a, g);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !g.partials) return e;
+    return finalize_sums(ctx->stream, g.partials, (int)nb, 3, ctx->force_acc_d, true);
+}
+
+}  // namespace
+
+cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps) {
+    const int threads = 256;
+    for (int s = 0; s < nsteps; ++s) {
+        StepArgs a;
+        a.src = cur(ctx);
+        a.dst = nxt(ctx);
+        a.flags = ctx->flags_d;
+        a.d = dims(ctx);
+        a.tau = ctx->desc.tau;
+        a.cli = ctx->desc.order == LBM_ORDER_CLI;
+        a.induced = (a.cli && ctx->flow_on) ? ctx->induced_d : nullptr;
+        fused_kernel<<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        if (a.cli) {
+            e = launch_gather(ctx, a, 0);
+            if (e != cudaSuccess) return e;
+        }
+        ctx->cur ^= 1;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t d3q27_apply(lbm_ctx *ctx, int op) {
+    const int threads = 256;
+    const Dims d = dims(ctx);
+    const unsigned nb = blocks_for(ctx->cells, threads);
+    cudaError_t e = cudaSuccess;
+    switch (op) {
+        case LBM_OP_STREAM:
+            stream_kernel<<<nb, threads, 0, ctx->stream>>>(cur(ctx), nxt(ctx), d);
+            e = cudaGetLastError();
+            ctx->cur ^= 1;
+            break;
+        case LBM_OP_REFLECT: {
+            reflect_copy_kernel<<<nb, threads, 0, ctx->stream>>>(cur(ctx), nxt(ctx), ctx->flags_d, d);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+            StepArgs a;
+            a.src = cur(ctx);
+            a.dst = nxt(ctx);
+            a.flags = ctx->flags_d;
+            a.d = d;
+            a.tau = ctx->desc.tau;
+            a.induced = nullptr;
+            a.cli = 1;
+            e = launch_gather(ctx, a, 1);
+            ctx->cur ^= 1;
+            break;
+        }
+        case LBM_OP_COLLIDE:
+            collide_kernel<<<nb, threads, 0, ctx->stream>>>(cur(ctx), d, ctx->desc.tau);
+            e = cudaGetLastError();
+            break;
+        case LBM_OP_FLOW:
+            if (ctx->flow_on) {
+                flow_kernel<<<nb, threads, 0, ctx->stream>>>(cur(ctx), ctx->flags_d, d, ctx->induced_d);
+                e = cudaGetLastError();
+            }
+            break;
+        default:
+            return cudaErrorInvalidValue;
+    }
+    return e;
+}
+
+cudaError_t d3q27_moments(lbm_ctx *ctx, float *rho_d, float *ux_d, float *uy_d, float *uz_d) {
+    moments_kernel<<<blocks_for(ctx->cells, 256), 256, 0, ctx->stream>>>(cur(ctx), dims(ctx), rho_d, ux_d, uy_d, uz_d);
+    return cudaGetLastError();
+}
+
+cudaError_t d3q27_conservation(lbm_ctx *ctx, double *out_d) {
+    const int nblocks = 512;
+    conservation_kernel<<<nblocks, 256, 0, ctx->stream>>>(cur(ctx), ctx->flags_d, dims(ctx), ctx->scratch.partials);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return finalize_sums(ctx->stream, ctx->scratch.partials, nblocks, 4, out_d);
+}
+
+cudaError_t d3q27_load(lbm_ctx *ctx, const void *src_d, int src_dtype, int aos) {
+    const unsigned nb = blocks_for(ctx->cells, 128);
+    if (aos || src_dtype == LBM_F32)
+        load_kernel<float><<<nb, 128, 0, ctx->stream>>>(cur(ctx), static_cast<const float *>(src_d), dims(ctx), aos);
+    else
+        load_kernel<double><<<nb, 128, 0, ctx->stream>>>(cur(ctx), static_cast<const double *>(src_d), dims(ctx), 0);
+    return cudaGetLastError();
+}
+
+cudaError_t d3q27_store(lbm_ctx *ctx, void *dst_d, int dst_dtype, int aos) {
+    const unsigned nb = blocks_for(ctx->cells, 128);
+    if (aos || dst_dtype == LBM_F32)
+        store_kernel<float><<<nb, 128, 0, ctx->stream>>>(cur(ctx), static_cast<float *>(dst_d), ctx->flags_d, dims(ctx), aos);
+    else
+        store_kernel<double><<<nb, 128, 0, ctx->stream>>>(cur(ctx), static_cast<double *>(dst_d), ctx->flags_d, dims(ctx), 0);
+    return cudaGetLastError();
+}
+
+}  // namespace lbm

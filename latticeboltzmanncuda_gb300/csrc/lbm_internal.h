@@ -1,0 +1,140 @@
+// Internal declarations shared by the library's translation units (host side).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "lbm_capi.h"
+
+namespace lbm {
+
+// D3Q27_REF gather entry: population `src_pop` of reflecting cell `src_cell` is scattered with
+// weight `w` into population `dst_pop` of the target cell (the reference's push of
+// SimCalcFuncs.cu:164-186 turned into a pull).  `src_stream` is the cell the reflecting cell's
+// population was streamed from (src_cell - c_{src_pop}), or -1 when that lies outside.
+struct GatherEntry {
+    int32_t src_cell;
+    int32_t src_stream;
+    float w;
+    uint8_t src_pop;
+    uint8_t dst_pop;
+    uint8_t slot;
+    uint8_t pad;
+};
+static_assert(sizeof(GatherEntry) == 16, "GatherEntry layout");
+
+// D2Q9 per-cell link word: bit j-1 set when population j (1..8) arrives from a wall (half-way
+// bounce-back), bit j+7 when that wall moves.  Solid cells hold LINK_SOLID, a pattern no fluid cell
+// can have (a moving link always has its bounce bit).
+constexpr uint16_t LINK_SOLID = 0x0100;
+
+// struct ReflectionValues of the reference (LatticePoint.h:3-7): 81 slots, direction of slot s in
+// bits 5*(s%6) .. 5*(s%6)+4 of dirs[s/6], weight in w[s]
+struct ReflRecord {
+    int32_t dirs[14];
+    float w[81];
+};
+static_assert(sizeof(ReflRecord) == 380, "ReflectionValues layout");
+
+inline int refl_dir(const ReflRecord &r, int s) {
+    return (int)(((uint32_t)r.dirs[s / 6] >> (5 * (s % 6))) & 31u);
+}
+
+struct D2Q9Params {
+    float omega;        // 1/tau
+    float fx, fy;       // body force
+    float uwx, uwy;     // moving-wall velocity
+    double omega_d, fx_d, fy_d, uwx_d, uwy_d;
+};
+
+// device scratch for reductions: per-block partial sums
+struct Scratch {
+    double *partials = nullptr;
+    size_t n = 0;
+};
+
+}  // namespace lbm
+
+struct lbm_ctx {
+    lbm_desc desc{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+
+    int64_t cells = 0;
+    int64_t pitch = 0;        // D2Q9: elements per row; D3Q27: == cells per plane
+    int64_t plane = 0;        // elements per population plane
+    int q = 9;
+    size_t elem = 4;          // bytes per stored population
+    void *f[2] = {nullptr, nullptr};
+    int cur = 0;              // f[cur] holds the current state
+    uint8_t *flags_d = nullptr;
+    uint16_t *links_d = nullptr;
+    bool flags_set = false;
+    int64_t fluid_cells = 0;
+    int64_t steps_done = 0;
+
+    // D3Q27_REF
+    int32_t *tgt_cells_d = nullptr;  // target cells of the gather lists
+    int32_t *tgt_off_d = nullptr;    // CSR offsets (ntgt + 1)
+    lbm::GatherEntry *entries_d = nullptr;
+    int64_t ntgt = 0, nent = 0;
+    float *induced_d = nullptr;      // 27 floats
+    bool flow_on = false;
+    double *force_acc_d = nullptr;   // running force sum (3 doubles)
+    bool force_on = false;
+
+    std::vector<uint8_t> flags_h;    // D3Q27_REF: host copy of the user flag bits
+    std::vector<std::pair<int32_t, lbm::ReflRecord>> tables_h;
+    bool d3_dirty = true;            // gather lists / device flags need a rebuild
+
+    lbm::Scratch scratch;
+    double *result_d = nullptr;      // small device result buffer (16 doubles)
+    void *staging = nullptr;         // host-layout staging buffer, grown on demand
+    size_t staging_bytes = 0;
+
+    int block_threads = 256;
+    int cells_per_thread = 1;
+
+    size_t device_bytes = 0;
+};
+
+namespace lbm {
+
+// error helpers
+lbm_status fail(lbm_ctx *ctx, lbm_status s, const std::string &msg);
+lbm_status cuda_fail(lbm_ctx *ctx, cudaError_t e, const char *what);
+lbm_status set_thread_error(lbm_status s, const std::string &msg);
+
+// memory helpers (count device bytes)
+lbm_status dalloc(lbm_ctx *ctx, void **p, size_t bytes, const char *what);
+void dfree(lbm_ctx *ctx, void *p, size_t bytes);
+lbm_status ensure_scratch(lbm_ctx *ctx, size_t n);
+
+// D2Q9 launchers (d2q9.cu)
+D2Q9Params d2q9_params(const lbm_desc &d);
+cudaError_t d2q9_build_links(lbm_ctx *ctx);
+cudaError_t d2q9_init_equilibrium(lbm_ctx *ctx, const float *rho_d, const float *ux_d, const float *uy_d);
+cudaError_t d2q9_step(lbm_ctx *ctx, int nsteps);
+cudaError_t d2q9_moments(lbm_ctx *ctx, float *rho_d, float *ux_d, float *uy_d);
+cudaError_t d2q9_conservation(lbm_ctx *ctx, double *out_d);
+cudaError_t d2q9_load(lbm_ctx *ctx, const void *src_d, int src_dtype, int aos);
+cudaError_t d2q9_store(lbm_ctx *ctx, void *dst_d, int dst_dtype, int aos);
+
+// D3Q27_REF launchers (d3q27.cu)
+cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps);
+cudaError_t d3q27_apply(lbm_ctx *ctx, int op);
+cudaError_t d3q27_moments(lbm_ctx *ctx, float *rho_d, float *ux_d, float *uy_d, float *uz_d);
+cudaError_t d3q27_conservation(lbm_ctx *ctx, double *out_d);
+cudaError_t d3q27_load(lbm_ctx *ctx, const void *src_d, int src_dtype, int aos);
+cudaError_t d3q27_store(lbm_ctx *ctx, void *dst_d, int dst_dtype, int aos);
+
+// reduction finaliser (common.cu): out[k] (+)= sum_b partials[b*ncomp + k], fixed order
+cudaError_t finalize_sums(cudaStream_t s, const double *partials, int nblocks, int ncomp, double *out,
+                          bool accumulate = false);
+
+}  // namespace lbm

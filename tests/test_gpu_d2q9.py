@@ -1,0 +1,190 @@
+"""D2Q9 parity: the CUDA kernels (through the C ABI) against the CPU oracle on the same seeded inputs.
+
+Tolerances (stated per storage type):
+  FP64 storage  max |f_gpu - f_oracle| <= 1e-12   (same arithmetic, different evaluation order)
+  FP32 storage  max |f_gpu - f_oracle64| <= 1e-5 * max|f|, and velocity field within 1e-4 of max|u|
+                relative after the run (FP32 rounding accumulated over the run)
+  FP16/BF16-shifted storage: velocity within 2e-2 / 1e-1 of max|u| (storage precision 2^-11 / 2^-8
+                of the shifted populations)
+"""
+import zlib
+
+import numpy as np
+import pytest
+
+import latticeboltzmanncuda_gb300 as lbm
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def box(nx, ny, lid=False):
+    fl = np.zeros((ny, nx), np.uint8)
+    fl[0, :] = 1
+    fl[:, 0] = 1
+    fl[:, -1] = 1
+    fl[-1, :] = 2 if lid else 1
+    return fl
+
+
+def random_state(nx, ny, seed, amp=0.02):
+    rng = np.random.default_rng(seed)
+    rho = 1 + amp * rng.standard_normal((ny, nx))
+    ux = amp * rng.standard_normal((ny, nx))
+    uy = amp * rng.standard_normal((ny, nx))
+    f = oracle.d2q9_equilibrium(rho, ux, uy)
+    f += 1e-3 * rng.standard_normal(f.shape)  # non-equilibrium part
+    return f
+
+
+def gpu_run(flags, f0, tau, steps, periodic=0, force=(0, 0), wall=(0, 0), dtype="f64"):
+    _, ny, nx = f0.shape
+    with lbm.Lattice(nx, ny, dtype=dtype, tau=tau, periodic=periodic, body_force=(force[0], force[1], 0),
+                     wall_velocity=(wall[0], wall[1], 0)) as L:
+        L.set_flags(flags)
+        L.load_populations(f0)
+        L.step(steps)
+        f = L.retrieve_populations(np.float64)
+        rho, ux, uy = L.moments()
+        cons = L.conservation()
+    return f, (rho, ux, uy), cons
+
+
+CASES = {
+    # name: (nx, ny, flags builder, periodic, force, wall, tau, steps)
+    "closed_box": (37, 23, lambda nx, ny: box(nx, ny), 0, (0, 0), (0, 0), 0.7, 60),
+    "cavity_lid": (40, 33, lambda nx, ny: box(nx, ny, lid=True), 0, (0, 0), (0.05, 0), 0.6, 80),
+    "channel_force": (64, 20, None, 1, (1e-5, 0), (0, 0), 0.55, 80),
+    "periodic_xy_force": (33, 31, lambda nx, ny: np.zeros((ny, nx), np.uint8), 3, (2e-5, -1e-5), (0, 0), 0.9, 50),
+    "open_edges": (29, 17, lambda nx, ny: np.zeros((ny, nx), np.uint8), 0, (0, 0), (0, 0), 0.8, 40),
+    "periodic_y_moving": (24, 30, None, 2, (0, 0), (0.03, 0.01), 0.65, 50),
+    "thin_1xN": (1, 40, lambda nx, ny: np.zeros((ny, nx), np.uint8), 3, (0, 1e-5), (0, 0), 0.75, 30),
+}
+
+
+def build_flags(name, nx, ny, builder):
+    if builder is not None:
+        return builder(nx, ny)
+    if name == "channel_force":
+        fl, _ = lbm.gen_channel(nx, ny, 2, 2.0, 4.0, 3)
+        return fl
+    fl = np.zeros((ny, nx), np.uint8)
+    fl[:, 0] = 1
+    fl[:, -1] = 2
+    fl[10:14, 8:12] = 1
+    return fl
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_fp64_gpu_matches_fp64_oracle(name):
+    nx, ny, builder, periodic, force, wall, tau, steps = CASES[name]
+    flags = build_flags(name, nx, ny, builder)
+    f0 = random_state(nx, ny, zlib.crc32(name.encode()))
+    ref = oracle.d2q9_run(f0, flags, tau, steps, periodic=periodic, force=force, wall_velocity=wall)
+    got, (rho, ux, uy), cons = gpu_run(flags, f0, tau, steps, periodic, force, wall, "f64")
+    fluid = flags == 0
+    assert np.max(np.abs(got - ref)[:, fluid]) <= 1e-12
+    r_rho, r_ux, r_uy = oracle.d2q9_moments(ref, flags, periodic=periodic, force=force, wall_velocity=wall)
+    assert np.max(np.abs(rho - r_rho)[fluid]) < 1e-6
+    assert np.max(np.abs(ux - r_ux)[fluid]) < 1e-7
+    assert np.max(np.abs(uy - r_uy)[fluid]) < 1e-7
+    want = oracle.d2q9_conservation(ref, flags)
+    assert np.allclose(cons[:3], want, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_fp32_gpu_within_tolerance_of_fp64_oracle(name):
+    nx, ny, builder, periodic, force, wall, tau, steps = CASES[name]
+    flags = build_flags(name, nx, ny, builder)
+    f0 = random_state(nx, ny, zlib.crc32(name.encode()))
+    ref = oracle.d2q9_run(f0, flags, tau, steps, periodic=periodic, force=force, wall_velocity=wall)
+    got, _, _ = gpu_run(flags, f0, tau, steps, periodic, force, wall, "f32")
+    fluid = flags == 0
+    err = np.max(np.abs(got - ref)[:, fluid])
+    assert err <= 1e-5 * np.max(np.abs(ref)), err
+
+
+@pytest.mark.parametrize("dtype,tol", [("f16s", 2e-2), ("bf16s", 1e-1)])
+def test_shifted_half_storage_velocity(dtype, tol):
+    nx, ny = 48, 40
+    flags = box(nx, ny, lid=True)
+    f0 = oracle.d2q9_equilibrium(np.ones((ny, nx)), np.zeros((ny, nx)), np.zeros((ny, nx)))
+    ref = oracle.d2q9_run(f0, flags, 0.6, 400, wall_velocity=(0.05, 0))
+    _, rux, ruy = oracle.d2q9_moments(ref, flags, wall_velocity=(0.05, 0))
+    _, (rho, ux, uy), _ = gpu_run(flags, f0, 0.6, 400, 0, (0, 0), (0.05, 0), dtype)
+    umax = np.max(np.hypot(rux, ruy))
+    err = np.max(np.hypot(ux - rux, uy - ruy)) / umax
+    assert err < tol, err
+
+
+def test_cavity_128_2000_steps_fp32():
+    """Lid-driven cavity 128x128, tau 0.6, lid 0.05, 2000 steps, FP32 against the FP64 oracle."""
+    n = 128
+    flags = lbm.gen_cavity(n, n)
+    f0 = oracle.d2q9_equilibrium(np.ones((n, n)), np.zeros((n, n)), np.zeros((n, n)))
+    ref = oracle.d2q9_run(f0, flags, 0.6, 2000, wall_velocity=(0.05, 0))
+    _, rux, ruy = oracle.d2q9_moments(ref, flags, wall_velocity=(0.05, 0))
+    with lbm.Lattice(n, n, tau=0.6, wall_velocity=(0.05, 0, 0)) as L:
+        L.set_flags(flags)
+        L.init_equilibrium()
+        L.step(2000)
+        _, ux, uy = L.moments()
+    umax = np.max(np.hypot(rux, ruy))
+    err = np.max(np.hypot(ux - rux, uy - ruy)) / umax
+    assert err < 1e-4, err
+
+
+def test_mass_conservation_fp32_channel():
+    nx, ny = 256, 64
+    flags, _ = lbm.gen_channel(nx, ny, 4, 3, 6, 9)
+    with lbm.Lattice(nx, ny, tau=0.55, periodic=1) as L:
+        L.set_flags(flags)
+        L.init_equilibrium()
+        m0 = L.conservation()
+        L.step(500)
+        m1 = L.conservation()
+    assert abs(m1[0] - m0[0]) / m0[0] < 1e-6
+
+
+def test_population_and_aos_round_trip():
+    nx, ny = 35, 18
+    f0 = random_state(nx, ny, 5)
+    with lbm.Lattice(nx, ny, dtype="f32") as L:
+        L.load_populations(f0.astype(np.float32))
+        back = L.retrieve_populations()
+        assert np.max(np.abs(back - f0)) < 1e-7
+        aos = L.retrieve_aos()
+        # record index y + ny*x, populations in the in-plane reference slots
+        recs = aos.reshape(nx, ny)
+        for q, slot in enumerate(lbm.capi.AOS_SLOTS_D2Q9):
+            assert np.allclose(recs["f"][:, :, slot].T, back[q], atol=0)
+        assert np.array_equal(recs["x"], np.repeat(np.arange(nx)[:, None], ny, 1))
+        L2 = lbm.Lattice(nx, ny, dtype="f32")
+        L2.load_aos(aos)
+        assert np.max(np.abs(L2.retrieve_populations() - back)) < 1e-7
+        L2.close()
+
+
+def test_invalid_flags_rejected():
+    with lbm.Lattice(8, 8) as L:
+        bad = np.zeros((8, 8), np.uint8)
+        bad[3, 3] = 7
+        with pytest.raises(lbm.LBMError):
+            L.set_flags(bad)
+        with pytest.raises(lbm.LBMError):
+            L.load_populations(np.zeros(5))
+        with pytest.raises(lbm.LBMError):
+            L.step(-1)
+
+
+def test_steps_are_deterministic():
+    nx, ny = 96, 40
+    flags, _ = lbm.gen_channel(nx, ny, 3, 3, 5, 2)
+    outs = []
+    for _ in range(2):
+        with lbm.Lattice(nx, ny, tau=0.55, periodic=1, body_force=(1e-5, 0, 0)) as L:
+            L.set_flags(flags)
+            L.init_equilibrium()
+            L.step(100)
+            outs.append(L.retrieve_populations())
+    assert np.array_equal(outs[0], outs[1])
