@@ -57,7 +57,8 @@ __device__ __forceinline__ void pull(const float *__restrict__ src, const Dims &
     for (int j = 0; j < 27; ++j) {
         const int sx = x - c_dir[j][0], sy = y - c_dir[j][1], sz = z - c_dir[j][2];
         const bool in = sx >= 0 && sy >= 0 && sz >= 0 && sx < d.X && sy < d.Y && sz < d.Z;
-        const int64_t s = c - (int64_t)c_dir[j][2] - (int64_t)d.Z * ((int64_t)c_dir[j][1] + (int64_t)d.Y * c_dir[j][0]);
+        // neighbours outside the lattice are never addressed: their index is replaced by the cell's own
+        const int64_t s = in ? c - (int64_t)c_dir[j][2] - (int64_t)d.Z * ((int64_t)c_dir[j][1] + (int64_t)d.Y * c_dir[j][0]) : c;
         v[j] = in ? __ldg(src + (int64_t)j * d.n + s) : 0.0f;
     }
 }
