@@ -75,9 +75,15 @@ def build_flags(name, nx, ny, builder):
     return fl
 
 
+def f32(*v):
+    """lbm_desc carries tau, force and wall velocity as float: the oracle gets the same values."""
+    return tuple(float(np.float32(x)) for x in v)
+
+
 @pytest.mark.parametrize("name", list(CASES))
 def test_fp64_gpu_matches_fp64_oracle(name):
     nx, ny, builder, periodic, force, wall, tau, steps = CASES[name]
+    (tau,), force, wall = f32(tau), f32(*force), f32(*wall)
     flags = build_flags(name, nx, ny, builder)
     f0 = random_state(nx, ny, zlib.crc32(name.encode()))
     ref = oracle.d2q9_run(f0, flags, tau, steps, periodic=periodic, force=force, wall_velocity=wall)

@@ -257,7 +257,7 @@ def test_moments_and_conservation():
     assert np.allclose(rho, f.sum(1), rtol=1e-6)
     assert np.allclose(ux, (f * C[:, 0] * split).sum(1) / f.sum(1), rtol=1e-5, atol=1e-7)
     assert np.allclose(cons[0], f.astype(np.float64).sum(), rtol=1e-12)
-    assert np.allclose(cons[1:], f.astype(np.float64) @ C, rtol=1e-9, atol=1e-9)
+    assert np.allclose(cons[1:], (f.astype(np.float64) @ C).sum(0), rtol=1e-9, atol=1e-9)
 
 
 def test_rejects_bad_tables():
