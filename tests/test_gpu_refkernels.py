@@ -74,9 +74,12 @@ CASES = [((6, 5, 6), (1, 1, 6)), ((12, 8, 12), (2, 4, 12)), ((32, 16, 32), (1, 1
 
 @pytest.mark.parametrize("dims,threads", CASES)
 def test_stream_collide_matches_reference(dims, threads):
-    f, flags, _, _, _ = random_lattice(dims, 11 + dims[0])
+    f, flags, cells, recs, _ = random_lattice(dims, 11 + dims[0])
     steps = 8
-    ref = refkern.run(dims, points_from(f, flags), "SC", nsteps=steps, tau=0.75, threads=threads)
+    # reflected cells carry their tables, as in a lattice prepared by Lattice::preProcessModel; the
+    # stream-collide order does not read them
+    ref = refkern.run(dims, points_from(f, flags), "SC", nsteps=steps, tau=0.75, tab_cells=cells,
+                      tab_records=recs, threads=threads)
     with lbm.Lattice(*dims, mode="d3q27_ref", tau=0.75, order=lbm.ORDER_STREAM_COLLIDE) as L:
         L.load_aos(points_from(f, flags))
         L.step(steps)
