@@ -248,8 +248,10 @@ def run_mine(args):
 
     # ---------------- device-resident
     for _ in range(args.warmup):
-        L.step(args.lbm_steps)
+        L.step(args.lbm_steps)  # the first step runs the launch-shape autotuner
     torch.cuda.synchronize(dev)
+    info = L.info()
+    shape = f"{info['cells_per_thread']} cells/thread, {info['block_threads']}x{info['rows_per_block']} threads"
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         barrier()
@@ -318,7 +320,7 @@ def run_mine(args):
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                          "bytes_per_update": bpu, "traffic": traffic,
-                         "kernel": f"step_kernel<{args.dtype}>", "avg_launch_us": round(avg_launch * 1e6, 3)},
+                         "kernel": f"D2Q9 step<{args.dtype}> ({shape})", "avg_launch_us": round(avg_launch * 1e6, 3)},
             "gpu_launches": launches,
             "e2e": e2e,
             "cpu_baseline": cpu,

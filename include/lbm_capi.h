@@ -106,8 +106,10 @@ typedef struct lbm_info {
     int64_t device_bytes;     /* all device bytes owned by the context */
     int64_t bytes_per_update; /* algorithmic bytes per cell update: 2 * Q * sizeof(storage) */
     int64_t steps_done;
-    int32_t block_threads;    /* launch shape of the step kernel */
-    int32_t cells_per_thread;
+    int32_t block_threads;    /* D2Q9 step kernel launch shape: threads along x per block, */
+    int32_t cells_per_thread; /* consecutive cells per thread, */
+    int32_t rows_per_block;   /* rows per block */
+    int32_t tuned;            /* 1 once the shape has been chosen */
 } lbm_info;
 
 /* ---------------------------------------------------------------- context life cycle */
@@ -172,6 +174,21 @@ LBM_API lbm_status lbm_get_force(lbm_ctx *ctx, float host_out[3]);
 LBM_API lbm_status lbm_step(lbm_ctx *ctx, int32_t nsteps);
 /* D3Q27_REF: one separate pass (LBM_OP_*), as the reference's Lattice::simulate* methods. */
 LBM_API lbm_status lbm_apply(lbm_ctx *ctx, int32_t op);
+
+/* D2Q9 launch shape.  The first lbm_step() picks it with a built-in autotuner: every candidate
+ * (cells per thread 1/2/4/8 as the storage type allows, block widths 32..256, 1..4 rows per block)
+ * is timed on the context's own domain, leaving the state unchanged, and the fastest is kept,
+ * cached per (dtype, size, periodicity, force) in the process and in the JSON file named by
+ * $LBM_TUNE_CACHE (default ~/.cache/lbm_gb300_tune.json; empty: no file).  LBM_AUTOTUNE=0 skips the
+ * timing and uses a fixed default shape.  lbm_autotune() runs the tuner now (retune != 0 ignores the
+ * caches); lbm_set_launch() fixes a shape (cells_per_thread in 1,2,4,8; block_threads a multiple of
+ * 32; block_threads * rows_per_block <= 256). */
+LBM_API lbm_status lbm_autotune(lbm_ctx *ctx, int32_t retune);
+LBM_API lbm_status lbm_set_launch(lbm_ctx *ctx, int32_t cells_per_thread, int32_t block_threads,
+                                  int32_t rows_per_block);
+/* D2Q9: visit rows in alternating order on successive steps (default 1), so each step starts on
+ * the rows that the previous step wrote last and that are still in L2. */
+LBM_API lbm_status lbm_set_sweep_alternation(lbm_ctx *ctx, int32_t enabled);
 
 /* ---------------------------------------------------------------- results */
 /* Density and velocity per cell (host arrays of cells floats, any may be NULL).

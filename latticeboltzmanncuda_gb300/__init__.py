@@ -175,6 +175,17 @@ class Lattice:
     def apply(self, op):
         self._call("lbm_apply", int(op))
 
+    def autotune(self, retune=False):
+        self._call("lbm_autotune", int(bool(retune)))
+        i = self.info()
+        return i["cells_per_thread"], i["block_threads"], i["rows_per_block"]
+
+    def set_launch(self, cells_per_thread, block_threads, rows_per_block=1):
+        self._call("lbm_set_launch", int(cells_per_thread), int(block_threads), int(rows_per_block))
+
+    def set_sweep_alternation(self, enabled):
+        self._call("lbm_set_sweep_alternation", int(bool(enabled)))
+
     # ------------------------------------------------------------------ results
     def moments(self, out=None):
         """(rho, ux, uy) for D2Q9, (rho, ux, uy, uz) for D3Q27_REF; `out` may give float32 arrays

@@ -56,7 +56,8 @@ class Info(ctypes.Structure):
     _fields_ = [("cells", ctypes.c_int64), ("fluid_cells", ctypes.c_int64), ("row_pitch", ctypes.c_int64),
                 ("state_bytes", ctypes.c_int64), ("device_bytes", ctypes.c_int64),
                 ("bytes_per_update", ctypes.c_int64), ("steps_done", ctypes.c_int64),
-                ("block_threads", ctypes.c_int32), ("cells_per_thread", ctypes.c_int32)]
+                ("block_threads", ctypes.c_int32), ("cells_per_thread", ctypes.c_int32),
+                ("rows_per_block", ctypes.c_int32), ("tuned", ctypes.c_int32)]
 
 
 # exported symbols and their signatures: (name, restype, argtypes)
@@ -85,6 +86,9 @@ SIGNATURES = [
     ("lbm_get_force", _S, [_P, _P]),
     ("lbm_step", _S, [_P, _I32]),
     ("lbm_apply", _S, [_P, _I32]),
+    ("lbm_autotune", _S, [_P, _I32]),
+    ("lbm_set_launch", _S, [_P, _I32, _I32, _I32]),
+    ("lbm_set_sweep_alternation", _S, [_P, _I32]),
     ("lbm_moments", _S, [_P, _P, _P, _P, _P]),
     ("lbm_conservation", _S, [_P, _P]),
     ("lbm_gen_channel", _S, [_I32, _I32, _I32, _F, _F, _U64, _P, _P]),

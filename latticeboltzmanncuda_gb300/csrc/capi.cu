@@ -312,6 +312,8 @@ LBM_API lbm_status lbm_get_info(lbm_ctx *ctx, lbm_info *out) {
     out->steps_done = ctx->steps_done;
     out->block_threads = ctx->block_threads;
     out->cells_per_thread = ctx->cells_per_thread;
+    out->rows_per_block = ctx->rows_per_block;
+    out->tuned = ctx->tuned ? 1 : 0;
     return LBM_OK;
 }
 
@@ -556,6 +558,35 @@ LBM_API lbm_status lbm_step(lbm_ctx *ctx, int32_t nsteps) {
         CUDA_TRY(ctx, d3q27_step(ctx, nsteps), "D3Q27 step");
     }
     ctx->steps_done += nsteps;
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_autotune(lbm_ctx *ctx, int32_t retune) {
+    CHECK_CTX(ctx);
+    if (ctx->desc.mode != LBM_D2Q9) return LBM_OK;  // D3Q27_REF has one launch shape
+    lbm_status st = use_device(ctx);
+    if (st != LBM_OK) return st;
+    CUDA_TRY(ctx, d2q9_autotune(ctx, retune != 0), "autotune");
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_set_launch(lbm_ctx *ctx, int32_t cells_per_thread, int32_t block_threads, int32_t rows_per_block) {
+    CHECK_CTX(ctx);
+    if (ctx->desc.mode != LBM_D2Q9) return fail(ctx, LBM_ERR_UNSUPPORTED, "lbm_set_launch is D2Q9 only");
+    if (!d2q9_shape_valid(ctx, cells_per_thread, block_threads, rows_per_block))
+        return fail(ctx, LBM_ERR_INVALID, "launch shape " + std::to_string(cells_per_thread) + "x" +
+                                              std::to_string(block_threads) + "x" + std::to_string(rows_per_block) +
+                                              " is not valid for this domain and dtype");
+    ctx->cells_per_thread = cells_per_thread;
+    ctx->block_threads = block_threads;
+    ctx->rows_per_block = rows_per_block;
+    ctx->tuned = true;
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_set_sweep_alternation(lbm_ctx *ctx, int32_t enabled) {
+    CHECK_CTX(ctx);
+    ctx->alternate_sweeps = enabled != 0;
     return LBM_OK;
 }
 

@@ -12,8 +12,17 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <map>
+#include <mutex>
+#include <string>
+
 #include "lbm_internal.h"
 #include "d2q9_core.cuh"
+#include "d2q9_vec.cuh"
 #include "reduce.cuh"
 
 namespace lbm {
@@ -80,25 +89,31 @@ __global__ void count_fluid_kernel(const uint8_t *__restrict__ flags, int64_t n,
 }
 
 // ------------------------------------------------------------------------------------------------
-// fused step, one thread per cell
+// fused step.  Rows are visited in increasing order on even sweeps and decreasing order on odd
+// ones (`reverse`): a step then starts on the rows the previous step wrote last, which are still in
+// L2, instead of on the rows it wrote first.
 // ------------------------------------------------------------------------------------------------
-template <class S, bool FORCE>
+template <class S, bool FORCE, class I>
 __global__ void __launch_bounds__(256) step_kernel(const S *__restrict__ src, S *__restrict__ dst,
-                                                   const uint16_t *__restrict__ links, int nx, int ny,
-                                                   int64_t pitch, int64_t plane, int periodic,
-                                                   D2Q9Params prm) {
-    using R = typename d2q9::Store<S>::R;
-    int x = blockIdx.x * blockDim.x + threadIdx.x;
-    int y = blockIdx.y;
-    if (x >= nx) return;
-    int64_t c = (int64_t)y * pitch + x;
-    uint16_t L = __ldg(links + c);
-    if (L == LINK_SOLID) return;
-    R g[9];
-    d2q9::gather<S>(src, L, x, y, nx, ny, pitch, plane, periodic, d2q9::wall_u<R>(prm), g);
-    d2q9::collide<R, FORCE>(g, d2q9::omega<R>(prm), d2q9::force<R>(prm));
-#pragma unroll
-    for (int q = 0; q < 9; ++q) d2q9::Store<S>::st(dst + q * plane + c, g[q]);
+                                                   const uint16_t *__restrict__ links, int nx, int ny, I pitch,
+                                                   I plane, int periodic, D2Q9Params prm, int reverse) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= nx || row >= ny) return;
+    const int y = reverse ? ny - 1 - row : row;
+    d2q9::scalar_cell<S, I>(src, dst, links, x, y, nx, ny, pitch, plane, periodic, prm, FORCE);
+}
+
+template <class S, int V, bool FORCE>
+__global__ void __launch_bounds__(256) step_vec_kernel(const S *__restrict__ src, S *__restrict__ dst,
+                                                       const uint16_t *__restrict__ links, int nx, int ny,
+                                                       int pitch, int plane, int periodic, D2Q9Params prm,
+                                                       int reverse) {
+    const int row = blockIdx.y * blockDim.y + threadIdx.y;
+    if (row >= ny) return;  // uniform per warp: warps never straddle rows
+    const int y = reverse ? ny - 1 - row : row;
+    const int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * V;
+    d2q9::step_vec<S, V, FORCE, int>(src, dst, links, x0, y, nx, ny, pitch, plane, periodic, prm);
 }
 
 template <class S>
@@ -235,25 +250,199 @@ __global__ void store_kernel(const S *__restrict__ src, H *__restrict__ host, in
     }
 }
 
+// ------------------------------------------------------------------------------------------------
+// launch shapes and the autotuner
+// ------------------------------------------------------------------------------------------------
+struct Shape {
+    int v, tx, ty;
+};
+
+template <class S>
+constexpr bool vec_ok(int v) {
+    return (sizeof(S) == 4 && (v == 2 || v == 4)) || (sizeof(S) == 2 && (v == 2 || v == 4 || v == 8)) ||
+           (sizeof(S) == 8 && v == 2);
+}
+
+bool small_index(const lbm_ctx *ctx) { return ctx->plane * 9 < (int64_t)INT32_MAX; }
+
+template <class S>
+cudaError_t launch_one(lbm_ctx *ctx, const Shape &sh, const S *src, S *dst, int reverse) {
+    const lbm_desc &d = ctx->desc;
+    const D2Q9Params prm = d2q9_params(d);
+    const bool force = prm.fx != 0.0f || prm.fy != 0.0f;
+    dim3 block(sh.tx, sh.ty);
+    const int per_row = sh.v == 1 ? d.nx : (int)(ctx->pitch / sh.v);
+    dim3 grid((unsigned)((per_row + sh.tx - 1) / sh.tx), (unsigned)((d.ny + sh.ty - 1) / sh.ty));
+    cudaStream_t st = ctx->stream;
+    if (sh.v == 1) {
+        if (small_index(ctx)) {
+            const int pitch = (int)ctx->pitch, plane = (int)ctx->plane;
+            if (force) step_kernel<S, true, int><<<grid, block, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, reverse);
+            else step_kernel<S, false, int><<<grid, block, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, reverse);
+        } else {
+            if (force) step_kernel<S, true, int64_t><<<grid, block, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, ctx->pitch, ctx->plane, d.periodic, prm, reverse);
+            else step_kernel<S, false, int64_t><<<grid, block, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, ctx->pitch, ctx->plane, d.periodic, prm, reverse);
+        }
+        return cudaGetLastError();
+    }
+    const int pitch = (int)ctx->pitch, plane = (int)ctx->plane;
+#define LBM_VEC_CASE(VV)                                                                                        \
+    if constexpr (vec_ok<S>(VV)) {                                                                              \
+        if (sh.v == VV) {                                                                                       \
+            if (force) step_vec_kernel<S, VV, true><<<grid, block, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, reverse); \
+            else step_vec_kernel<S, VV, false><<<grid, block, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, reverse); \
+            return cudaGetLastError();                                                                          \
+        }                                                                                                       \
+    }
+    LBM_VEC_CASE(2)
+    LBM_VEC_CASE(4)
+    LBM_VEC_CASE(8)
+#undef LBM_VEC_CASE
+    return cudaErrorInvalidValue;
+}
+
+template <class S>
+std::vector<Shape> candidates(const lbm_ctx *ctx) {
+    std::vector<Shape> c = {{1, 256, 1}, {1, 128, 2}};
+    if (!small_index(ctx)) return c;
+    for (int v : {2, 4, 8}) {
+        if (!vec_ok<S>(v) || ctx->pitch % v) continue;
+        const int per_row = (int)(ctx->pitch / v);
+        for (int tx : {32, 64, 128, 256}) {
+            if (tx > 32 && tx / 2 >= per_row) continue;  // a block wider than two rows' worth is idle
+            const int ty = std::max(1, std::min(256 / tx, 4));
+            c.push_back({v, tx, 1});
+            if (ty > 1 && tx * ty <= 256) c.push_back({v, tx, ty});
+        }
+    }
+    return c;
+}
+
+std::mutex g_tune_mu;
+std::map<std::string, Shape> g_tune_cache;
+bool g_tune_file_loaded = false;
+
+std::string tune_key(const lbm_ctx *ctx) {
+    const lbm_desc &d = ctx->desc;
+    const bool force = d.body_force[0] != 0.0f || d.body_force[1] != 0.0f;
+    char buf[128];
+    std::snprintf(buf, sizeof(buf), "d2q9/%d/%dx%d/p%d/f%d", d.dtype, d.nx, d.ny, d.periodic, force ? 1 : 0);
+    return buf;
+}
+
+std::string tune_path() {
+    const char *e = std::getenv("LBM_TUNE_CACHE");
+    if (e) return e;  // empty: no file cache
+    const char *xdg = std::getenv("XDG_CACHE_HOME");
+    const char *home = std::getenv("HOME");
+    if (xdg && *xdg) return std::string(xdg) + "/lbm_gb300_tune.json";
+    if (home && *home) return std::string(home) + "/.cache/lbm_gb300_tune.json";
+    return "";
+}
+
+// flat JSON object {"key": [v, tx, ty], ...}
+void load_tune_file() {
+    if (g_tune_file_loaded) return;
+    g_tune_file_loaded = true;
+    const std::string path = tune_path();
+    if (path.empty()) return;
+    FILE *fp = std::fopen(path.c_str(), "r");
+    if (!fp) return;
+    std::string txt;
+    char buf[4096];
+    size_t n;
+    while ((n = std::fread(buf, 1, sizeof(buf), fp)) > 0) txt.append(buf, n);
+    std::fclose(fp);
+    size_t pos = 0;
+    while ((pos = txt.find('"', pos)) != std::string::npos) {
+        const size_t end = txt.find('"', pos + 1);
+        if (end == std::string::npos) break;
+        const std::string key = txt.substr(pos + 1, end - pos - 1);
+        Shape sh{0, 0, 0};
+        if (std::sscanf(txt.c_str() + end + 1, " : [ %d , %d , %d ]", &sh.v, &sh.tx, &sh.ty) == 3 && sh.v > 0 && sh.tx > 0 &&
+            sh.ty > 0)
+            g_tune_cache[key] = sh;
+        pos = end + 1;
+    }
+}
+
+void save_tune_file() {
+    const std::string path = tune_path();
+    if (path.empty()) return;
+    const std::string tmp = path + ".tmp";
+    FILE *fp = std::fopen(tmp.c_str(), "w");
+    if (!fp) return;
+    std::fprintf(fp, "{\n");
+    size_t i = 0;
+    for (const auto &kv : g_tune_cache)
+        std::fprintf(fp, "  \"%s\": [%d, %d, %d]%s\n", kv.first.c_str(), kv.second.v, kv.second.tx, kv.second.ty,
+                     ++i < g_tune_cache.size() ? "," : "");
+    std::fprintf(fp, "}\n");
+    std::fclose(fp);
+    std::rename(tmp.c_str(), path.c_str());
+}
+
+// Time every candidate shape on the context's own domain (f[cur] -> f[cur^1] repeatedly, without
+// swapping, so the state is unchanged) and keep the fastest.
+template <class S>
+cudaError_t tune(lbm_ctx *ctx) {
+    const S *src = static_cast<const S *>(ctx->f[ctx->cur]);
+    S *dst = static_cast<S *>(ctx->f[ctx->cur ^ 1]);
+    cudaEvent_t e0, e1;
+    cudaError_t err = cudaEventCreate(&e0);
+    if (err != cudaSuccess) return err;
+    err = cudaEventCreate(&e1);
+    if (err != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return err;
+    }
+    const int64_t cells = (int64_t)ctx->desc.nx * ctx->desc.ny;
+    const int reps = cells > (1 << 22) ? 6 : (cells > (1 << 18) ? 12 : 30);
+    float best = 1e30f;
+    Shape pick = {1, 256, 1};
+    for (const Shape &sh : candidates<S>(ctx)) {
+        for (int w = 0; w < 2 && err == cudaSuccess; ++w) err = launch_one<S>(ctx, sh, src, dst, w & 1);
+        if (err != cudaSuccess) break;
+        cudaEventRecord(e0, ctx->stream);
+        for (int r = 0; r < reps && err == cudaSuccess; ++r) err = launch_one<S>(ctx, sh, src, dst, r & 1);
+        cudaEventRecord(e1, ctx->stream);
+        if (err != cudaSuccess) break;
+        err = cudaEventSynchronize(e1);
+        if (err != cudaSuccess) break;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            pick = sh;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (err != cudaSuccess) return err;
+    ctx->cells_per_thread = pick.v;
+    ctx->block_threads = pick.tx;
+    ctx->rows_per_block = pick.ty;
+    ctx->tuned = true;
+    return cudaSuccess;
+}
+
 template <class S>
 cudaError_t launch_step(lbm_ctx *ctx, int nsteps) {
-    const lbm_desc &d = ctx->desc;
-    D2Q9Params prm = d2q9_params(d);
-    bool force = prm.fx != 0.0f || prm.fy != 0.0f;
-    dim3 block(ctx->block_threads);
-    dim3 grid((unsigned)((d.nx + block.x - 1) / block.x), (unsigned)d.ny);
+    if (!ctx->tuned) {
+        cudaError_t e = d2q9_autotune(ctx, false);
+        if (e != cudaSuccess) return e;
+    }
+    const Shape sh{ctx->cells_per_thread, ctx->block_threads, ctx->rows_per_block};
     for (int s = 0; s < nsteps; ++s) {
         const S *src = static_cast<const S *>(ctx->f[ctx->cur]);
         S *dst = static_cast<S *>(ctx->f[ctx->cur ^ 1]);
-        if (force)
-            step_kernel<S, true><<<grid, block, 0, ctx->stream>>>(src, dst, ctx->links_d, d.nx, d.ny, ctx->pitch,
-                                                                   ctx->plane, d.periodic, prm);
-        else
-            step_kernel<S, false><<<grid, block, 0, ctx->stream>>>(src, dst, ctx->links_d, d.nx, d.ny, ctx->pitch,
-                                                                    ctx->plane, d.periodic, prm);
+        const int reverse = ctx->alternate_sweeps ? (int)(ctx->sweep & 1) : 0;
+        cudaError_t e = launch_one<S>(ctx, sh, src, dst, reverse);
+        if (e != cudaSuccess) return e;
+        ctx->sweep ^= 1;
         ctx->cur ^= 1;
     }
-    return cudaGetLastError();
+    return cudaSuccess;
 }
 
 template <class F>
@@ -299,6 +488,51 @@ cudaError_t d2q9_init_equilibrium(lbm_ctx *ctx, const float *rho_d, const float 
             ctx->plane, rho_d, ux_d, uy_d);
         return cudaGetLastError();
     });
+}
+
+bool d2q9_shape_valid(const lbm_ctx *ctx, int v, int tx, int ty) {
+    if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256) return false;
+    if (v == 1) return true;
+    if (!small_index(ctx) || ctx->pitch % v) return false;
+    switch (ctx->desc.dtype) {
+        case LBM_F32: return vec_ok<float>(v);
+        case LBM_F16S: return vec_ok<__half>(v);
+        case LBM_BF16S: return vec_ok<__nv_bfloat16>(v);
+        case LBM_F64: return vec_ok<double>(v);
+    }
+    return false;
+}
+
+cudaError_t d2q9_autotune(lbm_ctx *ctx, bool force_retune) {
+    const char *env = std::getenv("LBM_AUTOTUNE");
+    const std::string key = tune_key(ctx);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        load_tune_file();
+        auto it = g_tune_cache.find(key);
+        if (!force_retune && it != g_tune_cache.end() && d2q9_shape_valid(ctx, it->second.v, it->second.tx, it->second.ty)) {
+            ctx->cells_per_thread = it->second.v;
+            ctx->block_threads = it->second.tx;
+            ctx->rows_per_block = it->second.ty;
+            ctx->tuned = true;
+            return cudaSuccess;
+        }
+    }
+    if (env && env[0] == '0' && !force_retune) {
+        // tuning switched off: the default shape
+        const bool vec = d2q9_shape_valid(ctx, ctx->desc.dtype == LBM_F64 ? 2 : 4, 64, 1);
+        ctx->cells_per_thread = vec ? (ctx->desc.dtype == LBM_F64 ? 2 : 4) : 1;
+        ctx->block_threads = vec ? 64 : 256;
+        ctx->rows_per_block = 1;
+        ctx->tuned = true;
+        return cudaSuccess;
+    }
+    cudaError_t e = dispatch(ctx->desc.dtype, [&](auto tag) { return tune<decltype(tag)>(ctx); });
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = Shape{ctx->cells_per_thread, ctx->block_threads, ctx->rows_per_block};
+    save_tune_file();
+    return cudaSuccess;
 }
 
 cudaError_t d2q9_step(lbm_ctx *ctx, int nsteps) {

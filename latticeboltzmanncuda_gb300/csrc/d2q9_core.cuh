@@ -35,27 +35,86 @@ struct Store;
 template <>
 struct Store<float> {
     using R = float;
+    static __device__ __forceinline__ R to(float v) { return v; }
+    static __device__ __forceinline__ float from(R v) { return v; }
     static __device__ __forceinline__ R ld(const float *p) { return __ldg(p); }
     static __device__ __forceinline__ void st(float *p, R v) { *p = v; }
 };
 template <>
 struct Store<double> {
     using R = double;
+    static __device__ __forceinline__ R to(double v) { return v; }
+    static __device__ __forceinline__ double from(R v) { return v; }
     static __device__ __forceinline__ R ld(const double *p) { return __ldg(p); }
     static __device__ __forceinline__ void st(double *p, R v) { *p = v; }
 };
 template <>
 struct Store<__half> {
     using R = float;
+    static __device__ __forceinline__ R to(__half v) { return __half2float(v); }
+    static __device__ __forceinline__ __half from(R v) { return __float2half_rn(v); }
     static __device__ __forceinline__ R ld(const __half *p) { return __half2float(__ldg(p)); }
     static __device__ __forceinline__ void st(__half *p, R v) { *p = __float2half_rn(v); }
 };
 template <>
 struct Store<__nv_bfloat16> {
     using R = float;
+    static __device__ __forceinline__ R to(__nv_bfloat16 v) { return __bfloat162float(v); }
+    static __device__ __forceinline__ __nv_bfloat16 from(R v) { return __float2bfloat16_rn(v); }
     static __device__ __forceinline__ R ld(const __nv_bfloat16 *p) { return __bfloat162float(__ldg(p)); }
     static __device__ __forceinline__ void st(__nv_bfloat16 *p, R v) { *p = __float2bfloat16_rn(v); }
 };
+
+// V consecutive stored values moved as one 4-, 8- or 16-byte access (p aligned to V*sizeof(S))
+template <int B>
+struct RawPack;
+template <>
+struct RawPack<4> {
+    using T = unsigned int;
+};
+template <>
+struct RawPack<8> {
+    using T = uint2;
+};
+template <>
+struct RawPack<16> {
+    using T = uint4;
+};
+
+template <class S, int V>
+__device__ __forceinline__ void ld_pack(const S *__restrict__ p, typename Store<S>::R (&out)[V]) {
+    using T = typename RawPack<sizeof(S) * V>::T;
+    const T raw = __ldg(reinterpret_cast<const T *>(p));
+    S e[V];
+    memcpy(e, &raw, sizeof(raw));
+#pragma unroll
+    for (int k = 0; k < V; ++k) out[k] = Store<S>::to(e[k]);
+}
+
+template <class S, int V>
+__device__ __forceinline__ void st_pack(S *__restrict__ p, const typename Store<S>::R (&in)[V]) {
+    using T = typename RawPack<sizeof(S) * V>::T;
+    S e[V];
+#pragma unroll
+    for (int k = 0; k < V; ++k) e[k] = Store<S>::from(in[k]);
+    T raw;
+    memcpy(&raw, e, sizeof(raw));
+    *reinterpret_cast<T *>(p) = raw;
+}
+
+template <int V>
+__device__ __forceinline__ void ld_links(const uint16_t *__restrict__ p, uint32_t (&L)[V]) {
+    using T = typename RawPack<2 * V < 4 ? 4 : 2 * V>::T;
+    if constexpr (V == 1) {
+        L[0] = __ldg(p);
+    } else {
+        const T raw = __ldg(reinterpret_cast<const T *>(p));
+        uint16_t e[V];
+        memcpy(e, &raw, sizeof(e));
+#pragma unroll
+        for (int k = 0; k < V; ++k) L[k] = e[k];
+    }
+}
 
 template <class R, class P>
 __device__ __forceinline__ R omega(const P &p);

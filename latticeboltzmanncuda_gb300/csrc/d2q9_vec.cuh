@@ -1,0 +1,154 @@
+// Vectorised D2Q9 update: one thread updates V consecutive cells of a row with V-wide loads and
+// stores of every population plane.  The x-1 / x+1 neighbours that fall outside the thread's
+// vector come from the adjacent lane by warp shuffle (the lane at a warp edge loads them itself),
+// so each population costs one wide load and one wide store per V cells.  Threads whose vector
+// touches the first or last column of the domain (periodic wrap, domain edge) or the row padding
+// re-run their cells through the scalar per-cell path.  Cells with bounce-back links take their
+// own opposite population (extra wide loads, only in vectors that have such a cell); solid cells
+// copy their own populations, so both A/B buffers keep identical values there.
+//
+// All 32 lanes of a warp must call step_vec for the same row (the shuffles use the full mask):
+// blockDim.x is a multiple of 32 and threads beyond the row run the loads on clamped addresses
+// and store nothing.
+#pragma once
+
+#include "d2q9_core.cuh"
+
+namespace lbm {
+namespace d2q9 {
+
+template <class S, class I>
+__device__ __forceinline__ void scalar_cell(const S *__restrict__ src, S *__restrict__ dst,
+                                            const uint16_t *__restrict__ links, int x, int y, int nx, int ny,
+                                            I pitch, I plane, int periodic, const D2Q9Params &prm, bool force) {
+    using R = typename Store<S>::R;
+    const I c = (I)y * pitch + x;
+    const uint32_t L = __ldg(links + c);
+    if (L == LINK_SOLID) return;
+    R g[9];
+    gather<S, R>(src, L, x, y, nx, ny, (int64_t)pitch, (int64_t)plane, periodic, wall_u<R>(prm), g);
+    if (force)
+        collide<R, true>(g, omega<R>(prm), d2q9::force<R>(prm));
+    else
+        collide<R, false>(g, omega<R>(prm), d2q9::force<R>(prm));
+#pragma unroll
+    for (int q = 0; q < 9; ++q) Store<S>::st(dst + q * plane + c, g[q]);
+}
+
+template <class S, int V, bool FORCE, class I>
+__device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restrict__ dst,
+                                         const uint16_t *__restrict__ links, int x0, int y, int nx, int ny,
+                                         I pitch, I plane, int periodic, const D2Q9Params &prm) {
+    using R = typename Store<S>::R;
+    const int lane = threadIdx.x & 31;
+    const int xa = min(x0, (int)pitch - V);  // threads beyond the row load a valid vector
+    int ym = y - 1, yp = y + 1;
+    if (ym < 0) ym = (periodic & 2) ? ny - 1 : 0;
+    if (yp >= ny) yp = (periodic & 2) ? 0 : ny - 1;
+    const I r0 = (I)y * pitch, rm = (I)ym * pitch, rp = (I)yp * pitch;
+
+    R f[9][V];
+    R a1[V], a5[V], a8[V], b3[V], b6[V], b7[V];
+    ld_pack<S, V>(src + 0 * plane + r0 + xa, f[0]);
+    ld_pack<S, V>(src + 2 * plane + rm + xa, f[2]);
+    ld_pack<S, V>(src + 4 * plane + rp + xa, f[4]);
+    ld_pack<S, V>(src + 1 * plane + r0 + xa, a1);
+    ld_pack<S, V>(src + 5 * plane + rm + xa, a5);
+    ld_pack<S, V>(src + 8 * plane + rp + xa, a8);
+    ld_pack<S, V>(src + 3 * plane + r0 + xa, b3);
+    ld_pack<S, V>(src + 6 * plane + rm + xa, b6);
+    ld_pack<S, V>(src + 7 * plane + rp + xa, b7);
+    uint32_t L[V];
+    ld_links<V>(links + r0 + xa, L);
+
+    // populations moving +x come from x-1: the previous lane's last element
+    R p1 = __shfl_up_sync(0xffffffffu, a1[V - 1], 1);
+    R p5 = __shfl_up_sync(0xffffffffu, a5[V - 1], 1);
+    R p8 = __shfl_up_sync(0xffffffffu, a8[V - 1], 1);
+    // populations moving -x come from x+V: the next lane's first element
+    R n3 = __shfl_down_sync(0xffffffffu, b3[0], 1);
+    R n6 = __shfl_down_sync(0xffffffffu, b6[0], 1);
+    R n7 = __shfl_down_sync(0xffffffffu, b7[0], 1);
+    if (lane == 0) {
+        const int xm = max(x0 - 1, 0);
+        p1 = Store<S>::ld(src + 1 * plane + r0 + xm);
+        p5 = Store<S>::ld(src + 5 * plane + rm + xm);
+        p8 = Store<S>::ld(src + 8 * plane + rp + xm);
+    }
+    if (lane == 31) {
+        const int xq = min(x0 + V, (int)pitch - 1);
+        n3 = Store<S>::ld(src + 3 * plane + r0 + xq);
+        n6 = Store<S>::ld(src + 6 * plane + rm + xq);
+        n7 = Store<S>::ld(src + 7 * plane + rp + xq);
+    }
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+        f[1][k] = k == 0 ? p1 : a1[k - 1];
+        f[5][k] = k == 0 ? p5 : a5[k - 1];
+        f[8][k] = k == 0 ? p8 : a8[k - 1];
+        f[3][k] = k == V - 1 ? n3 : b3[k + 1];
+        f[6][k] = k == V - 1 ? n6 : b6[k + 1];
+        f[7][k] = k == V - 1 ? n7 : b7[k + 1];
+    }
+
+    const bool special = x0 == 0 || x0 + V - 1 >= nx - 1;
+    if (special) {
+        // first / last column or row padding: per-cell path with wrap and edge handling
+        for (int k = 0; k < V; ++k)
+            if (x0 + k < nx) scalar_cell<S, I>(src, dst, links, x0 + k, y, nx, ny, pitch, plane, periodic, prm, FORCE);
+        return;
+    }
+
+    uint32_t any = 0;
+#pragma unroll
+    for (int k = 0; k < V; ++k) any |= L[k];
+    bool solid_any = false;
+    if (any) {
+        const Vec2<R> uw = wall_u<R>(prm);
+#pragma unroll
+        for (int q = 1; q < 9; ++q) {
+            uint32_t hit = 0;
+#pragma unroll
+            for (int k = 0; k < V; ++k) hit |= L[k] != LINK_SOLID ? (L[k] >> (q - 1)) & 1u : 0u;
+            if (hit) {
+                R own[V];
+                ld_pack<S, V>(src + opp(q) * plane + r0 + x0, own);
+#pragma unroll
+                for (int k = 0; k < V; ++k) {
+                    if (L[k] != LINK_SOLID && ((L[k] >> (q - 1)) & 1u)) {
+                        R v = own[k];
+                        if ((L[k] >> (q + 7)) & 1u) v += (R)6 * w<R>(q) * ((R)cx(q) * uw.x + (R)cy(q) * uw.y);
+                        f[q][k] = v;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < V; ++k) solid_any |= L[k] == LINK_SOLID;
+    }
+
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+        R g[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) g[q] = f[q][k];
+        collide<R, FORCE>(g, omega<R>(prm), force<R>(prm));
+#pragma unroll
+        for (int q = 0; q < 9; ++q) f[q][k] = g[q];
+    }
+
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        if (solid_any) {
+            R own[V];
+            ld_pack<S, V>(src + q * plane + r0 + x0, own);
+#pragma unroll
+            for (int k = 0; k < V; ++k)
+                if (L[k] == LINK_SOLID) f[q][k] = own[k];
+        }
+        st_pack<S, V>(dst + q * plane + r0 + x0, f[q]);
+    }
+}
+
+}  // namespace d2q9
+}  // namespace lbm

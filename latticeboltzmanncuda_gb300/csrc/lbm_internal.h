@@ -97,8 +97,13 @@ struct lbm_ctx {
     void *staging = nullptr;         // host-layout staging buffer, grown on demand
     size_t staging_bytes = 0;
 
+    // D2Q9 step launch shape (set by the autotuner or lbm_set_launch)
     int block_threads = 256;
     int cells_per_thread = 1;
+    int rows_per_block = 1;
+    bool tuned = false;
+    bool alternate_sweeps = true;  // visit rows in alternating order on successive steps
+    unsigned sweep = 0;
 
     size_t device_bytes = 0;
 };
@@ -120,6 +125,8 @@ D2Q9Params d2q9_params(const lbm_desc &d);
 cudaError_t d2q9_build_links(lbm_ctx *ctx);
 cudaError_t d2q9_init_equilibrium(lbm_ctx *ctx, const float *rho_d, const float *ux_d, const float *uy_d);
 cudaError_t d2q9_step(lbm_ctx *ctx, int nsteps);
+cudaError_t d2q9_autotune(lbm_ctx *ctx, bool force_retune);
+bool d2q9_shape_valid(const lbm_ctx *ctx, int v, int tx, int ty);
 cudaError_t d2q9_moments(lbm_ctx *ctx, float *rho_d, float *ux_d, float *uy_d);
 cudaError_t d2q9_conservation(lbm_ctx *ctx, double *out_d);
 cudaError_t d2q9_load(lbm_ctx *ctx, const void *src_d, int src_dtype, int aos);

@@ -194,3 +194,85 @@ def test_steps_are_deterministic():
             L.step(100)
             outs.append(L.retrieve_populations())
     assert np.array_equal(outs[0], outs[1])
+
+
+SHAPES = [(1, 256, 1), (1, 128, 2), (2, 64, 1), (2, 32, 4), (4, 32, 1), (4, 64, 2), (4, 128, 1), (8, 32, 1)]
+
+
+def shape_ok(dtype, v):
+    return v == 1 or (dtype == "f32" and v in (2, 4)) or (dtype in ("f16s", "bf16s") and v in (2, 4, 8)) or \
+        (dtype == "f64" and v == 2)
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("name", ["closed_box", "channel_force", "cavity_lid", "periodic_xy_force", "open_edges",
+                                  "periodic_y_moving"])
+def test_every_launch_shape_fp64_exact(name, shape):
+    """Scalar and vectorised paths (odd widths, wrap and walls inside and at the edges of a vector,
+    solid cells inside vectors) all match the FP64 oracle."""
+    if not shape_ok("f64", shape[0]):
+        pytest.skip("shape not available for FP64 storage")
+    nx, ny, builder, periodic, force, wall, tau, steps = CASES[name]
+    (tau,), force, wall = f32(tau), f32(*force), f32(*wall)
+    flags = build_flags(name, nx, ny, builder)
+    f0 = random_state(nx, ny, zlib.crc32(name.encode()))
+    ref = oracle.d2q9_run(f0, flags, tau, steps, periodic=periodic, force=force, wall_velocity=wall)
+    with lbm.Lattice(nx, ny, dtype="f64", tau=tau, periodic=periodic, body_force=(*force, 0),
+                     wall_velocity=(*wall, 0)) as L:
+        L.set_flags(flags)
+        L.load_populations(f0)
+        L.set_launch(*shape)
+        L.step(steps)
+        got = L.retrieve_populations(np.float64)
+    fluid = flags == 0
+    assert np.max(np.abs(got - ref)[:, fluid]) <= 1e-12
+    # solid cells keep their initial populations in both buffers
+    assert np.array_equal(got[:, ~fluid], f0[:, ~fluid]) or np.max(np.abs(got - f0)[:, ~fluid]) < 1e-15
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f16s", "bf16s"])
+def test_shapes_and_sweep_orders_agree_bitwise(dtype):
+    """The update of a cell does not depend on the launch shape or on the row order: every shape
+    and both sweep orders give bit-identical populations."""
+    nx, ny = 203, 77
+    flags, _ = lbm.gen_channel(nx, ny, 5, 3.0, 7.0, 4)
+    flags[ny // 2, :] = np.where(np.arange(nx) % 9 == 0, lbm.MOVING_WALL, flags[ny // 2, :])
+    outs = {}
+    for shape in SHAPES:
+        if not shape_ok(dtype, shape[0]):
+            continue
+        for alt in (True, False):
+            with lbm.Lattice(nx, ny, dtype=dtype, tau=0.58, periodic=1, body_force=(2e-5, 1e-6, 0),
+                             wall_velocity=(0.02, 0, 0)) as L:
+                L.set_flags(flags)
+                L.init_equilibrium()
+                L.set_launch(*shape)
+                L.set_sweep_alternation(alt)
+                L.step(41)
+                outs[(shape, alt)] = L.retrieve_populations()
+    first = next(iter(outs.values()))
+    for k, v in outs.items():
+        assert np.array_equal(v, first), k
+
+
+def test_autotune_picks_a_valid_shape_and_keeps_state():
+    nx, ny = 512, 256
+    flags, _ = lbm.gen_channel(nx, ny, 6, 4, 9, 8)
+    with lbm.Lattice(nx, ny, tau=0.6, periodic=1) as L:
+        L.set_flags(flags)
+        L.init_equilibrium()
+        before = L.retrieve_populations()
+        v, tx, ty = L.autotune(retune=True)
+        assert v in (1, 2, 4) and tx % 32 == 0 and tx * ty <= 256
+        assert L.info()["tuned"] == 1
+        assert np.array_equal(L.retrieve_populations(), before)  # tuning leaves the state alone
+
+
+def test_bad_launch_shape_rejected():
+    with lbm.Lattice(64, 8, dtype="f64") as L:
+        with pytest.raises(lbm.LBMError):
+            L.set_launch(4, 64, 1)  # FP64 vectors are 2 wide
+        with pytest.raises(lbm.LBMError):
+            L.set_launch(2, 48, 1)  # not a multiple of 32
+        with pytest.raises(lbm.LBMError):
+            L.set_launch(2, 256, 2)  # more than 256 threads
