@@ -12,6 +12,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -369,6 +371,8 @@ void load_tune_file() {
 void save_tune_file() {
     const std::string path = tune_path();
     if (path.empty()) return;
+    const size_t slash = path.rfind('/');
+    if (slash != std::string::npos && slash > 0) mkdir(path.substr(0, slash).c_str(), 0755);  // may exist
     const std::string tmp = path + ".tmp";
     FILE *fp = std::fopen(tmp.c_str(), "w");
     if (!fp) return;
@@ -506,6 +510,17 @@ bool d2q9_shape_valid(const lbm_ctx *ctx, int v, int tx, int ty) {
 cudaError_t d2q9_autotune(lbm_ctx *ctx, bool force_retune) {
     const char *env = std::getenv("LBM_AUTOTUNE");
     const std::string key = tune_key(ctx);
+    // LBM_D2Q9_LAUNCH="v,tx,ty" fixes the shape (reproducible profiling); ignored when not valid
+    if (const char *fixed = std::getenv("LBM_D2Q9_LAUNCH")) {
+        Shape sh{0, 0, 0};
+        if (std::sscanf(fixed, "%d,%d,%d", &sh.v, &sh.tx, &sh.ty) == 3 && d2q9_shape_valid(ctx, sh.v, sh.tx, sh.ty)) {
+            ctx->cells_per_thread = sh.v;
+            ctx->block_threads = sh.tx;
+            ctx->rows_per_block = sh.ty;
+            ctx->tuned = true;
+            return cudaSuccess;
+        }
+    }
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         load_tune_file();
