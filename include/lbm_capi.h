@@ -200,6 +200,30 @@ LBM_API lbm_status lbm_moments(lbm_ctx *ctx, float *host_rho, float *host_ux, fl
 /* FP64 sums over non-solid cells of the stored populations: mass, momentum x, y, z. */
 LBM_API lbm_status lbm_conservation(lbm_ctx *ctx, double host_out[4]);
 
+/* ---------------------------------------------------------------- allocation-free reduction */
+/* No counterpart in the reference.  Mass and momentum sums (FP64) of a D2Q9 population buffer
+ * over the fluid cells, for callers that cannot allocate device memory while they run: an
+ * application that gives the solver a fixed, fully accounted device budget (an embedding
+ * framework that owns all device memory, a serving loop admitting work against a memory budget),
+ * or a loop with a latency bound, where cudaMalloc / cudaFree would synchronise the device.
+ * The call allocates nothing: every buffer is the caller's, in device memory of the current
+ * device, and the per-block partial sums go to a fixed array that the library keeps in device
+ * memory (a static array of LBM_NOALLOC_MAX_ROWS / 4 blocks, 192 KiB, held on every GPU that loads
+ * the library until the process exits).
+ *   dev_populations  unshifted populations, dev_populations[q][ny][row_pitch] (float for LBM_F32,
+ *                    double for LBM_F64), q in the D2Q9 order of this header
+ *   dev_flags        D2Q9 flags [ny][nx]; only LBM_FLUID cells are summed
+ *   dev_out          3 doubles: mass, momentum x, momentum y (written on `stream`)
+ *   stream           cudaStream_t (NULL: the legacy default stream)
+ * ny above LBM_NOALLOC_MAX_ROWS is rejected with LBM_ERR_INVALID.  The first call on a device looks
+ * up the array's device address (with that device current); make that first call before any stream
+ * capture.  All calls share the one array: calls whose work overlaps on the GPU race with each
+ * other; calls in one stream, or otherwise ordered, do not. */
+#define LBM_NOALLOC_MAX_ROWS 32768
+LBM_API lbm_status lbm_d2q9_conservation_noalloc(const void *dev_populations, int32_t dtype,
+                                                 const uint8_t *dev_flags, int32_t nx, int32_t ny,
+                                                 int64_t row_pitch, double *dev_out, void *stream);
+
 /* ---------------------------------------------------------------- seeded geometry generators */
 /* Channel of nx x ny: walls on rows 0 and ny-1, ndisks non-overlapping disks (x-periodic
  * distance), centres uniform in [0,nx) x [0,ny), radius uniform in [rmin, rmax]; a cell is

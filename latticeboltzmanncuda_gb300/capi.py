@@ -91,6 +91,7 @@ SIGNATURES = [
     ("lbm_set_sweep_alternation", _S, [_P, _I32]),
     ("lbm_moments", _S, [_P, _P, _P, _P, _P]),
     ("lbm_conservation", _S, [_P, _P]),
+    ("lbm_d2q9_conservation_noalloc", _S, [_P, _I32, _P, _I32, _I32, _I64, _P, _P]),
     ("lbm_gen_channel", _S, [_I32, _I32, _I32, _F, _F, _U64, _P, _P]),
     ("lbm_gen_cavity", _S, [_I32, _I32, _P]),
     ("lbm_gen_disks_fraction", _S, [_I32, _I32, _F, _F, _F, _U64, _P, _P]),
