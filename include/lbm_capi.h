@@ -110,6 +110,7 @@ typedef struct lbm_info {
     int32_t cells_per_thread; /* consecutive cells per thread, */
     int32_t rows_per_block;   /* rows per block */
     int32_t tuned;            /* 1 once the shape has been chosen */
+    int32_t l2_policy;        /* L2 eviction hints of the vectorised path (see lbm_set_launch) */
 } lbm_info;
 
 /* ---------------------------------------------------------------- context life cycle */
@@ -182,10 +183,12 @@ LBM_API lbm_status lbm_apply(lbm_ctx *ctx, int32_t op);
  * $LBM_TUNE_CACHE (default ~/.cache/lbm_gb300_tune.json; empty: no file).  LBM_AUTOTUNE=0 skips the
  * timing and uses a fixed default shape.  lbm_autotune() runs the tuner now (retune != 0 ignores the
  * caches); lbm_set_launch() fixes a shape (cells_per_thread in 1,2,4,8; block_threads a multiple of
- * 32; block_threads * rows_per_block <= 256). */
+ * 32; block_threads * rows_per_block <= 256) and the L2 eviction hints of the vectorised path
+ * (l2_policy 0: none; 1: loads evict-first, stores evict-last; 2: loads evict-first; the scalar
+ * path, cells_per_thread 1, takes 0 only). */
 LBM_API lbm_status lbm_autotune(lbm_ctx *ctx, int32_t retune);
 LBM_API lbm_status lbm_set_launch(lbm_ctx *ctx, int32_t cells_per_thread, int32_t block_threads,
-                                  int32_t rows_per_block);
+                                  int32_t rows_per_block, int32_t l2_policy);
 /* D2Q9: visit rows in alternating order on successive steps (default 1), so each step starts on
  * the rows that the previous step wrote last and that are still in L2. */
 LBM_API lbm_status lbm_set_sweep_alternation(lbm_ctx *ctx, int32_t enabled);

@@ -176,12 +176,13 @@ class Lattice:
         self._call("lbm_apply", int(op))
 
     def autotune(self, retune=False):
+        """Run the launch-shape tuner; returns (cells_per_thread, block_threads, rows_per_block, l2_policy)."""
         self._call("lbm_autotune", int(bool(retune)))
         i = self.info()
-        return i["cells_per_thread"], i["block_threads"], i["rows_per_block"]
+        return i["cells_per_thread"], i["block_threads"], i["rows_per_block"], i["l2_policy"]
 
-    def set_launch(self, cells_per_thread, block_threads, rows_per_block=1):
-        self._call("lbm_set_launch", int(cells_per_thread), int(block_threads), int(rows_per_block))
+    def set_launch(self, cells_per_thread, block_threads, rows_per_block=1, l2_policy=0):
+        self._call("lbm_set_launch", int(cells_per_thread), int(block_threads), int(rows_per_block), int(l2_policy))
 
     def set_sweep_alternation(self, enabled):
         self._call("lbm_set_sweep_alternation", int(bool(enabled)))

@@ -57,7 +57,7 @@ class Info(ctypes.Structure):
                 ("state_bytes", ctypes.c_int64), ("device_bytes", ctypes.c_int64),
                 ("bytes_per_update", ctypes.c_int64), ("steps_done", ctypes.c_int64),
                 ("block_threads", ctypes.c_int32), ("cells_per_thread", ctypes.c_int32),
-                ("rows_per_block", ctypes.c_int32), ("tuned", ctypes.c_int32)]
+                ("rows_per_block", ctypes.c_int32), ("tuned", ctypes.c_int32), ("l2_policy", ctypes.c_int32)]
 
 
 # exported symbols and their signatures: (name, restype, argtypes)
@@ -87,7 +87,7 @@ SIGNATURES = [
     ("lbm_step", _S, [_P, _I32]),
     ("lbm_apply", _S, [_P, _I32]),
     ("lbm_autotune", _S, [_P, _I32]),
-    ("lbm_set_launch", _S, [_P, _I32, _I32, _I32]),
+    ("lbm_set_launch", _S, [_P, _I32, _I32, _I32, _I32]),
     ("lbm_set_sweep_alternation", _S, [_P, _I32]),
     ("lbm_moments", _S, [_P, _P, _P, _P, _P]),
     ("lbm_conservation", _S, [_P, _P]),

@@ -314,6 +314,7 @@ LBM_API lbm_status lbm_get_info(lbm_ctx *ctx, lbm_info *out) {
     out->cells_per_thread = ctx->cells_per_thread;
     out->rows_per_block = ctx->rows_per_block;
     out->tuned = ctx->tuned ? 1 : 0;
+    out->l2_policy = ctx->l2_policy;
     return LBM_OK;
 }
 
@@ -570,16 +571,18 @@ LBM_API lbm_status lbm_autotune(lbm_ctx *ctx, int32_t retune) {
     return LBM_OK;
 }
 
-LBM_API lbm_status lbm_set_launch(lbm_ctx *ctx, int32_t cells_per_thread, int32_t block_threads, int32_t rows_per_block) {
+LBM_API lbm_status lbm_set_launch(lbm_ctx *ctx, int32_t cells_per_thread, int32_t block_threads, int32_t rows_per_block,
+                                  int32_t l2_policy) {
     CHECK_CTX(ctx);
     if (ctx->desc.mode != LBM_D2Q9) return fail(ctx, LBM_ERR_UNSUPPORTED, "lbm_set_launch is D2Q9 only");
-    if (!d2q9_shape_valid(ctx, cells_per_thread, block_threads, rows_per_block))
+    if (!d2q9_shape_valid(ctx, cells_per_thread, block_threads, rows_per_block, l2_policy))
         return fail(ctx, LBM_ERR_INVALID, "launch shape " + std::to_string(cells_per_thread) + "x" +
                                               std::to_string(block_threads) + "x" + std::to_string(rows_per_block) +
                                               " is not valid for this domain and dtype");
     ctx->cells_per_thread = cells_per_thread;
     ctx->block_threads = block_threads;
     ctx->rows_per_block = rows_per_block;
+    ctx->l2_policy = l2_policy;
     ctx->tuned = true;
     return LBM_OK;
 }

@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(256) step_kernel(const S *__restrict__ src, S 
     d2q9::scalar_cell<S, I>(src, dst, links, x, y, nx, ny, pitch, plane, periodic, prm, FORCE);
 }
 
-template <class S, int V, bool FORCE>
+template <class S, int V, bool FORCE, int POL>
 __global__ void __launch_bounds__(256) step_vec_kernel(const S *__restrict__ src, S *__restrict__ dst,
                                                        const uint16_t *__restrict__ links, int nx, int ny,
                                                        int pitch, int plane, int periodic, D2Q9Params prm,
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(256) step_vec_kernel(const S *__restrict__ src
     if (row >= ny) return;  // uniform per warp: warps never straddle rows
     const int y = reverse ? ny - 1 - row : row;
     const int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * V;
-    d2q9::step_vec<S, V, FORCE, int>(src, dst, links, x0, y, nx, ny, pitch, plane, periodic, prm);
+    d2q9::step_vec<S, V, FORCE, int, POL>(src, dst, links, x0, y, nx, ny, pitch, plane, periodic, prm);
 }
 
 template <class S>
@@ -256,7 +256,7 @@ __global__ void store_kernel(const S *__restrict__ src, H *__restrict__ host, in
 // launch shapes and the autotuner
 // ------------------------------------------------------------------------------------------------
 struct Shape {
-    int v, tx, ty;
+    int v, tx, ty, pol;  // cells per thread, block shape, L2 policy of the vector path (0, 1, 2)
 };
 
 template <class S>
@@ -288,11 +288,15 @@ cudaError_t launch_one(lbm_ctx *ctx, const Shape &sh, const S *src, S *dst, int 
         return cudaGetLastError();
     }
     const int pitch = (int)ctx->pitch, plane = (int)ctx->plane;
+#define LBM_VEC_LAUNCH(VV, PP)                                                                                  \
+    if (force) step_vec_kernel<S, VV, true, PP><<<grid, block, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, reverse); \
+    else step_vec_kernel<S, VV, false, PP><<<grid, block, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, reverse);
 #define LBM_VEC_CASE(VV)                                                                                        \
     if constexpr (vec_ok<S>(VV)) {                                                                              \
         if (sh.v == VV) {                                                                                       \
-            if (force) step_vec_kernel<S, VV, true><<<grid, block, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, reverse); \
-            else step_vec_kernel<S, VV, false><<<grid, block, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, reverse); \
+            if (sh.pol == 1) { LBM_VEC_LAUNCH(VV, 1) }                                                          \
+            else if (sh.pol == 2) { LBM_VEC_LAUNCH(VV, 2) }                                                     \
+            else { LBM_VEC_LAUNCH(VV, 0) }                                                                      \
             return cudaGetLastError();                                                                          \
         }                                                                                                       \
     }
@@ -300,12 +304,13 @@ cudaError_t launch_one(lbm_ctx *ctx, const Shape &sh, const S *src, S *dst, int 
     LBM_VEC_CASE(4)
     LBM_VEC_CASE(8)
 #undef LBM_VEC_CASE
+#undef LBM_VEC_LAUNCH
     return cudaErrorInvalidValue;
 }
 
 template <class S>
 std::vector<Shape> candidates(const lbm_ctx *ctx) {
-    std::vector<Shape> c = {{1, 256, 1}, {1, 128, 2}};
+    std::vector<Shape> c = {{1, 256, 1, 0}, {1, 128, 2, 0}};
     if (!small_index(ctx)) return c;
     for (int v : {2, 4, 8}) {
         if (!vec_ok<S>(v) || ctx->pitch % v) continue;
@@ -313,8 +318,10 @@ std::vector<Shape> candidates(const lbm_ctx *ctx) {
         for (int tx : {32, 64, 128, 256}) {
             if (tx > 32 && tx / 2 >= per_row) continue;  // a block wider than two rows' worth is idle
             const int ty = std::max(1, std::min(256 / tx, 4));
-            c.push_back({v, tx, 1});
-            if (ty > 1 && tx * ty <= 256) c.push_back({v, tx, ty});
+            for (int pol = 0; pol < 3; ++pol) {
+                c.push_back({v, tx, 1, pol});
+                if (ty > 1 && tx * ty <= 256) c.push_back({v, tx, ty, pol});
+            }
         }
     }
     return c;
@@ -360,9 +367,9 @@ void load_tune_file() {
         const size_t end = txt.find('"', pos + 1);
         if (end == std::string::npos) break;
         const std::string key = txt.substr(pos + 1, end - pos - 1);
-        Shape sh{0, 0, 0};
-        if (std::sscanf(txt.c_str() + end + 1, " : [ %d , %d , %d ]", &sh.v, &sh.tx, &sh.ty) == 3 && sh.v > 0 && sh.tx > 0 &&
-            sh.ty > 0)
+        Shape sh{0, 0, 0, 0};
+        if (std::sscanf(txt.c_str() + end + 1, " : [ %d , %d , %d , %d ]", &sh.v, &sh.tx, &sh.ty, &sh.pol) == 4 && sh.v > 0 &&
+            sh.tx > 0 && sh.ty > 0)
             g_tune_cache[key] = sh;
         pos = end + 1;
     }
@@ -379,8 +386,8 @@ void save_tune_file() {
     std::fprintf(fp, "{\n");
     size_t i = 0;
     for (const auto &kv : g_tune_cache)
-        std::fprintf(fp, "  \"%s\": [%d, %d, %d]%s\n", kv.first.c_str(), kv.second.v, kv.second.tx, kv.second.ty,
-                     ++i < g_tune_cache.size() ? "," : "");
+        std::fprintf(fp, "  \"%s\": [%d, %d, %d, %d]%s\n", kv.first.c_str(), kv.second.v, kv.second.tx, kv.second.ty,
+                     kv.second.pol, ++i < g_tune_cache.size() ? "," : "");
     std::fprintf(fp, "}\n");
     std::fclose(fp);
     std::rename(tmp.c_str(), path.c_str());
@@ -403,7 +410,7 @@ cudaError_t tune(lbm_ctx *ctx) {
     const int64_t cells = (int64_t)ctx->desc.nx * ctx->desc.ny;
     const int reps = cells > (1 << 22) ? 6 : (cells > (1 << 18) ? 12 : 30);
     float best = 1e30f;
-    Shape pick = {1, 256, 1};
+    Shape pick = {1, 256, 1, 0};
     for (const Shape &sh : candidates<S>(ctx)) {
         for (int w = 0; w < 2 && err == cudaSuccess; ++w) err = launch_one<S>(ctx, sh, src, dst, w & 1);
         if (err != cudaSuccess) break;
@@ -426,6 +433,7 @@ cudaError_t tune(lbm_ctx *ctx) {
     ctx->cells_per_thread = pick.v;
     ctx->block_threads = pick.tx;
     ctx->rows_per_block = pick.ty;
+    ctx->l2_policy = pick.pol;
     ctx->tuned = true;
     return cudaSuccess;
 }
@@ -436,7 +444,7 @@ cudaError_t launch_step(lbm_ctx *ctx, int nsteps) {
         cudaError_t e = d2q9_autotune(ctx, false);
         if (e != cudaSuccess) return e;
     }
-    const Shape sh{ctx->cells_per_thread, ctx->block_threads, ctx->rows_per_block};
+    const Shape sh{ctx->cells_per_thread, ctx->block_threads, ctx->rows_per_block, ctx->l2_policy};
     for (int s = 0; s < nsteps; ++s) {
         const S *src = static_cast<const S *>(ctx->f[ctx->cur]);
         S *dst = static_cast<S *>(ctx->f[ctx->cur ^ 1]);
@@ -494,9 +502,9 @@ cudaError_t d2q9_init_equilibrium(lbm_ctx *ctx, const float *rho_d, const float 
     });
 }
 
-bool d2q9_shape_valid(const lbm_ctx *ctx, int v, int tx, int ty) {
-    if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256) return false;
-    if (v == 1) return true;
+bool d2q9_shape_valid(const lbm_ctx *ctx, int v, int tx, int ty, int pol) {
+    if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256 || pol < 0 || pol > 2) return false;
+    if (v == 1) return pol == 0;
     if (!small_index(ctx) || ctx->pitch % v) return false;
     switch (ctx->desc.dtype) {
         case LBM_F32: return vec_ok<float>(v);
@@ -512,11 +520,13 @@ cudaError_t d2q9_autotune(lbm_ctx *ctx, bool force_retune) {
     const std::string key = tune_key(ctx);
     // LBM_D2Q9_LAUNCH="v,tx,ty" fixes the shape (reproducible profiling); ignored when not valid
     if (const char *fixed = std::getenv("LBM_D2Q9_LAUNCH")) {
-        Shape sh{0, 0, 0};
-        if (std::sscanf(fixed, "%d,%d,%d", &sh.v, &sh.tx, &sh.ty) == 3 && d2q9_shape_valid(ctx, sh.v, sh.tx, sh.ty)) {
+        Shape sh{0, 0, 0, 0};
+        if (std::sscanf(fixed, "%d,%d,%d,%d", &sh.v, &sh.tx, &sh.ty, &sh.pol) >= 3 &&
+            d2q9_shape_valid(ctx, sh.v, sh.tx, sh.ty, sh.pol)) {
             ctx->cells_per_thread = sh.v;
             ctx->block_threads = sh.tx;
             ctx->rows_per_block = sh.ty;
+            ctx->l2_policy = sh.pol;
             ctx->tuned = true;
             return cudaSuccess;
         }
@@ -525,27 +535,30 @@ cudaError_t d2q9_autotune(lbm_ctx *ctx, bool force_retune) {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         load_tune_file();
         auto it = g_tune_cache.find(key);
-        if (!force_retune && it != g_tune_cache.end() && d2q9_shape_valid(ctx, it->second.v, it->second.tx, it->second.ty)) {
+        if (!force_retune && it != g_tune_cache.end() &&
+            d2q9_shape_valid(ctx, it->second.v, it->second.tx, it->second.ty, it->second.pol)) {
             ctx->cells_per_thread = it->second.v;
             ctx->block_threads = it->second.tx;
             ctx->rows_per_block = it->second.ty;
+            ctx->l2_policy = it->second.pol;
             ctx->tuned = true;
             return cudaSuccess;
         }
     }
     if (env && env[0] == '0' && !force_retune) {
         // tuning switched off: the default shape
-        const bool vec = d2q9_shape_valid(ctx, ctx->desc.dtype == LBM_F64 ? 2 : 4, 64, 1);
+        const bool vec = d2q9_shape_valid(ctx, ctx->desc.dtype == LBM_F64 ? 2 : 4, 64, 1, 0);
         ctx->cells_per_thread = vec ? (ctx->desc.dtype == LBM_F64 ? 2 : 4) : 1;
         ctx->block_threads = vec ? 64 : 256;
         ctx->rows_per_block = 1;
+        ctx->l2_policy = 0;
         ctx->tuned = true;
         return cudaSuccess;
     }
     cudaError_t e = dispatch(ctx->desc.dtype, [&](auto tag) { return tune<decltype(tag)>(ctx); });
     if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune_cache[key] = Shape{ctx->cells_per_thread, ctx->block_threads, ctx->rows_per_block};
+    g_tune_cache[key] = Shape{ctx->cells_per_thread, ctx->block_threads, ctx->rows_per_block, ctx->l2_policy};
     save_tune_file();
     return cudaSuccess;
 }

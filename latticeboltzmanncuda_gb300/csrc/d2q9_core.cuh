@@ -102,6 +102,85 @@ __device__ __forceinline__ void st_pack(S *__restrict__ p, const typename Store<
     *reinterpret_cast<T *>(p) = raw;
 }
 
+// L2 eviction-priority policies (PTX createpolicy) for the wide loads and stores of the step:
+//   POL 0  no hint
+//   POL 1  loads evict_first, stores evict_last: a step's reads are dead once consumed, its writes
+//          are the next (reversed) sweep's first reads, so the written half is kept in L2
+//   POL 2  loads evict_first, stores without hint
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+template <class T>
+__device__ __forceinline__ T ld_hint(const T *p, uint64_t pol);
+template <>
+__device__ __forceinline__ uint4 ld_hint<uint4>(const uint4 *p, uint64_t pol) {
+    uint4 r;
+    asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+                 : "l"(p), "l"(pol));
+    return r;
+}
+template <>
+__device__ __forceinline__ uint2 ld_hint<uint2>(const uint2 *p, uint64_t pol) {
+    uint2 r;
+    asm volatile("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;" : "=r"(r.x), "=r"(r.y) : "l"(p), "l"(pol));
+    return r;
+}
+template <>
+__device__ __forceinline__ unsigned int ld_hint<unsigned int>(const unsigned int *p, uint64_t pol) {
+    unsigned int r;
+    asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
+    return r;
+}
+__device__ __forceinline__ void st_hint(uint4 *p, uint4 v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z),
+                 "r"(v.w), "l"(pol)
+                 : "memory");
+}
+__device__ __forceinline__ void st_hint(uint2 *p, uint2 v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v2.u32 [%0], {%1, %2}, %3;" ::"l"(p), "r"(v.x), "r"(v.y), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_hint(unsigned int *p, unsigned int v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+
+template <class S, int V, int POL>
+__device__ __forceinline__ void ld_pack_pol(const S *__restrict__ p, typename Store<S>::R (&out)[V], uint64_t pol) {
+    if constexpr (POL == 0) {
+        ld_pack<S, V>(p, out);
+    } else {
+        using T = typename RawPack<sizeof(S) * V>::T;
+        const T raw = ld_hint<T>(reinterpret_cast<const T *>(p), pol);
+        S e[V];
+        memcpy(e, &raw, sizeof(raw));
+#pragma unroll
+        for (int k = 0; k < V; ++k) out[k] = Store<S>::to(e[k]);
+    }
+}
+
+template <class S, int V, int POL>
+__device__ __forceinline__ void st_pack_pol(S *__restrict__ p, const typename Store<S>::R (&in)[V], uint64_t pol) {
+    if constexpr (POL != 1) {
+        st_pack<S, V>(p, in);
+    } else {
+        using T = typename RawPack<sizeof(S) * V>::T;
+        S e[V];
+#pragma unroll
+        for (int k = 0; k < V; ++k) e[k] = Store<S>::from(in[k]);
+        T raw;
+        memcpy(&raw, e, sizeof(raw));
+        st_hint(reinterpret_cast<T *>(p), raw, pol);
+    }
+}
+
 template <int V>
 __device__ __forceinline__ void ld_links(const uint16_t *__restrict__ p, uint32_t (&L)[V]) {
     using T = typename RawPack<2 * V < 4 ? 4 : 2 * V>::T;

@@ -35,11 +35,13 @@ __device__ __forceinline__ void scalar_cell(const S *__restrict__ src, S *__rest
     for (int q = 0; q < 9; ++q) Store<S>::st(dst + q * plane + c, g[q]);
 }
 
-template <class S, int V, bool FORCE, class I>
+template <class S, int V, bool FORCE, class I, int POL = 0>
 __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restrict__ dst,
                                          const uint16_t *__restrict__ links, int x0, int y, int nx, int ny,
                                          I pitch, I plane, int periodic, const D2Q9Params &prm) {
     using R = typename Store<S>::R;
+    const uint64_t pol_ld = POL ? policy_evict_first() : 0;
+    const uint64_t pol_st = POL == 1 ? policy_evict_last() : 0;
     const int lane = threadIdx.x & 31;
     const int xa = min(x0, (int)pitch - V);  // threads beyond the row load a valid vector
     int ym = y - 1, yp = y + 1;
@@ -49,15 +51,15 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
 
     R f[9][V];
     R a1[V], a5[V], a8[V], b3[V], b6[V], b7[V];
-    ld_pack<S, V>(src + 0 * plane + r0 + xa, f[0]);
-    ld_pack<S, V>(src + 2 * plane + rm + xa, f[2]);
-    ld_pack<S, V>(src + 4 * plane + rp + xa, f[4]);
-    ld_pack<S, V>(src + 1 * plane + r0 + xa, a1);
-    ld_pack<S, V>(src + 5 * plane + rm + xa, a5);
-    ld_pack<S, V>(src + 8 * plane + rp + xa, a8);
-    ld_pack<S, V>(src + 3 * plane + r0 + xa, b3);
-    ld_pack<S, V>(src + 6 * plane + rm + xa, b6);
-    ld_pack<S, V>(src + 7 * plane + rp + xa, b7);
+    ld_pack_pol<S, V, POL>(src + 0 * plane + r0 + xa, f[0], pol_ld);
+    ld_pack_pol<S, V, POL>(src + 2 * plane + rm + xa, f[2], pol_ld);
+    ld_pack_pol<S, V, POL>(src + 4 * plane + rp + xa, f[4], pol_ld);
+    ld_pack_pol<S, V, POL>(src + 1 * plane + r0 + xa, a1, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 5 * plane + rm + xa, a5, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 8 * plane + rp + xa, a8, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 3 * plane + r0 + xa, b3, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 6 * plane + rm + xa, b6, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 7 * plane + rp + xa, b7, pol_ld);
     uint32_t L[V];
     ld_links<V>(links + r0 + xa, L);
 
@@ -146,7 +148,7 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
             for (int k = 0; k < V; ++k)
                 if (L[k] == LINK_SOLID) f[q][k] = own[k];
         }
-        st_pack<S, V>(dst + q * plane + r0 + x0, f[q]);
+        st_pack_pol<S, V, POL>(dst + q * plane + r0 + x0, f[q], pol_st);
     }
 }
 

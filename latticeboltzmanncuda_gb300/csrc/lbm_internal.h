@@ -101,6 +101,7 @@ struct lbm_ctx {
     int block_threads = 256;
     int cells_per_thread = 1;
     int rows_per_block = 1;
+    int l2_policy = 0;             // vector path: L2 eviction hints (0 none, 1 ld first/st last, 2 ld first)
     bool tuned = false;
     bool alternate_sweeps = true;  // visit rows in alternating order on successive steps
     unsigned sweep = 0;
@@ -126,7 +127,7 @@ cudaError_t d2q9_build_links(lbm_ctx *ctx);
 cudaError_t d2q9_init_equilibrium(lbm_ctx *ctx, const float *rho_d, const float *ux_d, const float *uy_d);
 cudaError_t d2q9_step(lbm_ctx *ctx, int nsteps);
 cudaError_t d2q9_autotune(lbm_ctx *ctx, bool force_retune);
-bool d2q9_shape_valid(const lbm_ctx *ctx, int v, int tx, int ty);
+bool d2q9_shape_valid(const lbm_ctx *ctx, int v, int tx, int ty, int pol);
 cudaError_t d2q9_moments(lbm_ctx *ctx, float *rho_d, float *ux_d, float *uy_d);
 cudaError_t d2q9_conservation(lbm_ctx *ctx, double *out_d);
 cudaError_t d2q9_load(lbm_ctx *ctx, const void *src_d, int src_dtype, int aos);

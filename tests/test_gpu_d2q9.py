@@ -196,7 +196,9 @@ def test_steps_are_deterministic():
     assert np.array_equal(outs[0], outs[1])
 
 
-SHAPES = [(1, 256, 1), (1, 128, 2), (2, 64, 1), (2, 32, 4), (4, 32, 1), (4, 64, 2), (4, 128, 1), (8, 32, 1)]
+# (cells per thread, block width, rows per block, L2 policy)
+SHAPES = [(1, 256, 1, 0), (1, 128, 2, 0), (2, 64, 1, 0), (2, 32, 4, 1), (4, 32, 1, 2), (4, 64, 2, 0),
+          (4, 128, 1, 1), (8, 32, 1, 1), (8, 64, 2, 2)]
 
 
 def shape_ok(dtype, v):
@@ -262,14 +264,16 @@ def test_autotune_picks_a_valid_shape_and_keeps_state():
         L.set_flags(flags)
         L.init_equilibrium()
         before = L.retrieve_populations()
-        v, tx, ty = L.autotune(retune=True)
-        assert v in (1, 2, 4) and tx % 32 == 0 and tx * ty <= 256
+        v, tx, ty, pol = L.autotune(retune=True)
+        assert v in (1, 2, 4) and tx % 32 == 0 and tx * ty <= 256 and pol in (0, 1, 2)
         assert L.info()["tuned"] == 1
         assert np.array_equal(L.retrieve_populations(), before)  # tuning leaves the state alone
 
 
 def test_bad_launch_shape_rejected():
     with lbm.Lattice(64, 8, dtype="f64") as L:
+        with pytest.raises(lbm.LBMError):
+            L.set_launch(1, 64, 1, 1)  # the scalar path has no L2 hints
         with pytest.raises(lbm.LBMError):
             L.set_launch(4, 64, 1)  # FP64 vectors are 2 wide
         with pytest.raises(lbm.LBMError):
