@@ -203,6 +203,42 @@ LBM_API lbm_status lbm_moments(lbm_ctx *ctx, float *host_rho, float *host_ux, fl
 /* FP64 sums over non-solid cells of the stored populations: mass, momentum x, y, z. */
 LBM_API lbm_status lbm_conservation(lbm_ctx *ctx, double host_out[4]);
 
+/* ---------------------------------------------------------------- batched domains */
+/* Many independent D2Q9 domains ("slots": own size, tau, force, wall velocity, periodicity and
+ * flags) advanced together, one kernel launch per time step for all live slots.  No counterpart
+ * in the reference, which runs one lattice per process; each slot computes exactly what a
+ * single-domain context with the same descriptor computes (bit-identical populations).  Slots
+ * are added (allocated, flags set, equilibrium rho = 1, u = 0) and removed between steps;
+ * lbm_batch_step advances every live slot.  The tile shape (cells per thread, block width, rows
+ * per block) is tuned on the batch at the first step, or fixed with lbm_batch_set_launch. */
+typedef struct lbm_batch lbm_batch;
+LBM_API lbm_status lbm_batch_create(int32_t dtype, int32_t device, void *stream, lbm_batch **out);
+LBM_API lbm_status lbm_batch_destroy(lbm_batch *b);
+LBM_API const char *lbm_batch_last_error(const lbm_batch *b);
+/* device bytes a slot of this size takes (two population buffers, link words, flags) */
+LBM_API int64_t lbm_batch_slot_bytes(int32_t dtype, int32_t nx, int32_t ny);
+/* desc: mode LBM_D2Q9, nx, ny, tau, periodic, body_force, wall_velocity (dtype, device and stream
+ * come from the batch); host_flags[ny][nx] may be NULL (all fluid) */
+LBM_API lbm_status lbm_batch_add(lbm_batch *b, const lbm_desc *desc, const uint8_t *host_flags,
+                                 int32_t *slot_out);
+LBM_API lbm_status lbm_batch_remove(lbm_batch *b, int32_t slot);
+LBM_API lbm_status lbm_batch_step(lbm_batch *b, int32_t nsteps);
+LBM_API lbm_status lbm_batch_autotune(lbm_batch *b);
+LBM_API lbm_status lbm_batch_set_launch(lbm_batch *b, int32_t cells_per_thread, int32_t block_threads,
+                                        int32_t rows_per_block);
+LBM_API lbm_status lbm_batch_synchronize(lbm_batch *b);
+LBM_API lbm_status lbm_batch_get_stream(lbm_batch *b, void **stream);
+/* out: live slots, cells, fluid cells, device bytes of the slots, cells per thread, block width,
+ * rows per block, tiles per step */
+LBM_API lbm_status lbm_batch_info(lbm_batch *b, int64_t out[8]);
+LBM_API lbm_status lbm_batch_slot_steps(lbm_batch *b, int32_t slot, int64_t *steps_done);
+LBM_API lbm_status lbm_batch_moments(lbm_batch *b, int32_t slot, float *host_rho, float *host_ux,
+                                     float *host_uy);
+LBM_API lbm_status lbm_batch_load_populations(lbm_batch *b, int32_t slot, const void *host,
+                                              int32_t host_dtype);
+LBM_API lbm_status lbm_batch_retrieve_populations(lbm_batch *b, int32_t slot, void *host,
+                                                  int32_t host_dtype);
+
 /* ---------------------------------------------------------------- allocation-free reduction */
 /* No counterpart in the reference.  Mass and momentum sums (FP64) of a D2Q9 population buffer
  * over the fluid cells, for callers that cannot allocate device memory while they run: an

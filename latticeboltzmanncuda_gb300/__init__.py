@@ -229,3 +229,115 @@ def gen_disks_fraction(flags, solid_fraction, rmin, rmax, seed):
     check(capi.lib().lbm_gen_disks_fraction(int(nx), int(ny), float(solid_fraction), float(rmin), float(rmax),
                                             ctypes.c_uint64(int(seed)), ptr(flags), ctypes.byref(ach)))
     return flags, float(ach.value)
+
+
+def _desc_for(nx, ny, tau, periodic=0, body_force=(0.0, 0.0), wall_velocity=(0.0, 0.0)):
+    d = capi.Desc()
+    capi.lib().lbm_desc_init(ctypes.byref(d))
+    d.mode = D2Q9
+    d.nx, d.ny, d.nz = int(nx), int(ny), 1
+    d.tau = float(tau)
+    d.periodic = int(periodic)
+    for k in range(2):
+        d.body_force[k] = float(body_force[k])
+        d.wall_velocity[k] = float(wall_velocity[k])
+    return d
+
+
+class Batch:
+    """Many independent D2Q9 domains advanced together, one launch per time step (lbm_batch_*)."""
+
+    def __init__(self, dtype="f32", device=0, stream=None):
+        self._b = ctypes.c_void_p()
+        check(capi.lib().lbm_batch_create(_dtype(dtype), int(device), stream, ctypes.byref(self._b)))
+        self.shapes = {}
+
+    def _chk(self, status):
+        if status != capi.OK:
+            raise LBMError(status, (capi.lib().lbm_batch_last_error(self._b) or b"").decode())
+
+    def close(self):
+        if getattr(self, "_b", None) and self._b.value:
+            capi.lib().lbm_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @staticmethod
+    def slot_bytes(dtype, nx, ny):
+        return int(capi.lib().lbm_batch_slot_bytes(_dtype(dtype), int(nx), int(ny)))
+
+    def add(self, nx, ny, tau, flags=None, periodic=0, body_force=(0.0, 0.0), wall_velocity=(0.0, 0.0)):
+        d = _desc_for(nx, ny, tau, periodic, body_force, wall_velocity)
+        fl = None if flags is None else np.ascontiguousarray(flags, dtype=np.uint8).reshape(-1)
+        if fl is not None and fl.size != nx * ny:
+            raise LBMError(capi.ERR_INVALID, "flags size mismatch")
+        slot = ctypes.c_int32()
+        self._chk(capi.lib().lbm_batch_add(self._b, ctypes.byref(d), ptr(fl), ctypes.byref(slot)))
+        self.shapes[slot.value] = (int(nx), int(ny))
+        return slot.value
+
+    def remove(self, slot):
+        self._chk(capi.lib().lbm_batch_remove(self._b, int(slot)))
+        self.shapes.pop(slot, None)
+
+    def step(self, n=1):
+        self._chk(capi.lib().lbm_batch_step(self._b, int(n)))
+
+    def autotune(self):
+        self._chk(capi.lib().lbm_batch_autotune(self._b))
+        return self.info()
+
+    def set_launch(self, cells_per_thread, block_threads, rows_per_block):
+        self._chk(capi.lib().lbm_batch_set_launch(self._b, int(cells_per_thread), int(block_threads), int(rows_per_block)))
+
+    def synchronize(self):
+        self._chk(capi.lib().lbm_batch_synchronize(self._b))
+
+    @property
+    def stream(self):
+        s = ctypes.c_void_p()
+        self._chk(capi.lib().lbm_batch_get_stream(self._b, ctypes.byref(s)))
+        return s.value or 0
+
+    def info(self):
+        out = np.zeros(8, np.int64)
+        self._chk(capi.lib().lbm_batch_info(self._b, ptr(out)))
+        keys = ("slots", "cells", "fluid_cells", "device_bytes", "cells_per_thread", "block_threads",
+                "rows_per_block", "tiles")
+        return dict(zip(keys, (int(v) for v in out)))
+
+    def steps_done(self, slot):
+        v = ctypes.c_int64()
+        self._chk(capi.lib().lbm_batch_slot_steps(self._b, int(slot), ctypes.byref(v)))
+        return v.value
+
+    def moments(self, slot):
+        nx, ny = self.shapes[slot]
+        out = [np.empty((ny, nx), np.float32) for _ in range(3)]
+        self._chk(capi.lib().lbm_batch_moments(self._b, int(slot), *[ptr(o) for o in out]))
+        return tuple(out)
+
+    def load_populations(self, slot, f):
+        f = np.asarray(f)
+        dt = F64 if f.dtype == np.float64 else F32
+        a = np.ascontiguousarray(f, dtype=np.float64 if dt == F64 else np.float32)
+        self._chk(capi.lib().lbm_batch_load_populations(self._b, int(slot), ptr(a), dt))
+
+    def retrieve_populations(self, slot, dtype=np.float32):
+        nx, ny = self.shapes[slot]
+        dtype = np.dtype(dtype)
+        a = np.empty((9, ny, nx), dtype)
+        self._chk(capi.lib().lbm_batch_retrieve_populations(self._b, int(slot), ptr(a),
+                                                            F64 if dtype == np.float64 else F32))
+        return a

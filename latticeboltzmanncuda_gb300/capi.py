@@ -91,6 +91,22 @@ SIGNATURES = [
     ("lbm_set_sweep_alternation", _S, [_P, _I32]),
     ("lbm_moments", _S, [_P, _P, _P, _P, _P]),
     ("lbm_conservation", _S, [_P, _P]),
+    ("lbm_batch_create", _S, [_I32, _I32, _P, _P]),
+    ("lbm_batch_destroy", _S, [_P]),
+    ("lbm_batch_last_error", ctypes.c_char_p, [_P]),
+    ("lbm_batch_slot_bytes", _I64, [_I32, _I32, _I32]),
+    ("lbm_batch_add", _S, [_P, _P, _P, _P]),
+    ("lbm_batch_remove", _S, [_P, _I32]),
+    ("lbm_batch_step", _S, [_P, _I32]),
+    ("lbm_batch_autotune", _S, [_P]),
+    ("lbm_batch_set_launch", _S, [_P, _I32, _I32, _I32]),
+    ("lbm_batch_synchronize", _S, [_P]),
+    ("lbm_batch_get_stream", _S, [_P, _P]),
+    ("lbm_batch_info", _S, [_P, _P]),
+    ("lbm_batch_slot_steps", _S, [_P, _I32, _P]),
+    ("lbm_batch_moments", _S, [_P, _I32, _P, _P, _P]),
+    ("lbm_batch_load_populations", _S, [_P, _I32, _P, _I32]),
+    ("lbm_batch_retrieve_populations", _S, [_P, _I32, _P, _I32]),
     ("lbm_d2q9_conservation_noalloc", _S, [_P, _I32, _P, _I32, _I32, _I64, _P, _P]),
     ("lbm_gen_channel", _S, [_I32, _I32, _I32, _F, _F, _U64, _P, _P]),
     ("lbm_gen_cavity", _S, [_I32, _I32, _P]),

@@ -1,0 +1,607 @@
+// Batched D2Q9: many independent domains of uneven size, tau, forcing and obstacle mask advance
+// together, one kernel launch per time step for all of them.
+//
+// Each domain (a "slot") owns its two population buffers and link words, allocated when it is
+// added, so slots come and go without moving anyone else's state (the serving loop admits and
+// retires requests between rounds).  A device table holds one descriptor per slot (sizes,
+// pointers, relaxation rate, force, wall velocity, periodicity, buffer parity).  The launch grid
+// is a flat list of tiles (slot, x-chunk, first row): every block updates TY rows x (TX * V)
+// cells of one slot with the same vectorised update as the single-domain kernel, so a domain's
+// populations are bit-identical whether it runs alone or in any mix.  Tiles are ordered slot by
+// slot, rows ascending; odd steps walk the list backwards (each step starts where the previous
+// one ended, on data still in L2).  The tile shape (V, TX, TY) is picked by the autotuner from
+// timings on the batch itself.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "d2q9_vec.cuh"
+#include "lbm_internal.h"
+
+namespace lbm {
+lbm_status set_thread_error(lbm_status s, const std::string &msg);
+}
+
+using namespace lbm;
+
+namespace {
+
+struct SlotDesc {  // device descriptor, one per slot
+    void *f[2];
+    const uint16_t *links;
+    int nx, ny, pitch, plane;
+    int periodic, force;
+    int cur;  // buffer holding the current state at the start of the launch sequence
+    int pad;
+    D2Q9Params prm;
+};
+
+struct Tile {
+    int slot, xchunk, y0, pad;
+};
+
+struct Slot {
+    bool live = false;
+    lbm_desc desc{};
+    int pitch = 0;
+    int64_t plane = 0;
+    void *f[2] = {nullptr, nullptr};
+    uint16_t *links = nullptr;
+    uint8_t *flags = nullptr;
+    int cur = 0;
+    int64_t steps_done = 0;
+    int64_t fluid = 0;
+    size_t bytes = 0;
+};
+
+template <class S, int V>
+__global__ void __launch_bounds__(256) batch_step_kernel(const SlotDesc *__restrict__ slots,
+                                                         const Tile *__restrict__ tiles, int ntiles, int step,
+                                                         int reverse) {
+    const int t = reverse ? ntiles - 1 - (int)blockIdx.x : (int)blockIdx.x;
+    const Tile tile = tiles[t];
+    const SlotDesc &D = slots[tile.slot];
+    const int y = tile.y0 + (int)threadIdx.y;
+    if (y >= D.ny) return;  // uniform per warp
+    const int x0 = (tile.xchunk * (int)blockDim.x + (int)threadIdx.x) * V;
+    const int cur = (D.cur + step) & 1;
+    const S *src = static_cast<const S *>(D.f[cur]);
+    S *dst = static_cast<S *>(D.f[cur ^ 1]);
+    if (D.force)
+        d2q9::step_vec<S, V, true, int>(src, dst, D.links, x0, y, D.nx, D.ny, D.pitch, D.plane, D.periodic, D.prm);
+    else
+        d2q9::step_vec<S, V, false, int>(src, dst, D.links, x0, y, D.nx, D.ny, D.pitch, D.plane, D.periodic, D.prm);
+}
+
+size_t dsize(int dtype) { return dtype == LBM_F64 ? 8 : (dtype == LBM_F32 ? 4 : 2); }
+
+template <class S>
+constexpr bool vec_ok(int v) {
+    return (sizeof(S) == 4 && (v == 2 || v == 4)) || (sizeof(S) == 2 && (v == 2 || v == 4 || v == 8)) ||
+           (sizeof(S) == 8 && v == 2);
+}
+
+}  // namespace
+
+struct lbm_batch {
+    int dtype = LBM_F32;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    std::vector<Slot> slots;
+    // device tables (rebuilt when the live set or the shape changes)
+    SlotDesc *desc_d = nullptr;
+    size_t desc_cap = 0;
+    Tile *tiles_d = nullptr;
+    size_t tiles_cap = 0;
+    int ntiles = 0;
+    bool dirty = true;
+    // tile shape
+    int v = 4, tx = 32, ty = 4;
+    bool tuned = false;
+    unsigned sweep = 0;
+    int64_t device_bytes = 0;
+    // persistent staging for slot I/O and a small result buffer (no allocation per call)
+    void *staging = nullptr;
+    size_t staging_bytes = 0;
+    double *result_d = nullptr;
+};
+
+namespace {
+
+lbm_status bfail(lbm_batch *b, lbm_status s, const std::string &m) {
+    if (b) b->err = m;
+    return lbm::set_thread_error(s, m);
+}
+
+#define BCUDA(b, call, what)                                                                                  \
+    do {                                                                                                      \
+        cudaError_t e_ = (call);                                                                              \
+        if (e_ != cudaSuccess)                                                                                \
+            return bfail(b, e_ == cudaErrorMemoryAllocation ? LBM_ERR_OOM : LBM_ERR_CUDA,                     \
+                         std::string(what) + ": " + cudaGetErrorString(e_));                                  \
+    } while (0)
+
+bool shape_ok(int dtype, int v, int tx, int ty) {
+    if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256) return false;
+    switch (dtype) {
+        case LBM_F32: return vec_ok<float>(v);
+        case LBM_F16S: return vec_ok<__half>(v);
+        case LBM_BF16S: return vec_ok<__nv_bfloat16>(v);
+        case LBM_F64: return vec_ok<double>(v);
+    }
+    return false;
+}
+
+// Slot set-up and I/O run the single-domain kernels on a temporary lbm_ctx that views the slot's
+// buffers (the view owns nothing).
+struct CtxView {
+    lbm_ctx c;
+    CtxView(lbm_batch *b, Slot &s) {
+        c.desc = s.desc;
+        c.desc.dtype = b->dtype;
+        c.device = b->device;
+        c.stream = b->stream;
+        c.cells = (int64_t)s.desc.nx * s.desc.ny;
+        c.pitch = s.pitch;
+        c.plane = s.plane;
+        c.q = 9;
+        c.elem = dsize(b->dtype);
+        c.f[0] = s.f[0];
+        c.f[1] = s.f[1];
+        c.cur = s.cur;
+        c.flags_d = s.flags;
+        c.links_d = s.links;
+        c.flags_set = true;
+        c.result_d = nullptr;
+    }
+    ~CtxView() {
+        // the view owns nothing
+        c.f[0] = c.f[1] = nullptr;
+        c.flags_d = nullptr;
+        c.links_d = nullptr;
+        c.staging = nullptr;
+        c.result_d = nullptr;
+        c.scratch.partials = nullptr;
+    }
+};
+
+lbm_status rebuild(lbm_batch *b) {
+    if (!b->dirty) return LBM_OK;
+    std::vector<SlotDesc> descs(b->slots.size());
+    std::vector<Tile> tiles;
+    const int cells_per_chunk = b->tx * b->v;
+    for (size_t i = 0; i < b->slots.size(); ++i) {
+        const Slot &s = b->slots[i];
+        SlotDesc &d = descs[i];
+        std::memset(&d, 0, sizeof(d));
+        if (!s.live) continue;
+        d.f[0] = s.f[0];
+        d.f[1] = s.f[1];
+        d.links = s.links;
+        d.nx = s.desc.nx;
+        d.ny = s.desc.ny;
+        d.pitch = s.pitch;
+        d.plane = (int)s.plane;
+        d.periodic = s.desc.periodic;
+        d.force = (s.desc.body_force[0] != 0.0f || s.desc.body_force[1] != 0.0f) ? 1 : 0;
+        d.cur = s.cur;
+        d.prm = d2q9_params(s.desc);
+        const int chunks = (s.pitch / b->v + b->tx - 1) / b->tx;
+        for (int y0 = 0; y0 < s.desc.ny; y0 += b->ty)
+            for (int xc = 0; xc < chunks; ++xc) tiles.push_back(Tile{(int)i, xc, y0, 0});
+    }
+    (void)cells_per_chunk;
+    BCUDA(b, cudaStreamSynchronize(b->stream), "batch: synchronize before table upload");
+    if (descs.size() > b->desc_cap) {
+        if (b->desc_d) cudaFree(b->desc_d);
+        b->desc_d = nullptr;
+        b->desc_cap = std::max<size_t>(descs.size(), 64);
+        BCUDA(b, cudaMalloc(&b->desc_d, b->desc_cap * sizeof(SlotDesc)), "batch: descriptor table");
+    }
+    if (tiles.size() > b->tiles_cap) {
+        if (b->tiles_d) cudaFree(b->tiles_d);
+        b->tiles_d = nullptr;
+        b->tiles_cap = std::max<size_t>(tiles.size() + tiles.size() / 4, 1024);
+        BCUDA(b, cudaMalloc(&b->tiles_d, b->tiles_cap * sizeof(Tile)), "batch: tile table");
+    }
+    if (!descs.empty())
+        BCUDA(b, cudaMemcpy(b->desc_d, descs.data(), descs.size() * sizeof(SlotDesc), cudaMemcpyHostToDevice),
+              "batch: upload descriptors");
+    if (!tiles.empty())
+        BCUDA(b, cudaMemcpy(b->tiles_d, tiles.data(), tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice),
+              "batch: upload tiles");
+    b->ntiles = (int)tiles.size();
+    b->dirty = false;
+    return LBM_OK;
+}
+
+template <class S>
+cudaError_t launch(lbm_batch *b, int step, int reverse) {
+    dim3 block(b->tx, b->ty);
+    dim3 grid((unsigned)b->ntiles);
+    if constexpr (vec_ok<S>(2)) {
+        if (b->v == 2) {
+            batch_step_kernel<S, 2><<<grid, block, 0, b->stream>>>(b->desc_d, b->tiles_d, b->ntiles, step, reverse);
+            return cudaGetLastError();
+        }
+    }
+    if constexpr (vec_ok<S>(4)) {
+        if (b->v == 4) {
+            batch_step_kernel<S, 4><<<grid, block, 0, b->stream>>>(b->desc_d, b->tiles_d, b->ntiles, step, reverse);
+            return cudaGetLastError();
+        }
+    }
+    if constexpr (vec_ok<S>(8)) {
+        if (b->v == 8) {
+            batch_step_kernel<S, 8><<<grid, block, 0, b->stream>>>(b->desc_d, b->tiles_d, b->ntiles, step, reverse);
+            return cudaGetLastError();
+        }
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_any(lbm_batch *b, int step, int reverse) {
+    switch (b->dtype) {
+        case LBM_F32: return launch<float>(b, step, reverse);
+        case LBM_F16S: return launch<__half>(b, step, reverse);
+        case LBM_BF16S: return launch<__nv_bfloat16>(b, step, reverse);
+        case LBM_F64: return launch<double>(b, step, reverse);
+    }
+    return cudaErrorInvalidValue;
+}
+
+// Time every candidate tile shape on the live batch (two launches per candidate with the step
+// parity kept even, so src -> dst is recomputed without changing the state).
+lbm_status tune(lbm_batch *b) {
+    struct Cand {
+        int v, tx, ty;
+    };
+    std::vector<Cand> cands;
+    for (int v : {2, 4, 8})
+        for (int tx : {32, 64, 128})
+            for (int ty : {1, 2, 4, 8})
+                if (shape_ok(b->dtype, v, tx, ty)) cands.push_back({v, tx, ty});
+    if (cands.empty()) return bfail(b, LBM_ERR_UNSUPPORTED, "batch: no tile shape for this dtype");
+    cudaEvent_t e0, e1;
+    BCUDA(b, cudaEventCreate(&e0), "batch tune: event");
+    BCUDA(b, cudaEventCreate(&e1), "batch tune: event");
+    float best = 1e30f;
+    Cand pick = cands[0];
+    for (const Cand &c : cands) {
+        b->v = c.v;
+        b->tx = c.tx;
+        b->ty = c.ty;
+        b->dirty = true;
+        lbm_status st = rebuild(b);
+        if (st != LBM_OK) return st;
+        if (b->ntiles == 0) break;
+        cudaError_t e = launch_any(b, 0, 0);
+        if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+        for (int r = 0; r < 4 && e == cudaSuccess; ++r) e = launch_any(b, 0, r & 1);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        BCUDA(b, e, "batch tune: launch");
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            pick = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->v = pick.v;
+    b->tx = pick.tx;
+    b->ty = pick.ty;
+    b->dirty = true;
+    b->tuned = true;
+    return rebuild(b);
+}
+
+lbm_status ensure_staging(lbm_batch *b, size_t bytes) {
+    if (!b->result_d) BCUDA(b, cudaMalloc(&b->result_d, 16 * sizeof(double)), "batch: result buffer");
+    if (b->staging_bytes >= bytes) return LBM_OK;
+    BCUDA(b, cudaStreamSynchronize(b->stream), "batch: synchronize before staging resize");
+    if (b->staging) cudaFree(b->staging);
+    b->staging = nullptr;
+    b->staging_bytes = 0;
+    BCUDA(b, cudaMalloc(&b->staging, bytes), "batch: staging");
+    b->staging_bytes = bytes;
+    return LBM_OK;
+}
+
+Slot *get_slot(lbm_batch *b, int32_t slot) {
+    if (!b || slot < 0 || (size_t)slot >= b->slots.size() || !b->slots[slot].live) return nullptr;
+    return &b->slots[slot];
+}
+
+}  // namespace
+
+extern "C" {
+
+LBM_API lbm_status lbm_batch_create(int32_t dtype, int32_t device, void *stream, lbm_batch **out) {
+    if (!out) return lbm::set_thread_error(LBM_ERR_INVALID, "null output");
+    *out = nullptr;
+    if (dsize(dtype) == 0 || dtype < LBM_F32 || dtype > LBM_F64) return lbm::set_thread_error(LBM_ERR_INVALID, "bad dtype");
+    lbm_batch *b = new lbm_batch();
+    b->dtype = dtype;
+    b->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) {
+        if (stream) {
+            b->stream = static_cast<cudaStream_t>(stream);
+        } else {
+            e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+            b->own_stream = e == cudaSuccess;
+        }
+    }
+    if (e != cudaSuccess) {
+        delete b;
+        return lbm::set_thread_error(LBM_ERR_CUDA, std::string("lbm_batch_create: ") + cudaGetErrorString(e));
+    }
+    b->v = dtype == LBM_F64 ? 2 : 4;
+    *out = b;
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_batch_destroy(lbm_batch *b) {
+    if (!b) return LBM_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (Slot &s : b->slots) {
+        if (!s.live) continue;
+        cudaFree(s.f[0]);
+        cudaFree(s.f[1]);
+        cudaFree(s.links);
+        cudaFree(s.flags);
+    }
+    cudaFree(b->desc_d);
+    cudaFree(b->tiles_d);
+    cudaFree(b->staging);
+    cudaFree(b->result_d);
+    if (b->own_stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return LBM_OK;
+}
+
+LBM_API const char *lbm_batch_last_error(const lbm_batch *b) { return b ? b->err.c_str() : ""; }
+
+LBM_API int64_t lbm_batch_slot_bytes(int32_t dtype, int32_t nx, int32_t ny) {
+    if (nx < 1 || ny < 1 || dsize(dtype) == 0) return -1;
+    const int64_t pitch = ((int64_t)nx + 31) / 32 * 32;
+    return 2 * 9 * pitch * ny * (int64_t)dsize(dtype) + pitch * ny * 2 + (int64_t)nx * ny;
+}
+
+LBM_API lbm_status lbm_batch_add(lbm_batch *b, const lbm_desc *desc, const uint8_t *host_flags, int32_t *slot_out) {
+    if (!b || !desc || !slot_out) return bfail(b, LBM_ERR_INVALID, "lbm_batch_add: null argument");
+    if (desc->mode != LBM_D2Q9 || desc->nz != 1 || desc->nx < 1 || desc->ny < 1)
+        return bfail(b, LBM_ERR_INVALID, "lbm_batch_add: batches hold D2Q9 domains (nz = 1)");
+    if (!(desc->tau > 0.5f)) return bfail(b, LBM_ERR_INVALID, "lbm_batch_add: tau must be > 0.5");
+    if (desc->periodic < 0 || desc->periodic > 3) return bfail(b, LBM_ERR_INVALID, "lbm_batch_add: periodic must be 0..3");
+    const int64_t pitch = ((int64_t)desc->nx + 31) / 32 * 32;
+    if (pitch * desc->ny * 9 >= (int64_t)INT32_MAX) return bfail(b, LBM_ERR_INVALID, "lbm_batch_add: domain too large for a batch");
+    BCUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    Slot s;
+    s.desc = *desc;
+    s.desc.dtype = b->dtype;
+    s.pitch = (int)pitch;
+    s.plane = pitch * desc->ny;
+    const size_t pop = (size_t)s.plane * 9 * dsize(b->dtype);
+    s.bytes = (size_t)lbm_batch_slot_bytes(b->dtype, desc->nx, desc->ny);
+    auto cleanup = [&]() {
+        cudaFree(s.f[0]);
+        cudaFree(s.f[1]);
+        cudaFree(s.links);
+        cudaFree(s.flags);
+    };
+    cudaError_t e = cudaMalloc(&s.f[0], pop);
+    if (e == cudaSuccess) e = cudaMalloc(&s.f[1], pop);
+    if (e == cudaSuccess) e = cudaMalloc(&s.links, (size_t)s.plane * sizeof(uint16_t));
+    if (e == cudaSuccess) e = cudaMalloc(&s.flags, (size_t)desc->nx * desc->ny);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cleanup();
+        return bfail(b, e == cudaErrorMemoryAllocation ? LBM_ERR_OOM : LBM_ERR_CUDA,
+                     std::string("lbm_batch_add: ") + cudaGetErrorString(e));
+    }
+    s.live = true;
+    // flags, link words, equilibrium at rho = 1, u = 0 through the single-domain kernels
+    if (host_flags) {
+        for (int64_t i = 0; i < (int64_t)desc->nx * desc->ny; ++i)
+            if (host_flags[i] > LBM_MOVING_WALL) {
+                cleanup();
+                return bfail(b, LBM_ERR_INVALID, "lbm_batch_add: flag values must be 0, 1 or 2");
+            }
+        e = cudaMemcpyAsync(s.flags, host_flags, (size_t)desc->nx * desc->ny, cudaMemcpyHostToDevice, b->stream);
+    } else {
+        e = cudaMemsetAsync(s.flags, 0, (size_t)desc->nx * desc->ny, b->stream);
+    }
+    if (e == cudaSuccess && ensure_staging(b, 0) != LBM_OK) e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) {
+        CtxView v(b, s);
+        v.c.result_d = b->result_d;
+        e = d2q9_build_links(&v.c);
+        if (e == cudaSuccess) e = d2q9_init_equilibrium(&v.c, nullptr, nullptr, nullptr);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+        s.fluid = v.c.fluid_cells;
+    }
+    if (e != cudaSuccess) {
+        cleanup();
+        return bfail(b, LBM_ERR_CUDA, std::string("lbm_batch_add: initialisation: ") + cudaGetErrorString(e));
+    }
+    int32_t id = -1;
+    for (size_t i = 0; i < b->slots.size(); ++i)
+        if (!b->slots[i].live) {
+            id = (int32_t)i;
+            break;
+        }
+    if (id < 0) {
+        id = (int32_t)b->slots.size();
+        b->slots.push_back(Slot());
+    }
+    b->slots[id] = s;
+    b->device_bytes += (int64_t)s.bytes;
+    b->dirty = true;
+    *slot_out = id;
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_batch_remove(lbm_batch *b, int32_t slot) {
+    Slot *s = get_slot(b, slot);
+    if (!s) return bfail(b, LBM_ERR_INVALID, "lbm_batch_remove: no such slot");
+    BCUDA(b, cudaStreamSynchronize(b->stream), "lbm_batch_remove: synchronize");
+    cudaFree(s->f[0]);
+    cudaFree(s->f[1]);
+    cudaFree(s->links);
+    cudaFree(s->flags);
+    b->device_bytes -= (int64_t)s->bytes;
+    *s = Slot();
+    b->dirty = true;
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_batch_set_launch(lbm_batch *b, int32_t cells_per_thread, int32_t block_threads,
+                                        int32_t rows_per_block) {
+    if (!b) return lbm::set_thread_error(LBM_ERR_INVALID, "null batch");
+    if (!shape_ok(b->dtype, cells_per_thread, block_threads, rows_per_block))
+        return bfail(b, LBM_ERR_INVALID, "lbm_batch_set_launch: shape not valid for this dtype");
+    b->v = cells_per_thread;
+    b->tx = block_threads;
+    b->ty = rows_per_block;
+    b->tuned = true;
+    b->dirty = true;
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_batch_autotune(lbm_batch *b) {
+    if (!b) return lbm::set_thread_error(LBM_ERR_INVALID, "null batch");
+    BCUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    return tune(b);
+}
+
+LBM_API lbm_status lbm_batch_step(lbm_batch *b, int32_t nsteps) {
+    if (!b) return lbm::set_thread_error(LBM_ERR_INVALID, "null batch");
+    if (nsteps < 0) return bfail(b, LBM_ERR_INVALID, "nsteps must be >= 0");
+    if (nsteps == 0) return LBM_OK;
+    BCUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    if (!b->tuned) {
+        lbm_status st = tune(b);
+        if (st != LBM_OK) return st;
+    }
+    lbm_status st = rebuild(b);
+    if (st != LBM_OK) return st;
+    if (b->ntiles > 0) {
+        for (int s = 0; s < nsteps; ++s) {
+            BCUDA(b, launch_any(b, s, (int)((b->sweep + s) & 1)), "batch step");
+        }
+    }
+    b->sweep += (unsigned)nsteps;
+    // every live slot advanced nsteps: its current buffer moves on by the parity of nsteps
+    for (Slot &s : b->slots)
+        if (s.live) {
+            s.cur = (s.cur + nsteps) & 1;
+            s.steps_done += nsteps;
+        }
+    if (nsteps & 1) b->dirty = true;  // descriptors carry the parity
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_batch_synchronize(lbm_batch *b) {
+    if (!b) return lbm::set_thread_error(LBM_ERR_INVALID, "null batch");
+    BCUDA(b, cudaStreamSynchronize(b->stream), "batch synchronize");
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_batch_get_stream(lbm_batch *b, void **stream) {
+    if (!b || !stream) return lbm::set_thread_error(LBM_ERR_INVALID, "null argument");
+    *stream = b->stream;
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_batch_info(lbm_batch *b, int64_t out[8]) {
+    if (!b || !out) return lbm::set_thread_error(LBM_ERR_INVALID, "null argument");
+    int64_t live = 0, cells = 0, fluid = 0;
+    for (const Slot &s : b->slots)
+        if (s.live) {
+            ++live;
+            cells += (int64_t)s.desc.nx * s.desc.ny;
+            fluid += s.fluid;
+        }
+    out[0] = live;
+    out[1] = cells;
+    out[2] = fluid;
+    out[3] = b->device_bytes;
+    out[4] = b->v;
+    out[5] = b->tx;
+    out[6] = b->ty;
+    out[7] = b->ntiles;
+    return LBM_OK;
+}
+
+// Per-slot host I/O through the single-domain conversion kernels on a view of the slot
+LBM_API lbm_status lbm_batch_moments(lbm_batch *b, int32_t slot, float *rho, float *ux, float *uy) {
+    Slot *s = get_slot(b, slot);
+    if (!s) return bfail(b, LBM_ERR_INVALID, "lbm_batch_moments: no such slot");
+    BCUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    const size_t n = (size_t)s->desc.nx * s->desc.ny;
+    lbm_status st = ensure_staging(b, 3 * n * sizeof(float));
+    if (st != LBM_OK) return st;
+    float *buf = static_cast<float *>(b->staging);
+    CtxView v(b, *s);
+    cudaError_t e = d2q9_moments(&v.c, buf, buf + n, buf + 2 * n);
+    float *host[3] = {rho, ux, uy};
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+        if (host[k]) e = cudaMemcpyAsync(host[k], buf + k * n, n * sizeof(float), cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    BCUDA(b, e, "lbm_batch_moments");
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_batch_retrieve_populations(lbm_batch *b, int32_t slot, void *host, int32_t host_dtype) {
+    Slot *s = get_slot(b, slot);
+    if (!s || !host || (host_dtype != LBM_F32 && host_dtype != LBM_F64))
+        return bfail(b, LBM_ERR_INVALID, "lbm_batch_retrieve_populations: bad arguments");
+    BCUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    const size_t bytes = (size_t)s->desc.nx * s->desc.ny * 9 * (host_dtype == LBM_F64 ? 8 : 4);
+    lbm_status st = ensure_staging(b, bytes);
+    if (st != LBM_OK) return st;
+    void *buf = b->staging;
+    CtxView v(b, *s);
+    cudaError_t e = d2q9_store(&v.c, buf, host_dtype, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, buf, bytes, cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    BCUDA(b, e, "lbm_batch_retrieve_populations");
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_batch_load_populations(lbm_batch *b, int32_t slot, const void *host, int32_t host_dtype) {
+    Slot *s = get_slot(b, slot);
+    if (!s || !host || (host_dtype != LBM_F32 && host_dtype != LBM_F64))
+        return bfail(b, LBM_ERR_INVALID, "lbm_batch_load_populations: bad arguments");
+    BCUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    const size_t bytes = (size_t)s->desc.nx * s->desc.ny * 9 * (host_dtype == LBM_F64 ? 8 : 4);
+    lbm_status st = ensure_staging(b, bytes);
+    if (st != LBM_OK) return st;
+    void *buf = b->staging;
+    CtxView v(b, *s);
+    cudaError_t e = cudaMemcpyAsync(buf, host, bytes, cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = d2q9_load(&v.c, buf, host_dtype, 0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    BCUDA(b, e, "lbm_batch_load_populations");
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_batch_slot_steps(lbm_batch *b, int32_t slot, int64_t *steps_done) {
+    Slot *s = get_slot(b, slot);
+    if (!s || !steps_done) return bfail(b, LBM_ERR_INVALID, "lbm_batch_slot_steps: bad arguments");
+    *steps_done = s->steps_done;
+    return LBM_OK;
+}
+
+}  // extern "C"
