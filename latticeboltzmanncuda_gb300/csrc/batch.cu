@@ -7,9 +7,10 @@
 // pointers, relaxation rate, force, wall velocity, periodicity, buffer parity).  The launch grid
 // is a flat list of tiles (slot, x-chunk, first row): every block updates TY rows x (TX * V)
 // cells of one slot with the same vectorised update as the single-domain kernel, so a domain's
-// populations are bit-identical whether it runs alone or in any mix.  Tiles are ordered slot by
-// slot, rows ascending; odd steps walk the list backwards (each step starts where the previous
-// one ended, on data still in L2).  The tile shape (V, TX, TY) is picked by the autotuner from
+// populations are bit-identical whether it runs alone or in any mix.  The grid is persistent:
+// SMs x resident blocks, each block walking the tile list with a grid stride.  Tiles are ordered
+// slot by slot, rows ascending; odd steps walk the list backwards (each step starts where the
+// previous one ended, on data still in L2).  The tile shape (V, TX, TY) is picked by the autotuner from
 // timings on the batch itself.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -58,23 +59,27 @@ struct Slot {
     size_t bytes = 0;
 };
 
+// Resident blocks walk the tile list (grid-stride); each tile's slot descriptor is copied into
+// registers, so no field is re-read from global memory after the population stores.
 template <class S, int V>
 __global__ void __launch_bounds__(256) batch_step_kernel(const SlotDesc *__restrict__ slots,
                                                          const Tile *__restrict__ tiles, int ntiles, int step,
                                                          int reverse) {
-    const int t = reverse ? ntiles - 1 - (int)blockIdx.x : (int)blockIdx.x;
-    const Tile tile = tiles[t];
-    const SlotDesc &D = slots[tile.slot];
-    const int y = tile.y0 + (int)threadIdx.y;
-    if (y >= D.ny) return;  // uniform per warp
-    const int x0 = (tile.xchunk * (int)blockDim.x + (int)threadIdx.x) * V;
-    const int cur = (D.cur + step) & 1;
-    const S *src = static_cast<const S *>(D.f[cur]);
-    S *dst = static_cast<S *>(D.f[cur ^ 1]);
-    if (D.force)
-        d2q9::step_vec<S, V, true, int>(src, dst, D.links, x0, y, D.nx, D.ny, D.pitch, D.plane, D.periodic, D.prm);
-    else
-        d2q9::step_vec<S, V, false, int>(src, dst, D.links, x0, y, D.nx, D.ny, D.pitch, D.plane, D.periodic, D.prm);
+    for (int i = (int)blockIdx.x; i < ntiles; i += (int)gridDim.x) {
+        const int t = reverse ? ntiles - 1 - i : i;
+        const Tile tile = tiles[t];
+        const SlotDesc D = slots[tile.slot];
+        const int y = tile.y0 + (int)threadIdx.y;
+        if (y >= D.ny) continue;  // uniform per warp
+        const int x0 = (tile.xchunk * (int)blockDim.x + (int)threadIdx.x) * V;
+        const int cur = (D.cur + step) & 1;
+        const S *src = static_cast<const S *>(D.f[cur]);
+        S *dst = static_cast<S *>(D.f[cur ^ 1]);
+        if (D.force)
+            d2q9::step_vec<S, V, true, int>(src, dst, D.links, x0, y, D.nx, D.ny, D.pitch, D.plane, D.periodic, D.prm);
+        else
+            d2q9::step_vec<S, V, false, int>(src, dst, D.links, x0, y, D.nx, D.ny, D.pitch, D.plane, D.periodic, D.prm);
+    }
 }
 
 size_t dsize(int dtype) { return dtype == LBM_F64 ? 8 : (dtype == LBM_F32 ? 4 : 2); }
@@ -103,6 +108,7 @@ struct lbm_batch {
     bool dirty = true;
     // tile shape
     int v = 4, tx = 32, ty = 4;
+    int grid = 0;  // resident blocks for the current shape (SMs x occupancy)
     bool tuned = false;
     unsigned sweep = 0;
     int64_t device_bytes = 0;
@@ -221,27 +227,31 @@ lbm_status rebuild(lbm_batch *b) {
     return LBM_OK;
 }
 
+template <class S, int V>
+cudaError_t launch_v(lbm_batch *b, int step, int reverse) {
+    dim3 block(b->tx, b->ty);
+    if (b->grid == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_step_kernel<S, V>, b->tx * b->ty, 0);
+        b->grid = std::max(1, sms * std::max(1, per_sm));
+    }
+    dim3 grid((unsigned)std::min(b->ntiles, b->grid));
+    batch_step_kernel<S, V><<<grid, block, 0, b->stream>>>(b->desc_d, b->tiles_d, b->ntiles, step, reverse);
+    return cudaGetLastError();
+}
+
 template <class S>
 cudaError_t launch(lbm_batch *b, int step, int reverse) {
-    dim3 block(b->tx, b->ty);
-    dim3 grid((unsigned)b->ntiles);
     if constexpr (vec_ok<S>(2)) {
-        if (b->v == 2) {
-            batch_step_kernel<S, 2><<<grid, block, 0, b->stream>>>(b->desc_d, b->tiles_d, b->ntiles, step, reverse);
-            return cudaGetLastError();
-        }
+        if (b->v == 2) return launch_v<S, 2>(b, step, reverse);
     }
     if constexpr (vec_ok<S>(4)) {
-        if (b->v == 4) {
-            batch_step_kernel<S, 4><<<grid, block, 0, b->stream>>>(b->desc_d, b->tiles_d, b->ntiles, step, reverse);
-            return cudaGetLastError();
-        }
+        if (b->v == 4) return launch_v<S, 4>(b, step, reverse);
     }
     if constexpr (vec_ok<S>(8)) {
-        if (b->v == 8) {
-            batch_step_kernel<S, 8><<<grid, block, 0, b->stream>>>(b->desc_d, b->tiles_d, b->ntiles, step, reverse);
-            return cudaGetLastError();
-        }
+        if (b->v == 8) return launch_v<S, 8>(b, step, reverse);
     }
     return cudaErrorInvalidValue;
 }
@@ -277,6 +287,7 @@ lbm_status tune(lbm_batch *b) {
         b->v = c.v;
         b->tx = c.tx;
         b->ty = c.ty;
+        b->grid = 0;
         b->dirty = true;
         lbm_status st = rebuild(b);
         if (st != LBM_OK) return st;
@@ -299,6 +310,7 @@ lbm_status tune(lbm_batch *b) {
     b->v = pick.v;
     b->tx = pick.tx;
     b->ty = pick.ty;
+    b->grid = 0;
     b->dirty = true;
     b->tuned = true;
     return rebuild(b);
@@ -474,6 +486,7 @@ LBM_API lbm_status lbm_batch_set_launch(lbm_batch *b, int32_t cells_per_thread, 
     b->v = cells_per_thread;
     b->tx = block_threads;
     b->ty = rows_per_block;
+    b->grid = 0;
     b->tuned = true;
     b->dirty = true;
     return LBM_OK;

@@ -160,8 +160,8 @@ __global__ void equilibrium_kernel(S *__restrict__ a, S *__restrict__ b, int nx,
     d2q9::equilibrium_shifted(r - (R)1, r, u, v, g);
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
-        d2q9::Store<S>::st(a + q * plane + c, g[q]);
-        d2q9::Store<S>::st(b + q * plane + c, g[q]);
+        d2q9::stq<S>(a + q * plane + c, q, g[q]);
+        d2q9::stq<S>(b + q * plane + c, q, g[q]);
     }
 }
 
@@ -177,7 +177,7 @@ __global__ void conservation_kernel(const S *__restrict__ src, const uint16_t *_
         if (links[c] == LINK_SOLID) continue;
         double g[9];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) g[q] = (double)d2q9::Store<S>::ld(src + q * plane + c);
+        for (int q = 0; q < 9; ++q) g[q] = (double)d2q9::ldq<S>(src + q * plane + c, q);
         double s = 0;
 #pragma unroll
         for (int q = 0; q < 9; ++q) s += g[q];
@@ -216,8 +216,8 @@ __global__ void load_kernel(S *__restrict__ a, S *__restrict__ b, const H *__res
             v = (R)host[q * n + (int64_t)y * nx + x];
         }
         R g = v - d2q9::w<R>(q);
-        d2q9::Store<S>::st(a + q * plane + c, g);
-        d2q9::Store<S>::st(b + q * plane + c, g);
+        d2q9::stq<S>(a + q * plane + c, q, g);
+        d2q9::stq<S>(b + q * plane + c, q, g);
     }
 }
 
@@ -239,7 +239,7 @@ __global__ void store_kernel(const S *__restrict__ src, H *__restrict__ host, in
         float *f = reinterpret_cast<float *>(rec + 12);
         for (int k = 0; k < 27; ++k) f[k] = 0.0f;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) f[aos_slot(q)] = (float)(d2q9::Store<S>::ld(src + q * plane + c) + d2q9::w<R>(q));
+        for (int q = 0; q < 9; ++q) f[aos_slot(q)] = (float)(d2q9::ldq<S>(src + q * plane + c, q) + d2q9::w<R>(q));
         uint8_t fl = flags ? flags[(int64_t)y * nx + x] : 0;
         rec[120] = 0;        // isReflected
         rec[121] = fl != 0;  // isInternal: solid cell
@@ -248,7 +248,7 @@ __global__ void store_kernel(const S *__restrict__ src, H *__restrict__ host, in
     } else {
 #pragma unroll
         for (int q = 0; q < 9; ++q)
-            host[q * n + (int64_t)y * nx + x] = (H)(d2q9::Store<S>::ld(src + q * plane + c) + d2q9::w<R>(q));
+            host[q * n + (int64_t)y * nx + x] = (H)(d2q9::ldq<S>(src + q * plane + c, q) + d2q9::w<R>(q));
     }
 }
 

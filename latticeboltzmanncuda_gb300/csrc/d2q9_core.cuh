@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "lbm_internal.h"
 
@@ -65,6 +66,34 @@ struct Store<__nv_bfloat16> {
     static __device__ __forceinline__ void st(__nv_bfloat16 *p, R v) { *p = __float2bfloat16_rn(v); }
 };
 
+// FP16 storage holds h_q = 1024 (f_q - w_q) / w_q: the deviations of all nine populations scale
+// with w_q, so dividing by w_q puts them in one range, and the factor 1024 keeps deviations down to
+// ~1e-7 of w_q out of FP16's subnormal range (|h| < 6.1e-5).  The other storage types hold
+// g_q = f_q - w_q unscaled (the factors below are compile-time 1).
+template <class S, class R>
+__device__ __forceinline__ R unscale(R v, int q) {
+    if constexpr (std::is_same<S, __half>::value)
+        return v * (w<R>(q) * (R)(1.0 / 1024.0));
+    else
+        return v;
+}
+template <class S, class R>
+__device__ __forceinline__ R scale(R v, int q) {
+    if constexpr (std::is_same<S, __half>::value)
+        return v * ((R)1024.0 / w<R>(q));
+    else
+        return v;
+}
+// population q of the stored buffer (shifted, unscaled) and back
+template <class S>
+__device__ __forceinline__ typename Store<S>::R ldq(const S *p, int q) {
+    return unscale<S>(Store<S>::ld(p), q);
+}
+template <class S>
+__device__ __forceinline__ void stq(S *p, int q, typename Store<S>::R v) {
+    Store<S>::st(p, scale<S>(v, q));
+}
+
 // V consecutive stored values moved as one 4-, 8- or 16-byte access (p aligned to V*sizeof(S))
 template <int B>
 struct RawPack;
@@ -82,21 +111,21 @@ struct RawPack<16> {
 };
 
 template <class S, int V>
-__device__ __forceinline__ void ld_pack(const S *__restrict__ p, typename Store<S>::R (&out)[V]) {
+__device__ __forceinline__ void ld_pack(const S *__restrict__ p, int q, typename Store<S>::R (&out)[V]) {
     using T = typename RawPack<sizeof(S) * V>::T;
     const T raw = __ldg(reinterpret_cast<const T *>(p));
     S e[V];
     memcpy(e, &raw, sizeof(raw));
 #pragma unroll
-    for (int k = 0; k < V; ++k) out[k] = Store<S>::to(e[k]);
+    for (int k = 0; k < V; ++k) out[k] = unscale<S>(Store<S>::to(e[k]), q);
 }
 
 template <class S, int V>
-__device__ __forceinline__ void st_pack(S *__restrict__ p, const typename Store<S>::R (&in)[V]) {
+__device__ __forceinline__ void st_pack(S *__restrict__ p, int q, const typename Store<S>::R (&in)[V]) {
     using T = typename RawPack<sizeof(S) * V>::T;
     S e[V];
 #pragma unroll
-    for (int k = 0; k < V; ++k) e[k] = Store<S>::from(in[k]);
+    for (int k = 0; k < V; ++k) e[k] = Store<S>::from(scale<S>(in[k], q));
     T raw;
     memcpy(&raw, e, sizeof(raw));
     *reinterpret_cast<T *>(p) = raw;
@@ -153,28 +182,30 @@ __device__ __forceinline__ void st_hint(unsigned int *p, unsigned int v, uint64_
 }
 
 template <class S, int V, int POL>
-__device__ __forceinline__ void ld_pack_pol(const S *__restrict__ p, typename Store<S>::R (&out)[V], uint64_t pol) {
+__device__ __forceinline__ void ld_pack_pol(const S *__restrict__ p, int q, typename Store<S>::R (&out)[V],
+                                            uint64_t pol) {
     if constexpr (POL == 0) {
-        ld_pack<S, V>(p, out);
+        ld_pack<S, V>(p, q, out);
     } else {
         using T = typename RawPack<sizeof(S) * V>::T;
         const T raw = ld_hint<T>(reinterpret_cast<const T *>(p), pol);
         S e[V];
         memcpy(e, &raw, sizeof(raw));
 #pragma unroll
-        for (int k = 0; k < V; ++k) out[k] = Store<S>::to(e[k]);
+        for (int k = 0; k < V; ++k) out[k] = unscale<S>(Store<S>::to(e[k]), q);
     }
 }
 
 template <class S, int V, int POL>
-__device__ __forceinline__ void st_pack_pol(S *__restrict__ p, const typename Store<S>::R (&in)[V], uint64_t pol) {
+__device__ __forceinline__ void st_pack_pol(S *__restrict__ p, int q, const typename Store<S>::R (&in)[V],
+                                            uint64_t pol) {
     if constexpr (POL != 1) {
-        st_pack<S, V>(p, in);
+        st_pack<S, V>(p, q, in);
     } else {
         using T = typename RawPack<sizeof(S) * V>::T;
         S e[V];
 #pragma unroll
-        for (int k = 0; k < V; ++k) e[k] = Store<S>::from(in[k]);
+        for (int k = 0; k < V; ++k) e[k] = Store<S>::from(scale<S>(in[k], q));
         T raw;
         memcpy(&raw, e, sizeof(raw));
         st_hint(reinterpret_cast<T *>(p), raw, pol);
@@ -227,20 +258,20 @@ __device__ __forceinline__ void gather(const S *__restrict__ src, uint32_t L, in
     if (ym < 0) ym = (periodic & 2) ? ny - 1 : 0;
     if (yp >= ny) yp = (periodic & 2) ? 0 : ny - 1;
     const int64_t r0 = (int64_t)y * pitch, rm = (int64_t)ym * pitch, rp = (int64_t)yp * pitch;
-    g[0] = Store<S>::ld(src + r0 + x);
-    g[1] = Store<S>::ld(src + 1 * plane + r0 + xm);
-    g[2] = Store<S>::ld(src + 2 * plane + rm + x);
-    g[3] = Store<S>::ld(src + 3 * plane + r0 + xp);
-    g[4] = Store<S>::ld(src + 4 * plane + rp + x);
-    g[5] = Store<S>::ld(src + 5 * plane + rm + xm);
-    g[6] = Store<S>::ld(src + 6 * plane + rm + xp);
-    g[7] = Store<S>::ld(src + 7 * plane + rp + xp);
-    g[8] = Store<S>::ld(src + 8 * plane + rp + xm);
+    g[0] = ldq<S>(src + r0 + x, 0);
+    g[1] = ldq<S>(src + 1 * plane + r0 + xm, 1);
+    g[2] = ldq<S>(src + 2 * plane + rm + x, 2);
+    g[3] = ldq<S>(src + 3 * plane + r0 + xp, 3);
+    g[4] = ldq<S>(src + 4 * plane + rp + x, 4);
+    g[5] = ldq<S>(src + 5 * plane + rm + xm, 5);
+    g[6] = ldq<S>(src + 6 * plane + rm + xp, 6);
+    g[7] = ldq<S>(src + 7 * plane + rp + xp, 7);
+    g[8] = ldq<S>(src + 8 * plane + rp + xm, 8);
     if (L) {
 #pragma unroll
         for (int q = 1; q < 9; ++q) {
             if (L & (1u << (q - 1))) {
-                R v = Store<S>::ld(src + opp(q) * plane + r0 + x);
+                R v = ldq<S>(src + opp(q) * plane + r0 + x, opp(q));
                 if (L & (1u << (q + 7))) v += (R)6 * w<R>(q) * ((R)cx(q) * uw.x + (R)cy(q) * uw.y);
                 g[q] = v;
             }

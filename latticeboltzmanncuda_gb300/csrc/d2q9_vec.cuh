@@ -32,7 +32,7 @@ __device__ __forceinline__ void scalar_cell(const S *__restrict__ src, S *__rest
     else
         collide<R, false>(g, omega<R>(prm), d2q9::force<R>(prm));
 #pragma unroll
-    for (int q = 0; q < 9; ++q) Store<S>::st(dst + q * plane + c, g[q]);
+    for (int q = 0; q < 9; ++q) stq<S>(dst + q * plane + c, q, g[q]);
 }
 
 template <class S, int V, bool FORCE, class I, int POL = 0>
@@ -51,15 +51,15 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
 
     R f[9][V];
     R a1[V], a5[V], a8[V], b3[V], b6[V], b7[V];
-    ld_pack_pol<S, V, POL>(src + 0 * plane + r0 + xa, f[0], pol_ld);
-    ld_pack_pol<S, V, POL>(src + 2 * plane + rm + xa, f[2], pol_ld);
-    ld_pack_pol<S, V, POL>(src + 4 * plane + rp + xa, f[4], pol_ld);
-    ld_pack_pol<S, V, POL>(src + 1 * plane + r0 + xa, a1, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 5 * plane + rm + xa, a5, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 8 * plane + rp + xa, a8, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 3 * plane + r0 + xa, b3, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 6 * plane + rm + xa, b6, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 7 * plane + rp + xa, b7, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 0 * plane + r0 + xa, 0, f[0], pol_ld);
+    ld_pack_pol<S, V, POL>(src + 2 * plane + rm + xa, 2, f[2], pol_ld);
+    ld_pack_pol<S, V, POL>(src + 4 * plane + rp + xa, 4, f[4], pol_ld);
+    ld_pack_pol<S, V, POL>(src + 1 * plane + r0 + xa, 1, a1, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 5 * plane + rm + xa, 5, a5, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 8 * plane + rp + xa, 8, a8, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 3 * plane + r0 + xa, 3, b3, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 6 * plane + rm + xa, 6, b6, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 7 * plane + rp + xa, 7, b7, pol_ld);
     uint32_t L[V];
     ld_links<V>(links + r0 + xa, L);
 
@@ -73,15 +73,15 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
     R n7 = __shfl_down_sync(0xffffffffu, b7[0], 1);
     if (lane == 0) {
         const int xm = max(x0 - 1, 0);
-        p1 = Store<S>::ld(src + 1 * plane + r0 + xm);
-        p5 = Store<S>::ld(src + 5 * plane + rm + xm);
-        p8 = Store<S>::ld(src + 8 * plane + rp + xm);
+        p1 = ldq<S>(src + 1 * plane + r0 + xm, 1);
+        p5 = ldq<S>(src + 5 * plane + rm + xm, 5);
+        p8 = ldq<S>(src + 8 * plane + rp + xm, 8);
     }
     if (lane == 31) {
         const int xq = min(x0 + V, (int)pitch - 1);
-        n3 = Store<S>::ld(src + 3 * plane + r0 + xq);
-        n6 = Store<S>::ld(src + 6 * plane + rm + xq);
-        n7 = Store<S>::ld(src + 7 * plane + rp + xq);
+        n3 = ldq<S>(src + 3 * plane + r0 + xq, 3);
+        n6 = ldq<S>(src + 6 * plane + rm + xq, 6);
+        n7 = ldq<S>(src + 7 * plane + rp + xq, 7);
     }
 #pragma unroll
     for (int k = 0; k < V; ++k) {
@@ -114,7 +114,7 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
             for (int k = 0; k < V; ++k) hit |= L[k] != LINK_SOLID ? (L[k] >> (q - 1)) & 1u : 0u;
             if (hit) {
                 R own[V];
-                ld_pack<S, V>(src + opp(q) * plane + r0 + x0, own);
+                ld_pack<S, V>(src + opp(q) * plane + r0 + x0, opp(q), own);
 #pragma unroll
                 for (int k = 0; k < V; ++k) {
                     if (L[k] != LINK_SOLID && ((L[k] >> (q - 1)) & 1u)) {
@@ -143,12 +143,12 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
     for (int q = 0; q < 9; ++q) {
         if (solid_any) {
             R own[V];
-            ld_pack<S, V>(src + q * plane + r0 + x0, own);
+            ld_pack<S, V>(src + q * plane + r0 + x0, q, own);
 #pragma unroll
             for (int k = 0; k < V; ++k)
                 if (L[k] == LINK_SOLID) f[q][k] = own[k];
         }
-        st_pack_pol<S, V, POL>(dst + q * plane + r0 + x0, f[q], pol_st);
+        st_pack_pol<S, V, POL>(dst + q * plane + r0 + x0, q, f[q], pol_st);
     }
 }
 
