@@ -245,6 +245,8 @@ LBM_API lbm_status lbm_create(const lbm_desc *desc, lbm_ctx **out) {
         if ((st = dalloc(ctx, (void **)&ctx->links_d, (size_t)ctx->plane * sizeof(uint16_t), "links")) != LBM_OK)
             return bail(set_thread_error(st, ctx->err));
         cudaError_t e = cudaMemsetAsync(ctx->flags_d, 0, (size_t)ctx->cells, ctx->stream);
+        // link words of the row padding stay 0 (the vectorised step reads them)
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->links_d, 0, (size_t)ctx->plane * sizeof(uint16_t), ctx->stream);
         if (e == cudaSuccess) e = d2q9_build_links(ctx);
         if (e == cudaSuccess) e = d2q9_init_equilibrium(ctx, nullptr, nullptr, nullptr);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);

@@ -5,8 +5,9 @@
 //
 // Storage: structure of arrays, plane q holds population q of all cells, rows padded to `pitch`
 // elements (a multiple of 32) so each row starts 128-byte aligned in FP32.  Populations are
-// stored shifted, g_q = f_q - w_q, in FP32 / FP16 / BF16 (arithmetic in FP32) or FP64 (the GPU
-// oracle).  Two buffers (A/B): step n reads f[cur] and writes f[cur ^ 1].
+// stored in the w-normalised shifted space h_q = s (f_q - w_q) / w_q (d2q9_core.cuh) in FP32 / FP16 /
+// BF16 (arithmetic in FP32) or FP64 (the GPU oracle).  Two buffers (A/B): step n reads f[cur] and
+// writes f[cur ^ 1].
 //
 // Population order: 0:(0,0) 1:(1,0) 2:(0,1) 3:(-1,0) 4:(0,-1) 5:(1,1) 6:(-1,1) 7:(-1,-1) 8:(1,-1).
 #include <cuda_bf16.h>
@@ -131,10 +132,10 @@ __global__ void moments_kernel(const S *__restrict__ src, const uint16_t *__rest
     uint16_t L = links[c];
     R rho = 1, ux = 0, uy = 0;
     if (L != LINK_SOLID) {
-        R g[9];
-        d2q9::gather<S>(src, L, x, y, nx, ny, pitch, plane, periodic, d2q9::wall_u<R>(prm), g);
+        R h[9];
+        d2q9::gather<S, R>(src, L, x, y, nx, ny, pitch, plane, periodic, d2q9::wall_u<R>(prm), h);
         R drho, mx, my;
-        d2q9::moments(g, drho, mx, my);
+        d2q9::moments<S, R>(h, drho, mx, my);
         rho = (R)1 + drho;
         const auto F = d2q9::force<R>(prm);
         ux = (mx + (R)0.5 * F.x) / rho;
@@ -156,12 +157,12 @@ __global__ void equilibrium_kernel(S *__restrict__ a, S *__restrict__ b, int nx,
     int64_t o = (int64_t)y * nx + x;
     int64_t c = (int64_t)y * pitch + x;
     R r = rho ? (R)rho[o] : (R)1, u = ux ? (R)ux[o] : (R)0, v = uy ? (R)uy[o] : (R)0;
-    R g[9];
-    d2q9::equilibrium_shifted(r - (R)1, r, u, v, g);
+    R h[9];
+    d2q9::equilibrium_h<S, R>(r - (R)1, r, u, v, h);
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
-        d2q9::stq<S>(a + q * plane + c, q, g[q]);
-        d2q9::stq<S>(b + q * plane + c, q, g[q]);
+        d2q9::sth<S>(a + q * plane + c, h[q]);
+        d2q9::sth<S>(b + q * plane + c, h[q]);
     }
 }
 

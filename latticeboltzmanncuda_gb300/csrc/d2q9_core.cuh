@@ -1,4 +1,11 @@
 // D2Q9 device building blocks shared by the single-domain and the batched kernels.
+//
+// Storage space.  Population q is stored as h_q = s (f_q - w_q) / w_q, s = 1024 for FP16 storage
+// and 1 otherwise.  The deviations f_q - w_q of all nine populations scale with w_q, so dividing by
+// w_q puts them in one range; the factor 1024 keeps FP16 values out of its subnormal range down to
+// deviations of ~1e-7 w_q.  The collision works directly on h: the weights fold into the moment
+// sums and drop out of the equilibrium, the forcing term and the moving-wall term, so a stored
+// value needs no multiply on the way in or out.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -30,7 +37,7 @@ struct Vec2 {
     R x, y;
 };
 
-// storage traits: S is the stored type, R the arithmetic type
+// storage traits: S is the stored type, R the arithmetic type; `to` / `from` convert raw values
 template <class S>
 struct Store;
 template <>
@@ -38,60 +45,51 @@ struct Store<float> {
     using R = float;
     static __device__ __forceinline__ R to(float v) { return v; }
     static __device__ __forceinline__ float from(R v) { return v; }
-    static __device__ __forceinline__ R ld(const float *p) { return __ldg(p); }
-    static __device__ __forceinline__ void st(float *p, R v) { *p = v; }
 };
 template <>
 struct Store<double> {
     using R = double;
     static __device__ __forceinline__ R to(double v) { return v; }
     static __device__ __forceinline__ double from(R v) { return v; }
-    static __device__ __forceinline__ R ld(const double *p) { return __ldg(p); }
-    static __device__ __forceinline__ void st(double *p, R v) { *p = v; }
 };
 template <>
 struct Store<__half> {
     using R = float;
     static __device__ __forceinline__ R to(__half v) { return __half2float(v); }
     static __device__ __forceinline__ __half from(R v) { return __float2half_rn(v); }
-    static __device__ __forceinline__ R ld(const __half *p) { return __half2float(__ldg(p)); }
-    static __device__ __forceinline__ void st(__half *p, R v) { *p = __float2half_rn(v); }
 };
 template <>
 struct Store<__nv_bfloat16> {
     using R = float;
     static __device__ __forceinline__ R to(__nv_bfloat16 v) { return __bfloat162float(v); }
     static __device__ __forceinline__ __nv_bfloat16 from(R v) { return __float2bfloat16_rn(v); }
-    static __device__ __forceinline__ R ld(const __nv_bfloat16 *p) { return __bfloat162float(__ldg(p)); }
-    static __device__ __forceinline__ void st(__nv_bfloat16 *p, R v) { *p = __float2bfloat16_rn(v); }
 };
 
-// FP16 storage holds h_q = 1024 (f_q - w_q) / w_q: the deviations of all nine populations scale
-// with w_q, so dividing by w_q puts them in one range, and the factor 1024 keeps deviations down to
-// ~1e-7 of w_q out of FP16's subnormal range (|h| < 6.1e-5).  The other storage types hold
-// g_q = f_q - w_q unscaled (the factors below are compile-time 1).
+// s of the storage space
 template <class S, class R>
-__device__ __forceinline__ R unscale(R v, int q) {
-    if constexpr (std::is_same<S, __half>::value)
-        return v * (w<R>(q) * (R)(1.0 / 1024.0));
-    else
-        return v;
+__host__ __device__ constexpr R hscale() {
+    return std::is_same<S, __half>::value ? (R)1024 : (R)1;
 }
-template <class S, class R>
-__device__ __forceinline__ R scale(R v, int q) {
-    if constexpr (std::is_same<S, __half>::value)
-        return v * ((R)1024.0 / w<R>(q));
-    else
-        return v;
+
+// raw stored value h (read-only path) and back
+template <class S>
+__device__ __forceinline__ typename Store<S>::R ldh(const S *p) {
+    return Store<S>::to(__ldg(p));
 }
-// population q of the stored buffer (shifted, unscaled) and back
+template <class S>
+__device__ __forceinline__ void sth(S *p, typename Store<S>::R v) {
+    *p = Store<S>::from(v);
+}
+// population q as f_q - w_q (host-layout conversion, moments, sums, initialisation)
 template <class S>
 __device__ __forceinline__ typename Store<S>::R ldq(const S *p, int q) {
-    return unscale<S>(Store<S>::ld(p), q);
+    using R = typename Store<S>::R;
+    return ldh<S>(p) * (w<R>(q) / hscale<S, R>());
 }
 template <class S>
-__device__ __forceinline__ void stq(S *p, int q, typename Store<S>::R v) {
-    Store<S>::st(p, scale<S>(v, q));
+__device__ __forceinline__ void stq(S *p, int q, typename Store<S>::R g) {
+    using R = typename Store<S>::R;
+    sth<S>(p, g * (hscale<S, R>() / w<R>(q)));
 }
 
 // V consecutive stored values moved as one 4-, 8- or 16-byte access (p aligned to V*sizeof(S))
@@ -111,21 +109,21 @@ struct RawPack<16> {
 };
 
 template <class S, int V>
-__device__ __forceinline__ void ld_pack(const S *__restrict__ p, int q, typename Store<S>::R (&out)[V]) {
+__device__ __forceinline__ void ld_pack(const S *__restrict__ p, typename Store<S>::R (&out)[V]) {
     using T = typename RawPack<sizeof(S) * V>::T;
     const T raw = __ldg(reinterpret_cast<const T *>(p));
     S e[V];
     memcpy(e, &raw, sizeof(raw));
 #pragma unroll
-    for (int k = 0; k < V; ++k) out[k] = unscale<S>(Store<S>::to(e[k]), q);
+    for (int k = 0; k < V; ++k) out[k] = Store<S>::to(e[k]);
 }
 
 template <class S, int V>
-__device__ __forceinline__ void st_pack(S *__restrict__ p, int q, const typename Store<S>::R (&in)[V]) {
+__device__ __forceinline__ void st_pack(S *__restrict__ p, const typename Store<S>::R (&in)[V]) {
     using T = typename RawPack<sizeof(S) * V>::T;
     S e[V];
 #pragma unroll
-    for (int k = 0; k < V; ++k) e[k] = Store<S>::from(scale<S>(in[k], q));
+    for (int k = 0; k < V; ++k) e[k] = Store<S>::from(in[k]);
     T raw;
     memcpy(&raw, e, sizeof(raw));
     *reinterpret_cast<T *>(p) = raw;
@@ -182,30 +180,28 @@ __device__ __forceinline__ void st_hint(unsigned int *p, unsigned int v, uint64_
 }
 
 template <class S, int V, int POL>
-__device__ __forceinline__ void ld_pack_pol(const S *__restrict__ p, int q, typename Store<S>::R (&out)[V],
-                                            uint64_t pol) {
+__device__ __forceinline__ void ld_pack_pol(const S *__restrict__ p, typename Store<S>::R (&out)[V], uint64_t pol) {
     if constexpr (POL == 0) {
-        ld_pack<S, V>(p, q, out);
+        ld_pack<S, V>(p, out);
     } else {
         using T = typename RawPack<sizeof(S) * V>::T;
         const T raw = ld_hint<T>(reinterpret_cast<const T *>(p), pol);
         S e[V];
         memcpy(e, &raw, sizeof(raw));
 #pragma unroll
-        for (int k = 0; k < V; ++k) out[k] = unscale<S>(Store<S>::to(e[k]), q);
+        for (int k = 0; k < V; ++k) out[k] = Store<S>::to(e[k]);
     }
 }
 
 template <class S, int V, int POL>
-__device__ __forceinline__ void st_pack_pol(S *__restrict__ p, int q, const typename Store<S>::R (&in)[V],
-                                            uint64_t pol) {
+__device__ __forceinline__ void st_pack_pol(S *__restrict__ p, const typename Store<S>::R (&in)[V], uint64_t pol) {
     if constexpr (POL != 1) {
-        st_pack<S, V>(p, q, in);
+        st_pack<S, V>(p, in);
     } else {
         using T = typename RawPack<sizeof(S) * V>::T;
         S e[V];
 #pragma unroll
-        for (int k = 0; k < V; ++k) e[k] = Store<S>::from(scale<S>(in[k], q));
+        for (int k = 0; k < V; ++k) e[k] = Store<S>::from(in[k]);
         T raw;
         memcpy(&raw, e, sizeof(raw));
         st_hint(reinterpret_cast<T *>(p), raw, pol);
@@ -245,65 +241,91 @@ __device__ __forceinline__ Vec2<float> wall_u<float>(const lbm::D2Q9Params &p) {
 template <>
 __device__ __forceinline__ Vec2<double> wall_u<double>(const lbm::D2Q9Params &p) { return {p.uwx_d, p.uwy_d}; }
 
-// Streamed populations of fluid cell (x, y): population q is pulled from (x - cx_q, y - cy_q)
-// (periodic wrap, or clamped when the link bit says the value is not used), and replaced by the
-// half-way bounce-back of the cell's own opposite population when link bit q-1 is set, plus the
-// moving-wall term 6 w_q (c_q . u_w) when bit q+7 is set.
+// moving-wall term of population q in storage space: s * 6 (c_q . u_w) (the w_q of
+// 6 w_q (c_q . u_w) cancels against the 1/w_q of the storage space)
+template <class S, class R>
+__device__ __forceinline__ R wall_term(int q, Vec2<R> uw) {
+    return hscale<S, R>() * (R)6 * ((R)cx(q) * uw.x + (R)cy(q) * uw.y);
+}
+
+// Streamed populations of fluid cell (x, y) in storage space: population q is pulled from
+// (x - cx_q, y - cy_q) (periodic wrap, or clamped when the link bit says the value is not used),
+// and replaced by the half-way bounce-back of the cell's own opposite population when link bit
+// q-1 is set, plus the moving-wall term when bit q+7 is set.
 template <class S, class R>
 __device__ __forceinline__ void gather(const S *__restrict__ src, uint32_t L, int x, int y, int nx, int ny,
-                                       int64_t pitch, int64_t plane, int periodic, Vec2<R> uw, R g[9]) {
+                                       int64_t pitch, int64_t plane, int periodic, Vec2<R> uw, R h[9]) {
     int xm = x - 1, xp = x + 1, ym = y - 1, yp = y + 1;
     if (xm < 0) xm = (periodic & 1) ? nx - 1 : 0;
     if (xp >= nx) xp = (periodic & 1) ? 0 : nx - 1;
     if (ym < 0) ym = (periodic & 2) ? ny - 1 : 0;
     if (yp >= ny) yp = (periodic & 2) ? 0 : ny - 1;
     const int64_t r0 = (int64_t)y * pitch, rm = (int64_t)ym * pitch, rp = (int64_t)yp * pitch;
-    g[0] = ldq<S>(src + r0 + x, 0);
-    g[1] = ldq<S>(src + 1 * plane + r0 + xm, 1);
-    g[2] = ldq<S>(src + 2 * plane + rm + x, 2);
-    g[3] = ldq<S>(src + 3 * plane + r0 + xp, 3);
-    g[4] = ldq<S>(src + 4 * plane + rp + x, 4);
-    g[5] = ldq<S>(src + 5 * plane + rm + xm, 5);
-    g[6] = ldq<S>(src + 6 * plane + rm + xp, 6);
-    g[7] = ldq<S>(src + 7 * plane + rp + xp, 7);
-    g[8] = ldq<S>(src + 8 * plane + rp + xm, 8);
+    h[0] = ldh<S>(src + r0 + x);
+    h[1] = ldh<S>(src + 1 * plane + r0 + xm);
+    h[2] = ldh<S>(src + 2 * plane + rm + x);
+    h[3] = ldh<S>(src + 3 * plane + r0 + xp);
+    h[4] = ldh<S>(src + 4 * plane + rp + x);
+    h[5] = ldh<S>(src + 5 * plane + rm + xm);
+    h[6] = ldh<S>(src + 6 * plane + rm + xp);
+    h[7] = ldh<S>(src + 7 * plane + rp + xp);
+    h[8] = ldh<S>(src + 8 * plane + rp + xm);
     if (L) {
 #pragma unroll
         for (int q = 1; q < 9; ++q) {
             if (L & (1u << (q - 1))) {
-                R v = ldq<S>(src + opp(q) * plane + r0 + x, opp(q));
-                if (L & (1u << (q + 7))) v += (R)6 * w<R>(q) * ((R)cx(q) * uw.x + (R)cy(q) * uw.y);
-                g[q] = v;
+                R v = ldh<S>(src + opp(q) * plane + r0 + x);
+                if (L & (1u << (q + 7))) v += wall_term<S, R>(q, uw);
+                h[q] = v;
             }
         }
     }
 }
 
-template <class R>
-__device__ __forceinline__ void moments(const R g[9], R &drho, R &mx, R &my) {
-    drho = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
-    mx = (g[1] - g[3]) + (g[5] - g[6]) + (g[8] - g[7]);
-    my = (g[2] - g[4]) + (g[5] + g[6]) - (g[7] + g[8]);
+// density deviation and momentum of populations in storage space
+template <class S, class R>
+__device__ __forceinline__ void moments(const R h[9], R &drho, R &mx, R &my) {
+    constexpr R s = hscale<S, R>();
+    const R w0 = w<R>(0) / s, ws = w<R>(1) / s, wd = w<R>(5) / s;
+    const R sf = (h[1] + h[3]) + (h[2] + h[4]);
+    const R sd = (h[5] + h[7]) + (h[6] + h[8]);
+    drho = w0 * h[0] + ws * sf + wd * sd;
+    const R d57 = h[5] - h[7], d86 = h[8] - h[6];
+    mx = ws * (h[1] - h[3]) + wd * (d57 + d86);
+    my = ws * (h[2] - h[4]) + wd * (d57 - d86);
 }
 
-// shifted equilibrium geq_q = feq_q - w_q = w_q (drho + rho (3 cu + 4.5 cu^2 - 1.5 u^2))
+// 1/rho: fast FP32 division (__fdividef, within 2 ulp; rho is close to 1), exact division in FP64
 template <class R>
-__device__ __forceinline__ void equilibrium_shifted(R drho, R rho, R ux, R uy, R g[9]) {
+__device__ __forceinline__ R recip(R rho) {
+    if constexpr (std::is_same<R, float>::value)
+        return __fdividef(1.0f, rho);
+    else
+        return (R)1 / rho;
+}
+
+// shifted equilibrium (f^eq_q - w_q) of (rho, u), in storage space
+template <class S, class R>
+__device__ __forceinline__ void equilibrium_h(R drho, R rho, R ux, R uy, R h[9]) {
+    constexpr R s = hscale<S, R>();
     const R usq = (R)1.5 * (ux * ux + uy * uy);
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         const R cu = (R)cx(q) * ux + (R)cy(q) * uy;
-        g[q] = w<R>(q) * (drho + rho * ((R)3 * cu + (R)4.5 * cu * cu - usq));
+        h[q] = s * (drho + rho * ((R)3 * cu + (R)4.5 * cu * cu - usq));
     }
 }
 
-// BGK collision with Guo forcing on shifted populations, in place
-template <class R, bool FORCE>
-__device__ __forceinline__ void collide(R g[9], R om, Vec2<R> F) {
+// BGK collision with Guo forcing, in place, in storage space.  Opposite populations q, q' share
+// c_q . u with opposite signs, so the equilibrium and the forcing term split into a symmetric part
+// A and an antisymmetric part B per pair: h_q <- (1 - om) h_q + A + B, h_q' <- (1 - om) h_q' + A - B.
+template <class S, class R, bool FORCE>
+__device__ __forceinline__ void collide(R h[9], R om, Vec2<R> F) {
+    constexpr R s = hscale<S, R>();
     R drho, mx, my;
-    moments(g, drho, mx, my);
+    moments<S, R>(h, drho, mx, my);
     const R rho = (R)1 + drho;
-    const R inv = (R)1 / rho;
+    const R inv = recip(rho);
     R ux, uy;
     if (FORCE) {
         ux = (mx + (R)0.5 * F.x) * inv;
@@ -313,19 +335,37 @@ __device__ __forceinline__ void collide(R g[9], R om, Vec2<R> F) {
         uy = my * inv;
     }
     const R usq = (R)1.5 * (ux * ux + uy * uy);
-    const R pre = (R)1 - (R)0.5 * om;
-    const R uF = ux * F.x + uy * F.y;
-#pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        const R cu = (R)cx(q) * ux + (R)cy(q) * uy;
-        const R geq = w<R>(q) * (drho + rho * ((R)3 * cu + (R)4.5 * cu * cu - usq));
-        R v = g[q] + om * (geq - g[q]);
-        if (FORCE) {
-            const R cF = (R)cx(q) * F.x + (R)cy(q) * F.y;
-            v += pre * w<R>(q) * ((R)3 * (cF - uF) + (R)9 * cu * cF);
-        }
-        g[q] = v;
+    const R om1 = (R)1 - om;
+    const R s_drho = s * drho, s_rho = s * rho;
+    const R om_s_drho = om * s_drho;
+    const R om_s_rho = om * s_rho;
+    R pre = 0, uF = 0;
+    if (FORCE) {
+        pre = s * ((R)1 - (R)0.5 * om);
+        uF = ux * F.x + uy * F.y;
     }
+    // rest population: h0eq = s (drho - rho usq), S0 = s pre (-3 u.F)
+    {
+        R a = om_s_drho - om_s_rho * usq;
+        if (FORCE) a -= (R)3 * pre * uF;
+        h[0] = om1 * h[0] + a;
+    }
+    auto pair = [&](int q, int qb, R cu, R cF) {
+        // A = om s (drho + rho (4.5 cu^2 - 1.5 u^2)) + s pre (9 cu cF - 3 u.F),  B = om s rho 3 cu + s pre 3 cF
+        R a = om_s_drho + om_s_rho * ((R)4.5 * cu * cu - usq);
+        R b = (R)3 * om_s_rho * cu;
+        if (FORCE) {
+            a += pre * ((R)9 * cu * cF - (R)3 * uF);
+            b += (R)3 * pre * cF;
+        }
+        const R hq = h[q], hqb = h[qb];
+        h[q] = om1 * hq + (a + b);
+        h[qb] = om1 * hqb + (a - b);
+    };
+    pair(1, 3, ux, F.x);
+    pair(2, 4, uy, F.y);
+    pair(5, 7, ux + uy, F.x + F.y);
+    pair(8, 6, ux - uy, F.x - F.y);
 }
 
 }  // namespace d2q9

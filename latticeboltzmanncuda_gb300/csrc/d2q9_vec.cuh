@@ -1,15 +1,16 @@
 // Vectorised D2Q9 update: one thread updates V consecutive cells of a row with V-wide loads and
-// stores of every population plane.  The x-1 / x+1 neighbours that fall outside the thread's
-// vector come from the adjacent lane by warp shuffle (the lane at a warp edge loads them itself),
-// so each population costs one wide load and one wide store per V cells.  Threads whose vector
-// touches the first or last column of the domain (periodic wrap, domain edge) or the row padding
-// re-run their cells through the scalar per-cell path.  Cells with bounce-back links take their
-// own opposite population (extra wide loads, only in vectors that have such a cell); solid cells
-// copy their own populations, so both A/B buffers keep identical values there.
+// stores of every population plane (values in storage space, see d2q9_core.cuh).  The x-1 / x+1
+// neighbours that fall outside the thread's vector come from the adjacent lane by warp shuffle;
+// lane 0 loads its left neighbour itself (wrapped at x = 0 in a periodic row) and lane 31 its right
+// one.  In a periodic row, the vector holding the last column patches that cell's three values from
+// x = 0.  Cells with bounce-back links take their own opposite population (one extra wide load per
+// population that bounces somewhere in the vector); solid cells copy their own populations, so both
+// A/B buffers keep identical values there.  Elements beyond the last column compute garbage that is
+// stored only into the row padding, which no cell ever reads.
 //
-// All 32 lanes of a warp must call step_vec for the same row (the shuffles use the full mask):
-// blockDim.x is a multiple of 32 and threads beyond the row run the loads on clamped addresses
-// and store nothing.
+// All 32 lanes of a warp must call step_vec for the same row with consecutive vectors, lane 0
+// holding a vector that starts on a multiple of 32 * V (the shuffles use the full mask): blockDim.x
+// is a multiple of 32, and threads beyond the row load clamped addresses and store nothing.
 #pragma once
 
 #include "d2q9_core.cuh"
@@ -25,14 +26,14 @@ __device__ __forceinline__ void scalar_cell(const S *__restrict__ src, S *__rest
     const I c = (I)y * pitch + x;
     const uint32_t L = __ldg(links + c);
     if (L == LINK_SOLID) return;
-    R g[9];
-    gather<S, R>(src, L, x, y, nx, ny, (int64_t)pitch, (int64_t)plane, periodic, wall_u<R>(prm), g);
+    R h[9];
+    gather<S, R>(src, L, x, y, nx, ny, (int64_t)pitch, (int64_t)plane, periodic, wall_u<R>(prm), h);
     if (force)
-        collide<R, true>(g, omega<R>(prm), d2q9::force<R>(prm));
+        collide<S, R, true>(h, omega<R>(prm), d2q9::force<R>(prm));
     else
-        collide<R, false>(g, omega<R>(prm), d2q9::force<R>(prm));
+        collide<S, R, false>(h, omega<R>(prm), d2q9::force<R>(prm));
 #pragma unroll
-    for (int q = 0; q < 9; ++q) stq<S>(dst + q * plane + c, q, g[q]);
+    for (int q = 0; q < 9; ++q) sth<S>(dst + q * plane + c, h[q]);
 }
 
 template <class S, int V, bool FORCE, class I, int POL = 0>
@@ -51,15 +52,15 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
 
     R f[9][V];
     R a1[V], a5[V], a8[V], b3[V], b6[V], b7[V];
-    ld_pack_pol<S, V, POL>(src + 0 * plane + r0 + xa, 0, f[0], pol_ld);
-    ld_pack_pol<S, V, POL>(src + 2 * plane + rm + xa, 2, f[2], pol_ld);
-    ld_pack_pol<S, V, POL>(src + 4 * plane + rp + xa, 4, f[4], pol_ld);
-    ld_pack_pol<S, V, POL>(src + 1 * plane + r0 + xa, 1, a1, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 5 * plane + rm + xa, 5, a5, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 8 * plane + rp + xa, 8, a8, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 3 * plane + r0 + xa, 3, b3, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 6 * plane + rm + xa, 6, b6, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 7 * plane + rp + xa, 7, b7, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 0 * plane + r0 + xa, f[0], pol_ld);
+    ld_pack_pol<S, V, POL>(src + 2 * plane + rm + xa, f[2], pol_ld);
+    ld_pack_pol<S, V, POL>(src + 4 * plane + rp + xa, f[4], pol_ld);
+    ld_pack_pol<S, V, POL>(src + 1 * plane + r0 + xa, a1, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 5 * plane + rm + xa, a5, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 8 * plane + rp + xa, a8, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 3 * plane + r0 + xa, b3, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 6 * plane + rm + xa, b6, pol_ld);
+    ld_pack_pol<S, V, POL>(src + 7 * plane + rp + xa, b7, pol_ld);
     uint32_t L[V];
     ld_links<V>(links + r0 + xa, L);
 
@@ -72,16 +73,17 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
     R n6 = __shfl_down_sync(0xffffffffu, b6[0], 1);
     R n7 = __shfl_down_sync(0xffffffffu, b7[0], 1);
     if (lane == 0) {
-        const int xm = max(x0 - 1, 0);
-        p1 = ldq<S>(src + 1 * plane + r0 + xm, 1);
-        p5 = ldq<S>(src + 5 * plane + rm + xm, 5);
-        p8 = ldq<S>(src + 8 * plane + rp + xm, 8);
+        int xm = x0 - 1;
+        if (xm < 0) xm = (periodic & 1) ? nx - 1 : 0;  // unused (bounce-back) when not periodic
+        p1 = ldh<S>(src + 1 * plane + r0 + xm);
+        p5 = ldh<S>(src + 5 * plane + rm + xm);
+        p8 = ldh<S>(src + 8 * plane + rp + xm);
     }
     if (lane == 31) {
         const int xq = min(x0 + V, (int)pitch - 1);
-        n3 = ldq<S>(src + 3 * plane + r0 + xq, 3);
-        n6 = ldq<S>(src + 6 * plane + rm + xq, 6);
-        n7 = ldq<S>(src + 7 * plane + rp + xq, 7);
+        n3 = ldh<S>(src + 3 * plane + r0 + xq);
+        n6 = ldh<S>(src + 6 * plane + rm + xq);
+        n7 = ldh<S>(src + 7 * plane + rp + xq);
     }
 #pragma unroll
     for (int k = 0; k < V; ++k) {
@@ -92,13 +94,17 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
         f[6][k] = k == V - 1 ? n6 : b6[k + 1];
         f[7][k] = k == V - 1 ? n7 : b7[k + 1];
     }
-
-    const bool special = x0 == 0 || x0 + V - 1 >= nx - 1;
-    if (special) {
-        // first / last column or row padding: per-cell path with wrap and edge handling
+    // periodic row: the last column pulls q = 3, 6, 7 from x = 0
+    const int kl = nx - 1 - x0;
+    if ((periodic & 1) && kl >= 0 && kl < V) {
+        const R w3 = ldh<S>(src + 3 * plane + r0), w6 = ldh<S>(src + 6 * plane + rm), w7 = ldh<S>(src + 7 * plane + rp);
+#pragma unroll
         for (int k = 0; k < V; ++k)
-            if (x0 + k < nx) scalar_cell<S, I>(src, dst, links, x0 + k, y, nx, ny, pitch, plane, periodic, prm, FORCE);
-        return;
+            if (k == kl) {
+                f[3][k] = w3;
+                f[6][k] = w6;
+                f[7][k] = w7;
+            }
     }
 
     uint32_t any = 0;
@@ -114,12 +120,12 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
             for (int k = 0; k < V; ++k) hit |= L[k] != LINK_SOLID ? (L[k] >> (q - 1)) & 1u : 0u;
             if (hit) {
                 R own[V];
-                ld_pack<S, V>(src + opp(q) * plane + r0 + x0, opp(q), own);
+                ld_pack<S, V>(src + opp(q) * plane + r0 + xa, own);
 #pragma unroll
                 for (int k = 0; k < V; ++k) {
                     if (L[k] != LINK_SOLID && ((L[k] >> (q - 1)) & 1u)) {
                         R v = own[k];
-                        if ((L[k] >> (q + 7)) & 1u) v += (R)6 * w<R>(q) * ((R)cx(q) * uw.x + (R)cy(q) * uw.y);
+                        if ((L[k] >> (q + 7)) & 1u) v += wall_term<S, R>(q, uw);
                         f[q][k] = v;
                     }
                 }
@@ -131,24 +137,25 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
 
 #pragma unroll
     for (int k = 0; k < V; ++k) {
-        R g[9];
+        R h[9];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) g[q] = f[q][k];
-        collide<R, FORCE>(g, omega<R>(prm), force<R>(prm));
+        for (int q = 0; q < 9; ++q) h[q] = f[q][k];
+        collide<S, R, FORCE>(h, omega<R>(prm), force<R>(prm));
 #pragma unroll
-        for (int q = 0; q < 9; ++q) f[q][k] = g[q];
+        for (int q = 0; q < 9; ++q) f[q][k] = h[q];
     }
 
+    if (x0 >= nx) return;  // vector entirely in the row padding
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         if (solid_any) {
             R own[V];
-            ld_pack<S, V>(src + q * plane + r0 + x0, q, own);
+            ld_pack<S, V>(src + q * plane + r0 + x0, own);
 #pragma unroll
             for (int k = 0; k < V; ++k)
                 if (L[k] == LINK_SOLID) f[q][k] = own[k];
         }
-        st_pack_pol<S, V, POL>(dst + q * plane + r0 + x0, q, f[q], pol_st);
+        st_pack_pol<S, V, POL>(dst + q * plane + r0 + x0, f[q], pol_st);
     }
 }
 
