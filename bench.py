@@ -350,8 +350,11 @@ def _timed(stream, fn):
 
 
 def _vel_err(u, v, u64, v64):
+    """(max-norm, L2-norm) relative velocity error against the FP64 run"""
     ref = float(np.max(np.hypot(u64, v64)))
-    return float(np.max(np.hypot(u - u64, v - v64))) / max(ref, 1e-30)
+    d = np.hypot(u - u64, v - v64)
+    l2 = float(np.sqrt(np.sum(d * d) / max(float(np.sum(u64 * u64 + v64 * v64)), 1e-300)))
+    return float(np.max(d)) / max(ref, 1e-30), l2
 
 
 def run_batch(args):
@@ -405,7 +408,9 @@ def run_batch(args):
     errs = {}
     for dtype in ("f32", "f16s"):
         e = [_vel_err(vel[dtype][i][1], vel[dtype][i][2], vel["f64"][i][1], vel["f64"][i][2]) for i in subset]
-        errs[dtype] = {"max": max(e), "median": float(np.median(e))}
+        mx, l2 = [a for a, _ in e], [b for _, b in e]
+        errs[dtype] = {"max_norm_max": max(mx), "max_norm_median": float(np.median(mx)),
+                       "l2_max": max(l2), "l2_median": float(np.median(l2))}
     peak, peak_kind = peaks()
     line = {
         "metric": "aggregate MLUPS, batched vs plain", "workload": "batch", "unit": "MLUPS",

@@ -37,6 +37,18 @@ struct Vec2 {
     R x, y;
 };
 
+// Arithmetic of the collision with explicit IEEE rounding: these intrinsics are never contracted,
+// fused or re-associated by the compiler, so a cell's update is bit-identical in every launch shape
+// and in the batched kernel, whatever instruction selection each inlining context gets.
+__device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float mul_(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add_(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub_(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double fma_(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ double mul_(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add_(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_(double a, double b) { return __dsub_rn(a, b); }
+
 // storage traits: S is the stored type, R the arithmetic type; `to` / `from` convert raw values
 template <class S>
 struct Store;
@@ -245,7 +257,9 @@ __device__ __forceinline__ Vec2<double> wall_u<double>(const lbm::D2Q9Params &p)
 // 6 w_q (c_q . u_w) cancels against the 1/w_q of the storage space)
 template <class S, class R>
 __device__ __forceinline__ R wall_term(int q, Vec2<R> uw) {
-    return hscale<S, R>() * (R)6 * ((R)cx(q) * uw.x + (R)cy(q) * uw.y);
+    const R cu = cx(q) == 0 ? mul_((R)cy(q), uw.y) : (cy(q) == 0 ? mul_((R)cx(q), uw.x)
+                                                             : fma_((R)cx(q), uw.x, mul_((R)cy(q), uw.y)));
+    return mul_(hscale<S, R>() * (R)6, cu);
 }
 
 // Streamed populations of fluid cell (x, y) in storage space: population q is pulled from
@@ -275,7 +289,7 @@ __device__ __forceinline__ void gather(const S *__restrict__ src, uint32_t L, in
         for (int q = 1; q < 9; ++q) {
             if (L & (1u << (q - 1))) {
                 R v = ldh<S>(src + opp(q) * plane + r0 + x);
-                if (L & (1u << (q + 7))) v += wall_term<S, R>(q, uw);
+                if (L & (1u << (q + 7))) v = add_(v, wall_term<S, R>(q, uw));
                 h[q] = v;
             }
         }
@@ -287,12 +301,12 @@ template <class S, class R>
 __device__ __forceinline__ void moments(const R h[9], R &drho, R &mx, R &my) {
     constexpr R s = hscale<S, R>();
     const R w0 = w<R>(0) / s, ws = w<R>(1) / s, wd = w<R>(5) / s;
-    const R sf = (h[1] + h[3]) + (h[2] + h[4]);
-    const R sd = (h[5] + h[7]) + (h[6] + h[8]);
-    drho = w0 * h[0] + ws * sf + wd * sd;
-    const R d57 = h[5] - h[7], d86 = h[8] - h[6];
-    mx = ws * (h[1] - h[3]) + wd * (d57 + d86);
-    my = ws * (h[2] - h[4]) + wd * (d57 - d86);
+    const R sf = add_(add_(h[1], h[3]), add_(h[2], h[4]));
+    const R sd = add_(add_(h[5], h[7]), add_(h[6], h[8]));
+    drho = fma_(wd, sd, fma_(ws, sf, mul_(w0, h[0])));
+    const R d57 = sub_(h[5], h[7]), d86 = sub_(h[8], h[6]);
+    mx = fma_(wd, add_(d57, d86), mul_(ws, sub_(h[1], h[3])));
+    my = fma_(wd, sub_(d57, d86), mul_(ws, sub_(h[2], h[4])));
 }
 
 // 1/rho: fast FP32 division (__fdividef, within 2 ulp; rho is close to 1), exact division in FP64
@@ -301,71 +315,73 @@ __device__ __forceinline__ R recip(R rho) {
     if constexpr (std::is_same<R, float>::value)
         return __fdividef(1.0f, rho);
     else
-        return (R)1 / rho;
+        return __ddiv_rn(1.0, rho);
 }
 
 // shifted equilibrium (f^eq_q - w_q) of (rho, u), in storage space
 template <class S, class R>
 __device__ __forceinline__ void equilibrium_h(R drho, R rho, R ux, R uy, R h[9]) {
     constexpr R s = hscale<S, R>();
-    const R usq = (R)1.5 * (ux * ux + uy * uy);
+    const R usq = mul_((R)1.5, fma_(ux, ux, mul_(uy, uy)));
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
-        const R cu = (R)cx(q) * ux + (R)cy(q) * uy;
-        h[q] = s * (drho + rho * ((R)3 * cu + (R)4.5 * cu * cu - usq));
+        const R cu = fma_((R)cx(q), ux, mul_((R)cy(q), uy));
+        const R t = sub_(fma_(mul_((R)4.5, cu), cu, mul_((R)3, cu)), usq);
+        h[q] = mul_(s, fma_(rho, t, drho));
     }
 }
 
 // BGK collision with Guo forcing, in place, in storage space.  Opposite populations q, q' share
 // c_q . u with opposite signs, so the equilibrium and the forcing term split into a symmetric part
-// A and an antisymmetric part B per pair: h_q <- (1 - om) h_q + A + B, h_q' <- (1 - om) h_q' + A - B.
+// A and an antisymmetric part B per pair: h_q <- (1 - om) h_q + A + B, h_q' <- (1 - om) h_q' + A - B,
+//   A = om s (drho + rho (4.5 cu^2 - 1.5 u^2)) + s (1 - om/2) (9 cu cF - 3 u.F)
+//   B = 3 om s rho cu + 3 s (1 - om/2) cF
 template <class S, class R, bool FORCE>
 __device__ __forceinline__ void collide(R h[9], R om, Vec2<R> F) {
     constexpr R s = hscale<S, R>();
     R drho, mx, my;
     moments<S, R>(h, drho, mx, my);
-    const R rho = (R)1 + drho;
+    const R rho = add_((R)1, drho);
     const R inv = recip(rho);
     R ux, uy;
     if (FORCE) {
-        ux = (mx + (R)0.5 * F.x) * inv;
-        uy = (my + (R)0.5 * F.y) * inv;
+        ux = mul_(fma_((R)0.5, F.x, mx), inv);
+        uy = mul_(fma_((R)0.5, F.y, my), inv);
     } else {
-        ux = mx * inv;
-        uy = my * inv;
+        ux = mul_(mx, inv);
+        uy = mul_(my, inv);
     }
-    const R usq = (R)1.5 * (ux * ux + uy * uy);
-    const R om1 = (R)1 - om;
-    const R s_drho = s * drho, s_rho = s * rho;
-    const R om_s_drho = om * s_drho;
-    const R om_s_rho = om * s_rho;
-    R pre = 0, uF = 0;
+    const R usq = mul_((R)1.5, fma_(ux, ux, mul_(uy, uy)));
+    const R om1 = sub_((R)1, om);
+    const R om_s_drho = mul_(om, mul_(s, drho));
+    const R om_s_rho = mul_(om, mul_(s, rho));
+    const R om_s_rho3 = mul_((R)3, om_s_rho);
+    R pre = 0, pre3 = 0, uF3 = 0;
     if (FORCE) {
-        pre = s * ((R)1 - (R)0.5 * om);
-        uF = ux * F.x + uy * F.y;
+        pre = mul_(s, fma_((R)-0.5, om, (R)1));
+        pre3 = mul_((R)3, pre);
+        uF3 = mul_((R)3, fma_(ux, F.x, mul_(uy, F.y)));
     }
-    // rest population: h0eq = s (drho - rho usq), S0 = s pre (-3 u.F)
+    // rest population: h0eq = s (drho - rho usq), forcing s (1 - om/2) (-3 u.F)
     {
-        R a = om_s_drho - om_s_rho * usq;
-        if (FORCE) a -= (R)3 * pre * uF;
-        h[0] = om1 * h[0] + a;
+        R a = fma_(-om_s_rho, usq, om_s_drho);
+        if (FORCE) a = fma_(-pre, uF3, a);
+        h[0] = fma_(om1, h[0], a);
     }
     auto pair = [&](int q, int qb, R cu, R cF) {
-        // A = om s (drho + rho (4.5 cu^2 - 1.5 u^2)) + s pre (9 cu cF - 3 u.F),  B = om s rho 3 cu + s pre 3 cF
-        R a = om_s_drho + om_s_rho * ((R)4.5 * cu * cu - usq);
-        R b = (R)3 * om_s_rho * cu;
+        R a = fma_(om_s_rho, fma_(mul_((R)4.5, cu), cu, -usq), om_s_drho);
+        R b = mul_(om_s_rho3, cu);
         if (FORCE) {
-            a += pre * ((R)9 * cu * cF - (R)3 * uF);
-            b += (R)3 * pre * cF;
+            a = fma_(pre, fma_(mul_((R)9, cu), cF, -uF3), a);
+            b = fma_(pre3, cF, b);
         }
-        const R hq = h[q], hqb = h[qb];
-        h[q] = om1 * hq + (a + b);
-        h[qb] = om1 * hqb + (a - b);
+        h[q] = fma_(om1, h[q], add_(a, b));
+        h[qb] = fma_(om1, h[qb], sub_(a, b));
     };
     pair(1, 3, ux, F.x);
     pair(2, 4, uy, F.y);
-    pair(5, 7, ux + uy, F.x + F.y);
-    pair(8, 6, ux - uy, F.x - F.y);
+    pair(5, 7, add_(ux, uy), add_(F.x, F.y));
+    pair(8, 6, sub_(ux, uy), sub_(F.x, F.y));
 }
 
 }  // namespace d2q9

@@ -125,7 +125,7 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
                 for (int k = 0; k < V; ++k) {
                     if (L[k] != LINK_SOLID && ((L[k] >> (q - 1)) & 1u)) {
                         R v = own[k];
-                        if ((L[k] >> (q + 7)) & 1u) v += wall_term<S, R>(q, uw);
+                        if ((L[k] >> (q + 7)) & 1u) v = add_(v, wall_term<S, R>(q, uw));
                         f[q][k] = v;
                     }
                 }
