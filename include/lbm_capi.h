@@ -239,6 +239,58 @@ LBM_API lbm_status lbm_batch_load_populations(lbm_batch *b, int32_t slot, const 
 LBM_API lbm_status lbm_batch_retrieve_populations(lbm_batch *b, int32_t slot, void *host,
                                                   int32_t host_dtype);
 
+/* ---------------------------------------------------------------- serving */
+/* Continuous-batching solve server.  No counterpart in the reference.  lbm_server_run plays a
+ * list of solve requests with arrival times in real time: requests wait in arrival order and are
+ * admitted when their device bytes (lbm_batch_slot_bytes) fit into budget_bytes next to the live
+ * solves and fewer than max_slots run (0: no slot limit); every round advances all live solves by
+ * up to round_steps steps in one lbm_batch, so requests that arrive meanwhile join at the next
+ * round and their work overlaps with the running ones.  A finished solve's density and velocity
+ * go to the request's host buffers (if given) and its memory is released.  Per request: status
+ * (LBM_OK; LBM_ERR_BUDGET if it alone exceeds the budget; LBM_ERR_INVALID; LBM_ERR_TIMEOUT if
+ * time_limit seconds passed first), admission and completion times.  Each solve's result is
+ * bit-identical to the same solve run alone. */
+typedef struct lbm_server lbm_server;
+typedef struct lbm_server_config {
+    int32_t dtype;          /* storage type of every solve (lbm_dtype) */
+    int32_t device;
+    int64_t budget_bytes;   /* device bytes the live solves may hold together */
+    int32_t max_slots;      /* 0: no limit */
+    int32_t round_steps;    /* steps per round */
+    double time_limit;      /* seconds for the whole run, 0: none */
+    void *stream;           /* cudaStream_t, or NULL for a private stream */
+} lbm_server_config;
+typedef struct lbm_request {
+    int32_t nx, ny;
+    float tau;
+    int32_t periodic;
+    float body_force[2];
+    float wall_velocity[2];
+    const uint8_t *flags;   /* host [ny][nx] D2Q9 flags, or NULL (all fluid) */
+    int64_t steps;
+    double arrival;         /* seconds after the start of the run */
+    float *out_rho, *out_ux, *out_uy;  /* host [ny][nx] results, each may be NULL */
+} lbm_request;
+typedef struct lbm_request_result {
+    double admitted, finished;  /* seconds after the start of the run */
+    int32_t status;
+    int32_t slot;
+} lbm_request_result;
+typedef struct lbm_server_stats {
+    double makespan;        /* seconds from the start to the last completion */
+    double cell_updates;    /* sum over requests of cells * steps */
+    int64_t rounds;
+    int64_t peak_bytes;
+    int32_t peak_slots;
+    int32_t rejected;
+} lbm_server_stats;
+LBM_API void lbm_server_config_init(lbm_server_config *cfg);
+LBM_API lbm_status lbm_server_create(const lbm_server_config *cfg, lbm_server **out);
+LBM_API lbm_status lbm_server_destroy(lbm_server *s);
+LBM_API const char *lbm_server_last_error(const lbm_server *s);
+LBM_API lbm_status lbm_server_run(lbm_server *s, const lbm_request *reqs, int64_t n, lbm_request_result *results,
+                                  lbm_server_stats *stats);
+
 /* ---------------------------------------------------------------- allocation-free reduction */
 /* No counterpart in the reference.  Mass and momentum sums (FP64) of a D2Q9 population buffer
  * over the fluid cells, for callers that cannot allocate device memory while they run: an

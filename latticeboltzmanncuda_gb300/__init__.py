@@ -341,3 +341,52 @@ class Batch:
         self._chk(capi.lib().lbm_batch_retrieve_populations(self._b, int(slot), ptr(a),
                                                             F64 if dtype == np.float64 else F32))
         return a
+
+
+def serve(requests, dtype="f32", budget_bytes=150e9, max_slots=0, round_steps=200, time_limit=0.0,
+          outputs=False, device=0, stream=None):
+    """Play `requests` (objects with nx, ny, tau, flags, periodic, body_force, wall_velocity, steps
+    and arrival in seconds) through the continuous-batching server (lbm_server_run).  Returns
+    (results, stats, run_status): per request a dict with status, admitted, finished, latency and,
+    with outputs=True, (rho, ux, uy)."""
+    L = capi.lib()
+    cfg = capi.ServerConfig()
+    L.lbm_server_config_init(ctypes.byref(cfg))
+    cfg.dtype, cfg.device = _dtype(dtype), int(device)
+    cfg.budget_bytes, cfg.max_slots, cfg.round_steps = int(budget_bytes), int(max_slots), int(round_steps)
+    cfg.time_limit, cfg.stream = float(time_limit), stream
+    srv = ctypes.c_void_p()
+    check(L.lbm_server_create(ctypes.byref(cfg), ctypes.byref(srv)))
+    n = len(requests)
+    arr = (capi.Request * max(n, 1))()
+    keep, outs = [], []
+    for i, r in enumerate(requests):
+        q = arr[i]
+        q.nx, q.ny, q.tau, q.periodic = int(r.nx), int(r.ny), float(r.tau), int(r.periodic)
+        q.body_force[0], q.body_force[1] = float(r.body_force[0]), float(r.body_force[1])
+        q.wall_velocity[0], q.wall_velocity[1] = float(r.wall_velocity[0]), float(r.wall_velocity[1])
+        fl = None if r.flags is None else np.ascontiguousarray(r.flags, dtype=np.uint8)
+        keep.append(fl)
+        q.flags = None if fl is None else fl.ctypes.data
+        q.steps, q.arrival = int(r.steps), float(r.arrival)
+        if outputs:
+            o = [np.zeros((r.ny, r.nx), np.float32) for _ in range(3)]
+            outs.append(o)
+            q.out_rho, q.out_ux, q.out_uy = (a.ctypes.data for a in o)
+        else:
+            outs.append(None)
+    res = (capi.RequestResult * max(n, 1))()
+    st = capi.ServerStats()
+    try:
+        status = L.lbm_server_run(srv, arr, n, res, ctypes.byref(st))
+    finally:
+        L.lbm_server_destroy(srv)
+    results = []
+    for i in range(n):
+        d = {"status": res[i].status, "admitted": res[i].admitted, "finished": res[i].finished,
+             "latency": res[i].finished - float(requests[i].arrival)}
+        if outputs:
+            d["moments"] = tuple(outs[i])
+        results.append(d)
+    stats = {k: getattr(st, k) for k, _ in capi.ServerStats._fields_}
+    return results, stats, status

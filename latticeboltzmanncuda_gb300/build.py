@@ -23,7 +23,7 @@ OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "liblbm_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["common.cu", "capi.cu", "d2q9.cu", "d3q27.cu", "geometry.cpp", "noalloc.cu", "batch.cu"]
+SOURCES = ["common.cu", "capi.cu", "d2q9.cu", "d3q27.cu", "geometry.cpp", "noalloc.cu", "batch.cu", "server.cpp"]
 
 
 def nvcc() -> str:

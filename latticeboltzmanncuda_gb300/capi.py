@@ -60,6 +60,30 @@ class Info(ctypes.Structure):
                 ("rows_per_block", ctypes.c_int32), ("tuned", ctypes.c_int32), ("l2_policy", ctypes.c_int32)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("dtype", ctypes.c_int32), ("device", ctypes.c_int32), ("budget_bytes", ctypes.c_int64),
+                ("max_slots", ctypes.c_int32), ("round_steps", ctypes.c_int32), ("time_limit", ctypes.c_double),
+                ("stream", ctypes.c_void_p)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("tau", ctypes.c_float),
+                ("periodic", ctypes.c_int32), ("body_force", ctypes.c_float * 2),
+                ("wall_velocity", ctypes.c_float * 2), ("flags", ctypes.c_void_p), ("steps", ctypes.c_int64),
+                ("arrival", ctypes.c_double), ("out_rho", ctypes.c_void_p), ("out_ux", ctypes.c_void_p),
+                ("out_uy", ctypes.c_void_p)]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [("admitted", ctypes.c_double), ("finished", ctypes.c_double), ("status", ctypes.c_int32),
+                ("slot", ctypes.c_int32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("makespan", ctypes.c_double), ("cell_updates", ctypes.c_double), ("rounds", ctypes.c_int64),
+                ("peak_bytes", ctypes.c_int64), ("peak_slots", ctypes.c_int32), ("rejected", ctypes.c_int32)]
+
+
 # exported symbols and their signatures: (name, restype, argtypes)
 _P, _I32, _I64, _U64, _F = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64, ctypes.c_float
 _S = ctypes.c_int
@@ -107,6 +131,11 @@ SIGNATURES = [
     ("lbm_batch_moments", _S, [_P, _I32, _P, _P, _P]),
     ("lbm_batch_load_populations", _S, [_P, _I32, _P, _I32]),
     ("lbm_batch_retrieve_populations", _S, [_P, _I32, _P, _I32]),
+    ("lbm_server_config_init", None, [_P]),
+    ("lbm_server_create", _S, [_P, _P]),
+    ("lbm_server_destroy", _S, [_P]),
+    ("lbm_server_last_error", ctypes.c_char_p, [_P]),
+    ("lbm_server_run", _S, [_P, _P, _I64, _P, _P]),
     ("lbm_d2q9_conservation_noalloc", _S, [_P, _I32, _P, _I32, _I32, _I64, _P, _P]),
     ("lbm_gen_channel", _S, [_I32, _I32, _I32, _F, _F, _U64, _P, _P]),
     ("lbm_gen_cavity", _S, [_I32, _I32, _P]),

@@ -119,3 +119,33 @@ def test_gen_cavity_and_fraction():
 def test_gen_rejects_impossible_packing():
     with pytest.raises(lbm.LBMError):
         lbm.gen_channel(64, 16, 500, 8, 8, 1)
+
+
+def test_server_struct_layouts(tmp_path):
+    """ctypes mirrors of the serving structs match the C compiler's layout of the header."""
+    src = tmp_path / "srv.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "lbm_capi.h"\n'
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(lbm_server_config), '
+                   'sizeof(lbm_request), offsetof(lbm_request, flags), offsetof(lbm_request, arrival), '
+                   'sizeof(lbm_request_result), sizeof(lbm_server_stats), offsetof(lbm_server_stats, peak_slots));'
+                   ' return 0;}\n')
+    exe = tmp_path / "srv"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = [int(v) for v in subprocess.check_output([str(exe)]).split()]
+    assert got == [ctypes.sizeof(capi.ServerConfig), ctypes.sizeof(capi.Request), capi.Request.flags.offset,
+                   capi.Request.arrival.offset, ctypes.sizeof(capi.RequestResult), ctypes.sizeof(capi.ServerStats),
+                   capi.ServerStats.peak_slots.offset]
+
+
+def test_server_rejects_bad_configuration():
+    L = capi.lib()
+    cfg = capi.ServerConfig()
+    L.lbm_server_config_init(ctypes.byref(cfg))
+    assert cfg.round_steps > 0 and cfg.budget_bytes == 150 * 10 ** 9
+    srv = ctypes.c_void_p()
+    for field, value in (("budget_bytes", 0), ("round_steps", 0), ("max_slots", -1), ("time_limit", -1.0)):
+        c = capi.ServerConfig.from_buffer_copy(cfg)
+        setattr(c, field, value)
+        assert L.lbm_server_create(ctypes.byref(c), ctypes.byref(srv)) == capi.ERR_INVALID
+    assert L.lbm_batch_slot_bytes(capi.F32, 0, 8) == -1
+    assert L.lbm_batch_slot_bytes(capi.F16S, 64, 64) == 2 * 9 * 64 * 64 * 2 + 64 * 64 * 2 + 64 * 64
