@@ -5,7 +5,7 @@ seed, so every workload is a pure function of its seed."""
 from __future__ import annotations
 
 import math
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 
@@ -26,6 +26,8 @@ class Domain:
     drive: str = "lid"
     solid_fraction: float = 0.0
     steps: int = 0
+    arrival: float = 0.0  # seconds after the start of a request stream
+    rid: int = 0
 
     @property
     def cells(self):
@@ -89,17 +91,10 @@ def batch(count=512, seed=DEFAULT_SEED, steps=2000):
     return out
 
 
-@dataclass
-class Request:
-    rid: int
-    arrival: float  # seconds after the start of the stream
-    domain: Domain = field(repr=False)
-
-
 def requests(rate, duration, seed=DEFAULT_SEED, side_lo=128, side_hi=2048, steps_lo=1000, steps_hi=50000):
     """Poisson arrivals at `rate` per second for `duration` seconds.  Side length log-uniform in
     [side_lo, side_hi] (area = side^2, aspect as in batch()), solid 0-30 %, tau 0.52-1.2, steps
-    log-uniform in [steps_lo, steps_hi]."""
+    log-uniform in [steps_lo, steps_hi].  Returns Domains with `arrival` and `rid` set."""
     rng = np.random.default_rng(seed + 7)
     t, out, i = 0.0, [], 0
     while True:
@@ -109,6 +104,7 @@ def requests(rate, duration, seed=DEFAULT_SEED, side_lo=128, side_hi=2048, steps
         side = math.exp(rng.uniform(math.log(side_lo), math.log(side_hi)))
         d = _random_domain(rng, seed * 7919 + i, side * side, side * side * 1.0000001, 4.0, 0.52, 1.2, 0.30)
         d.steps = int(round(math.exp(rng.uniform(math.log(steps_lo), math.log(steps_hi)))))
-        out.append(Request(i, t, d))
+        d.arrival, d.rid = t, i
+        out.append(d)
         i += 1
     return out
