@@ -73,7 +73,8 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
     R n6 = __shfl_down_sync(0xffffffffu, b6[0], 1);
     R n7 = __shfl_down_sync(0xffffffffu, b7[0], 1);
     if (lane == 0) {
-        int xm = x0 - 1;
+        // from the clamped xa: a warp lying wholly beyond the row must not address past it
+        int xm = xa - 1;
         if (xm < 0) xm = (periodic & 1) ? nx - 1 : 0;  // unused (bounce-back) when not periodic
         p1 = ldh<S>(src + 1 * plane + r0 + xm);
         p5 = ldh<S>(src + 5 * plane + rm + xm);

@@ -39,7 +39,7 @@ def make_requests(n, seed=5):
             per, force, wall = 1, (2e-6, 0.0), (0.0, 0.0)
         fl, _ = lbm.gen_disks_fraction(fl, float(rng.uniform(0, 0.2)), 1.5, 4.0, 100 + i)
         out.append(Req(nx, ny, float(rng.uniform(0.55, 1.1)), fl, per, force, wall, int(rng.integers(50, 400)),
-                       float(0.004 * i)))
+                       float(0.0002 * i)))
     return out
 
 

@@ -1,0 +1,95 @@
+"""CPU replay of the vectorised D2Q9 step's address arithmetic (csrc/d2q9_vec.cuh, step_vec) for
+every thread of every launch shape the library can use, single-domain grids and batch tiles,
+over many domain sizes: every population offset must lie in [0, 9 * plane) and every link-word
+offset in [0, plane).  The kernel has no device-side bounds checks, so this replay is where its
+indexing is checked; keep it in step with step_vec."""
+import itertools
+
+import numpy as np
+import pytest
+
+
+def thread_offsets(nx, ny, pitch, V, x0, y, lane, periodic):
+    """(population offsets, link offsets) one thread of step_vec touches, as element indices."""
+    plane = pitch * ny
+    xa = np.minimum(x0, pitch - V)
+    ym = y - 1
+    yp = y + 1
+    ym = np.where(ym < 0, ny - 1 if periodic & 2 else 0, ym)
+    yp = np.where(yp >= ny, 0 if periodic & 2 else ny - 1, yp)
+    r0, rm, rp = y * pitch, ym * pitch, yp * pitch
+    pop, lnk = [], []
+    rows = {0: r0, 2: rm, 4: rp, 1: r0, 5: rm, 8: rp, 3: r0, 6: rm, 7: rp}
+    for q, r in rows.items():
+        for k in range(V):
+            pop.append(q * plane + r + xa + k)
+    for k in range(V):
+        lnk.append(r0 + xa + k)
+    # lane 0: left neighbour from the clamped xa, wrapped or clamped at x = 0
+    xm = xa - 1
+    xm = np.where(xm < 0, nx - 1 if periodic & 1 else 0, xm)
+    m0 = lane == 0
+    for q, r in ((1, r0), (5, rm), (8, rp)):
+        pop.append(np.where(m0, q * plane + r + xm, 0))
+    # lane 31: right neighbour, clamped to the row
+    xq = np.minimum(x0 + V, pitch - 1)
+    m31 = lane == 31
+    for q, r in ((3, r0), (6, rm), (7, rp)):
+        pop.append(np.where(m31, q * plane + r + xq, 0))
+    # periodic patch of the last column from x = 0
+    kl = nx - 1 - x0
+    mp = bool(periodic & 1) & (kl >= 0) & (kl < V)
+    for q, r in ((3, r0), (6, rm), (7, rp)):
+        pop.append(np.where(mp, q * plane + r, 0))
+    # own populations for bounce-back (any q), at xa
+    for q in range(9):
+        for k in range(V):
+            pop.append(q * plane + r0 + xa + k)
+    # solid copies and stores, only for vectors that start inside the row
+    act = x0 < nx
+    for q in range(9):
+        for k in range(V):
+            pop.append(np.where(act, q * plane + r0 + x0 + k, 0))
+    return np.stack(pop), np.stack(lnk), plane
+
+
+def check(nx, ny, V, tx, ty, periodic, batch):
+    pitch = (nx + 31) // 32 * 32
+    per_row = pitch // V
+    chunks = (per_row + tx - 1) // tx
+    xs, ys, lanes = [], [], []
+    for yb in range(0, ny if batch else (ny + ty - 1) // ty * ty, ty):
+        for xc in range(chunks):
+            for ti in range(ty):
+                y = yb + ti
+                if y >= ny:
+                    continue  # the kernel returns before any access
+                t = np.arange(tx)
+                xs.append((xc * tx + t) * V)
+                ys.append(np.full(tx, y))
+                lanes.append(t % 32)
+    x0, y, lane = np.concatenate(xs), np.concatenate(ys), np.concatenate(lanes)
+    pop, lnk, plane = thread_offsets(nx, ny, pitch, V, x0, y, lane, periodic)
+    assert pop.min() >= 0 and pop.max() < 9 * plane, (nx, ny, V, tx, ty, periodic, pop.max() - 9 * plane)
+    assert lnk.min() >= 0 and lnk.max() < plane, (nx, ny, V, tx, ty, periodic)
+
+
+SIZES = [(1, 1), (5, 3), (31, 7), (33, 2), (64, 64), (150, 41), (203, 77), (1000, 9), (4096, 3)]
+SHAPES = [(V, tx, ty) for V in (2, 4, 8) for tx in (32, 64, 128, 256) for ty in (1, 2, 4, 8) if tx * ty <= 256]
+
+
+@pytest.mark.parametrize("nx,ny", SIZES)
+def test_vector_step_addresses_stay_in_buffers(nx, ny):
+    for (V, tx, ty), periodic, batch in itertools.product(SHAPES, range(4), (False, True)):
+        check(nx, ny, V, tx, ty, periodic, batch)
+
+
+def test_replay_catches_an_unclamped_left_neighbour():
+    """The replay would have flagged lane 0's left neighbour taken from x0 instead of xa: a warp
+    wholly beyond a narrow row reads past the last plane."""
+    nx, ny, V, tx = 150, 41, 8, 128
+    pitch = (nx + 31) // 32 * 32
+    plane = pitch * ny
+    x0 = np.array([(3 * 32) * V])  # lane 0 of the fourth warp, beyond the 160-wide row
+    bad = 8 * plane + (ny - 1) * pitch + (x0 - 1)
+    assert bad.max() >= 9 * plane
