@@ -60,7 +60,7 @@ def parse():
                          "serve: Poisson request streams through the continuous-batching server")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=2000)
-    ap.add_argument("--serve-rates", default="1,3,6,10", help="requests per second, comma separated")
+    ap.add_argument("--serve-rates", default="2,6,10,15,25", help="requests per second, comma separated")
     ap.add_argument("--serve-duration", type=float, default=6.0, help="seconds of arrivals per rate")
     ap.add_argument("--round-steps", type=int, default=200)
     return ap.parse_args()
