@@ -55,9 +55,12 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--workload", default="channel", choices=["channel", "batch", "serve"],
+    ap.add_argument("--workload", default="channel", choices=["channel", "batch", "serve", "tgv"],
                     help="channel: the headline single-domain solve; batch: 512 uneven domains; "
-                         "serve: Poisson request streams through the continuous-batching server")
+                         "serve: Poisson request streams through the continuous-batching server; "
+                         "tgv: Taylor-Green precision runs per storage type")
+    ap.add_argument("--tgv-n", type=int, default=2048)
+    ap.add_argument("--tgv-steps", type=int, default=5000)
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=2000)
     ap.add_argument("--serve-rates", default="2,6,10,15,25", help="requests per second, comma separated")
@@ -502,12 +505,56 @@ def run_serve(args):
     return 0
 
 
+def run_tgv(args):
+    """Taylor-Green vortex, n x n periodic, u0 = 0.04, k = 2 pi / n, for each tau and storage type:
+    velocity L2 error against the analytic decay u0 exp(-2 nu k^2 t) and against the FP64 GPU run
+    of the same grid, with the MLUPS of each run."""
+    import torch
+    import latticeboltzmanncuda_gb300 as lbm
+    from latticeboltzmanncuda_gb300 import workloads
+
+    n, steps, u0 = args.tgv_n, args.tgv_steps, 0.04
+    rho, ux0, uy0 = workloads.taylor_green_fields(n, u0)
+    k = 2 * math.pi / n
+    rows = []
+    for tau in (0.51, 0.6, 1.0):
+        nu = (tau - 0.5) / 3
+        decay = math.exp(-2 * nu * k * k * (steps + 1))  # moments are those of the streamed populations
+        ua, va = ux0 * decay, uy0 * decay
+        vel, mlups = {}, {}
+        for dtype in ("f64", "f32", "bf16s", "f16s"):
+            stream = torch.cuda.Stream()
+            with lbm.Lattice(n, n, dtype=dtype, tau=tau, periodic=3, stream=stream.cuda_stream) as L:
+                L.init_equilibrium(rho, ux0, uy0)
+                L.autotune()
+                t = _timed(stream, lambda: L.step(steps))
+                _, ux, uy = L.moments()
+            vel[dtype] = (ux.astype(np.float64), uy.astype(np.float64))
+            mlups[dtype] = n * n * steps / t / 1e6
+
+        def l2(a, b):
+            return float(np.sqrt(np.sum((a[0] - b[0]) ** 2 + (a[1] - b[1]) ** 2) / np.sum(b[0] ** 2 + b[1] ** 2)))
+
+        for dtype in ("f64", "f32", "bf16s", "f16s"):
+            rows.append({"tau": tau, "dtype": dtype, "mlups": round(mlups[dtype], 1),
+                         "l2_vs_analytic": float(f"{l2(vel[dtype], (ua, va)):.3e}"),
+                         "l2_vs_fp64": float(f"{l2(vel[dtype], vel['f64']):.3e}") if dtype != "f64" else 0.0})
+    line = {"metric": "velocity L2 error vs analytic decay and vs FP64, per storage type", "workload": "tgv",
+            "unit": "relative L2", "data": "synthetic",
+            "config": {"workload": f"Taylor-Green vortex {n}x{n}, periodic, u0 {u0}, tau 0.51 / 0.6 / 1.0, {steps} steps"},
+            "runs": rows}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "tgv":
+        return run_tgv(args)
     if args.workload == "serve":
         return run_serve(args)
     return run_mine(args)
