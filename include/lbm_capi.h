@@ -232,6 +232,9 @@ LBM_API lbm_status lbm_batch_get_stream(lbm_batch *b, void **stream);
  * rows per block, tiles per step */
 LBM_API lbm_status lbm_batch_info(lbm_batch *b, int64_t out[8]);
 LBM_API lbm_status lbm_batch_slot_steps(lbm_batch *b, int32_t slot, int64_t *steps_done);
+/* step budget of a slot: lbm_batch_step advances it by min(nsteps, budget) and lowers the budget;
+ * a slot whose budget runs out mid-sequence stops there (-1: no budget, the default) */
+LBM_API lbm_status lbm_batch_set_slot_steps(lbm_batch *b, int32_t slot, int64_t steps);
 LBM_API lbm_status lbm_batch_moments(lbm_batch *b, int32_t slot, float *host_rho, float *host_ux,
                                      float *host_uy);
 LBM_API lbm_status lbm_batch_load_populations(lbm_batch *b, int32_t slot, const void *host,

@@ -317,6 +317,10 @@ class Batch:
                 "rows_per_block", "tiles")
         return dict(zip(keys, (int(v) for v in out)))
 
+    def set_slot_steps(self, slot, steps):
+        """Step budget of a slot (-1: none): later steps advance it by at most `steps` in total."""
+        self._chk(capi.lib().lbm_batch_set_slot_steps(self._b, int(slot), int(steps)))
+
     def steps_done(self, slot):
         v = ctypes.c_int64()
         self._chk(capi.lib().lbm_batch_slot_steps(self._b, int(slot), ctypes.byref(v)))

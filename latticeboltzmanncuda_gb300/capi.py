@@ -128,6 +128,7 @@ SIGNATURES = [
     ("lbm_batch_get_stream", _S, [_P, _P]),
     ("lbm_batch_info", _S, [_P, _P]),
     ("lbm_batch_slot_steps", _S, [_P, _I32, _P]),
+    ("lbm_batch_set_slot_steps", _S, [_P, _I32, _I64]),
     ("lbm_batch_moments", _S, [_P, _I32, _P, _P, _P]),
     ("lbm_batch_load_populations", _S, [_P, _I32, _P, _I32]),
     ("lbm_batch_retrieve_populations", _S, [_P, _I32, _P, _I32]),

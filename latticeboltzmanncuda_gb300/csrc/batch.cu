@@ -35,8 +35,8 @@ struct SlotDesc {  // device descriptor, one per slot
     const uint16_t *links;
     int nx, ny, pitch, plane;
     int periodic, force;
-    int cur;  // buffer holding the current state at the start of the launch sequence
-    int pad;
+    int cur;   // buffer holding the current state at the start of the launch sequence
+    int stop;  // steps this slot takes in the launch sequence (its remaining step budget)
     D2Q9Params prm;
 };
 
@@ -54,6 +54,7 @@ struct Slot {
     uint8_t *flags = nullptr;
     int cur = 0;
     int64_t steps_done = 0;
+    int64_t limit = -1;  // steps the slot may still take (-1: no limit)
     int64_t fluid = 0;
     size_t bytes = 0;
 };
@@ -68,6 +69,7 @@ __global__ void __launch_bounds__(256) batch_step_kernel(const SlotDesc *__restr
     const int t = reverse ? ntiles - 1 - (int)blockIdx.x : (int)blockIdx.x;
     const Tile tile = tiles[t];
     const SlotDesc D = slots[tile.slot];
+    if (step >= D.stop) return;  // the slot has used its step budget (uniform per block)
     const int y = tile.y0 + (int)threadIdx.y;
     if (y >= D.ny) return;  // uniform per warp
     const int x0 = (tile.xchunk * (int)blockDim.x + (int)threadIdx.x) * V;
@@ -174,16 +176,25 @@ struct CtxView {
     }
 };
 
-lbm_status rebuild(lbm_batch *b) {
-    if (!b->dirty) return LBM_OK;
+// steps slot s takes in a launch sequence of nsteps
+int64_t advance_of(const Slot &s, int64_t nsteps) { return s.limit < 0 ? nsteps : std::min(nsteps, s.limit); }
+
+// Descriptors and tiles for a launch sequence of nsteps (slots with a step budget stop early;
+// slots with no steps left get no tiles).
+lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
+    bool limited = false;
+    for (const Slot &s : b->slots) limited |= s.live && s.limit >= 0;
+    if (!b->dirty && !limited) return LBM_OK;
     std::vector<SlotDesc> descs(b->slots.size());
     std::vector<Tile> tiles;
-    const int cells_per_chunk = b->tx * b->v;
     for (size_t i = 0; i < b->slots.size(); ++i) {
         const Slot &s = b->slots[i];
         SlotDesc &d = descs[i];
         std::memset(&d, 0, sizeof(d));
         if (!s.live) continue;
+        const int64_t adv = advance_of(s, nsteps);
+        // only slots with a step budget stop early; their tables are rebuilt for every launch sequence
+        d.stop = s.limit < 0 ? INT32_MAX : (int)std::min<int64_t>(adv, INT32_MAX);
         d.f[0] = s.f[0];
         d.f[1] = s.f[1];
         d.links = s.links;
@@ -195,11 +206,11 @@ lbm_status rebuild(lbm_batch *b) {
         d.force = (s.desc.body_force[0] != 0.0f || s.desc.body_force[1] != 0.0f) ? 1 : 0;
         d.cur = s.cur;
         d.prm = d2q9_params(s.desc);
+        if (adv <= 0) continue;
         const int chunks = (s.pitch / b->v + b->tx - 1) / b->tx;
         for (int y0 = 0; y0 < s.desc.ny; y0 += b->ty)
             for (int xc = 0; xc < chunks; ++xc) tiles.push_back(Tile{(int)i, xc, y0, 0});
     }
-    (void)cells_per_chunk;
     BCUDA(b, cudaStreamSynchronize(b->stream), "batch: synchronize before table upload");
     if (descs.size() > b->desc_cap) {
         if (b->desc_d) cudaFree(b->desc_d);
@@ -278,7 +289,7 @@ lbm_status tune(lbm_batch *b) {
         b->tx = c.tx;
         b->ty = c.ty;
         b->dirty = true;
-        lbm_status st = rebuild(b);
+        lbm_status st = rebuild(b, 1);
         if (st != LBM_OK) return st;
         if (b->ntiles == 0) break;
         cudaError_t e = launch_any(b, 0, 0);
@@ -301,7 +312,7 @@ lbm_status tune(lbm_batch *b) {
     b->ty = pick.ty;
     b->dirty = true;
     b->tuned = true;
-    return rebuild(b);
+    return LBM_OK;
 }
 
 lbm_status ensure_staging(lbm_batch *b, size_t bytes) {
@@ -496,7 +507,7 @@ LBM_API lbm_status lbm_batch_step(lbm_batch *b, int32_t nsteps) {
         lbm_status st = tune(b);
         if (st != LBM_OK) return st;
     }
-    lbm_status st = rebuild(b);
+    lbm_status st = rebuild(b, nsteps);
     if (st != LBM_OK) return st;
     if (b->ntiles > 0) {
         for (int s = 0; s < nsteps; ++s) {
@@ -504,13 +515,23 @@ LBM_API lbm_status lbm_batch_step(lbm_batch *b, int32_t nsteps) {
         }
     }
     b->sweep += (unsigned)nsteps;
-    // every live slot advanced nsteps: its current buffer moves on by the parity of nsteps
+    // each live slot advanced by its own count: its current buffer moves on by that parity
     for (Slot &s : b->slots)
         if (s.live) {
-            s.cur = (s.cur + nsteps) & 1;
-            s.steps_done += nsteps;
+            const int64_t adv = advance_of(s, nsteps);
+            s.cur = (int)((s.cur + adv) & 1);
+            s.steps_done += adv;
+            if (s.limit >= 0) s.limit -= adv;
+            if (adv & 1) b->dirty = true;  // descriptors carry the parity
         }
-    if (nsteps & 1) b->dirty = true;  // descriptors carry the parity
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_batch_set_slot_steps(lbm_batch *b, int32_t slot, int64_t steps) {
+    Slot *s = get_slot(b, slot);
+    if (!s) return bfail(b, LBM_ERR_INVALID, "lbm_batch_set_slot_steps: no such slot");
+    s->limit = steps < 0 ? -1 : steps;
+    b->dirty = true;
     return LBM_OK;
 }
 

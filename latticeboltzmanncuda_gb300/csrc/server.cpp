@@ -8,9 +8,11 @@
 //             bytes fit into the budget next to the live solves (and a slot is free); a request that
 //             is larger than the whole budget is rejected (LBM_ERR_BUDGET), an invalid one fails
 //             alone (its own status) without stopping the others
-//   rounds    every round advances all live solves by min(round_steps, smallest remaining step
-//             count) steps with one launch per step; requests that arrive meanwhile join at the
-//             next round boundary, so their work overlaps on the device with the running ones
+//   rounds    every round is one launch per step for all live solves, min(round_steps, largest
+//             remaining step count) steps long; each solve carries its remaining step count as the
+//             batch slot's step budget, so one that finishes mid-round just stops there (its blocks
+//             exit at once); requests that arrive meanwhile join at the next round boundary, so
+//             their work overlaps on the device with the running ones
 //   retire    a finished solve's density and velocity are read back into the request's host
 //             buffers (if given), its slot is freed and its completion time recorded
 //
@@ -172,6 +174,7 @@ LBM_API lbm_status lbm_server_run(lbm_server *s, const lbm_request *reqs, int64_
                 continue;
             }
             results[r].slot = slot;
+            lbm_batch_set_slot_steps(s->batch, slot, q.steps);
             if (q.steps == 0) {
                 lbm_batch_remove(s->batch, slot);
                 finish(r, LBM_OK);
@@ -194,8 +197,9 @@ LBM_API lbm_status lbm_server_run(lbm_server *s, const lbm_request *reqs, int64_
             continue;
         }
 
-        int64_t k = cfg.round_steps;
-        for (const Live &l : live) k = std::min(k, l.remaining);
+        int64_t longest = 0;
+        for (const Live &l : live) longest = std::max(longest, l.remaining);
+        const int64_t k = std::min<int64_t>(cfg.round_steps, longest);
         lbm_status e = lbm_batch_step(s->batch, (int32_t)k);
         if (e == LBM_OK) e = lbm_batch_synchronize(s->batch);
         if (e != LBM_OK) {
@@ -207,8 +211,9 @@ LBM_API lbm_status lbm_server_run(lbm_server *s, const lbm_request *reqs, int64_
         std::vector<Live> still;
         still.reserve(live.size());
         for (Live &l : live) {
-            l.remaining -= k;
-            st.cell_updates += (double)reqs[l.req].nx * reqs[l.req].ny * (double)k;
+            const int64_t adv = std::min(k, l.remaining);
+            l.remaining -= adv;
+            st.cell_updates += (double)reqs[l.req].nx * reqs[l.req].ny * (double)adv;
             if (l.remaining > 0) {
                 still.push_back(l);
                 continue;

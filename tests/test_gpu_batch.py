@@ -112,6 +112,27 @@ def test_slots_join_and_leave_without_disturbing_others():
     assert np.array_equal(gc, single(c, init_state(c[0], c[1], 4), 12, "f32"))
 
 
+def test_step_budgets_stop_slots_mid_sequence():
+    """A slot with a step budget stops when it runs out, inside one lbm_batch_step call, and its
+    populations equal a solo run of exactly that many steps; slots without a budget run on."""
+    sp = specs()
+    budgets = [5, 12, -1, 0, 7, 30]
+    with lbm.Batch("f32") as B:
+        slots = []
+        for i, s in enumerate(sp):
+            slot = B.add(*s[:4], s[4], s[5], s[6])
+            B.load_populations(slot, init_state(s[0], s[1], 40 + i))
+            B.set_slot_steps(slot, budgets[i])
+            slots.append(slot)
+        B.step(9)
+        B.step(8)
+        for i, (s, slot) in enumerate(zip(sp, slots)):
+            want_steps = 17 if budgets[i] < 0 else min(17, budgets[i])
+            assert B.steps_done(slot) == want_steps
+            got = B.retrieve_populations(slot, np.float64)
+            assert np.array_equal(got, single(s, init_state(s[0], s[1], 40 + i), want_steps, "f32")), i
+
+
 @pytest.mark.parametrize("shape", [(2, 32, 1), (4, 32, 4), (4, 64, 2), (4, 128, 1), (8, 32, 8)])
 def test_every_batch_tile_shape(shape):
     sp = specs()
