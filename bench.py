@@ -55,7 +55,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--workload", default="channel", choices=["channel", "batch", "serve", "tgv"],
+    ap.add_argument("--d3-n", type=int, default=128)
+    ap.add_argument("--d3-steps", type=int, default=100)
+    ap.add_argument("--workload", default="channel", choices=["channel", "batch", "serve", "tgv", "d3q27"],
                     help="channel: the headline single-domain solve; batch: 512 uneven domains; "
                          "serve: Poisson request streams through the continuous-batching server; "
                          "tgv: Taylor-Green precision runs per storage type")
@@ -547,10 +549,94 @@ def run_tgv(args):
     return 0
 
 
+def d3q27_case(n):
+    """n^3 lattice in the reference CLI's set-up (LatticeBoltzmannCuda.cpp:53-73): populations 0.001
+    with f6 = 0.002, the same vector injected on the plane x = 0, plus a solid sphere of radius n/6
+    at the centre (internal cells)."""
+    cells = n ** 3
+    f = np.full((cells, 27), 0.001, np.float32)
+    f[:, 6] = 0.002
+    x, y, z = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    inside = ((x - n / 2) ** 2 + (y - n / 2) ** 2 + (z - n / 2) ** 2 <= (n / 6) ** 2).ravel()
+    flags = np.where(inside, 1, 0).astype(np.uint8)
+    plane = (x == 0).ravel()
+    induced = f[0].copy()
+    return f, flags, plane, induced
+
+
+def run_d3q27(args):
+    """The reference-compatible D3Q27 step (stream, reflect, collide, flow) on n^3 through the
+    library: MLUPS and the HBM roofline at 216 algorithmic bytes per cell update."""
+    import torch
+    import latticeboltzmanncuda_gb300 as lbm
+
+    n, steps = args.d3_n, args.d3_steps
+    f, flags, plane, induced = d3q27_case(n)
+    cells = n ** 3
+    stream = torch.cuda.Stream()
+    with lbm.Lattice(n, n, n, mode="d3q27_ref", tau=0.8, order=lbm.ORDER_CLI, stream=stream.cuda_stream) as L:
+        L.set_flags(flags)
+        L.set_flow(plane, induced)
+        L.load_populations(f)
+        L.step(args.warmup)
+        t = _timed(stream, lambda: L.step(steps))
+    mlups = cells * steps / t / 1e6
+    peak, kind = peaks()
+    achieved = mlups * 216 / 1000
+    line = {"metric": "MLUPS", "workload": "d3q27", "value": round(mlups, 1), "unit": "MLUPS", "steps": steps,
+            "higher_is_better": True, "dtype": "f32 (FP64 equilibrium)", "data": "synthetic",
+            "config": {"workload": f"D3Q27 reference step {n}^3, order stream-reflect-collide-flow, tau 0.8, "
+                                   f"solid sphere r = n/6, source plane x = 0", "cells": cells},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "peak_kind": kind, "bytes_per_update": 216}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_d3q27_reference(args):
+    """The same D3Q27 case on the reference's own kernels (compiled from its sources, run on this GPU
+    in Lattice.cpp's pass order with its full-lattice temporary copies) and on the CPU port."""
+    import oracle
+    from oracle import refkern
+
+    n, steps = args.d3_n, args.d3_steps
+    f, flags, plane, induced = d3q27_case(n)
+    cells = n ** 3
+    line = {"impl": "reference", "metric": "MLUPS", "workload": "d3q27", "unit": "MLUPS", "higher_is_better": True,
+            "data": "synthetic", "config": {"workload": f"D3Q27 reference step {n}^3 (as --workload d3q27)"}}
+    try:
+        if not refkern.available():
+            raise RuntimeError("reference kernels not built")
+        pts = np.zeros(cells, refkern.LATTICE_POINT)
+        pts["f"] = f
+        pts["isInternal"] = flags != 0
+        tz = min(n, 64)
+        shape = (1, max(1, min(n, 512 // tz)), tz)
+        refkern.run((n, n, n), pts, "SRCF", nsteps=1, tau=0.8, flow_criterion=2, induced=induced, threads=shape)
+        refkern.run((n, n, n), pts, "SRCF", nsteps=steps, tau=0.8, flow_criterion=2, induced=induced, threads=shape)
+        line["value"] = round(cells * steps / refkern.last_seconds() / 1e6, 1)
+        line["reference_gpu_kernels"] = {"mlups": line["value"], "seconds": refkern.last_seconds(),
+                                         "block": list(shape)}
+    except Exception as e:  # no GPU or no cubin: the CPU port alone
+        line["reference_gpu_kernels"] = {"unavailable": str(e)[:200]}
+    t0 = time.perf_counter()
+    oracle.d3q27_run((n, n, n), f, flags | np.where(plane, 4, 0).astype(np.uint8), 0.8, 2, order=1, induced=induced)
+    cpu = cells * 2 / (time.perf_counter() - t0) / 1e6
+    line["cpu_baseline"] = {"value": round(cpu, 2), "unit": "MLUPS", "cores": oracle.num_threads(), "kind": "port",
+                            "sample": f"{n}^3, 2 steps"}
+    line.setdefault("value", line["cpu_baseline"]["value"])
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.impl == "reference" and args.workload == "d3q27":
+        return run_d3q27_reference(args)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "d3q27":
+        return run_d3q27(args)
     if args.workload == "batch":
         return run_batch(args)
     if args.workload == "tgv":

@@ -17,6 +17,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -53,6 +54,7 @@ static_assert(sizeof(LatticePoint) == 144, "LatticePoint layout");
 static_assert(sizeof(ReflectionValues) == 380, "ReflectionValues layout");
 
 std::string g_err;
+double g_last_seconds = 0.0;
 CUmodule g_mod = nullptr;
 CUfunction g_stream, g_collide, g_reflect, g_flow, g_prime;
 CUdeviceptr g_crit_point = 0, g_crit_plane = 0;
@@ -100,6 +102,10 @@ int refl_dir(const ReflectionValues &r, int s) {
 extern "C" {
 
 const char *rk_error() { return g_err.c_str(); }
+
+// seconds of the last rk_run's step loop (launches, temporary copies and synchronisations; not the
+// set-up, upload or download)
+double rk_last_seconds() { return g_last_seconds; }
 
 int rk_init(const char *cubin_path) {
     if (g_mod) return 0;
@@ -189,6 +195,11 @@ int rk_run(int X, int Y, int Z, void *points, const int32_t *tab_cells, const vo
         LatticeData la = data_of(a, X, Y, Z), lb = data_of(b, X, Y, Z);
         void *pargs[] = {&la};
         if (launch(g_prime, X, Y, Z, pargs)) return -1;  // RunCudaFunctions::run_prime_points
+        const auto t_start = std::chrono::steady_clock::now();
+        struct StepTimer {  // wall time of the step loop (every launch above and below synchronises)
+            std::chrono::steady_clock::time_point t0;
+            ~StepTimer() { g_last_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+        } timer{t_start};
         for (int step = 0; step < nsteps; ++step) {
             for (const char *o = ops; *o; ++o) {
                 la = data_of(a, X, Y, Z);

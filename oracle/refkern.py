@@ -87,6 +87,7 @@ def harness():
         L = ctypes.CDLL(HARNESS)
         P = ctypes.c_void_p
         L.rk_error.restype = ctypes.c_char_p
+        L.rk_last_seconds.restype = ctypes.c_double
         L.rk_init.argtypes = [ctypes.c_char_p]
         L.rk_run.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, ctypes.c_int, ctypes.c_float,
                              ctypes.c_char_p, ctypes.c_int, ctypes.c_int, P, P, P]
@@ -118,3 +119,8 @@ def run(dims, points, ops, nsteps=1, tau=1.0, tab_cells=None, tab_records=None, 
     if rc != 0:
         raise RuntimeError("reference kernels: " + harness().rk_error().decode())
     return pts
+
+
+def last_seconds():
+    """Seconds of the last run()'s step loop."""
+    return float(harness().rk_last_seconds())
