@@ -333,6 +333,62 @@ LBM_API lbm_status lbm_gen_disks_fraction(int32_t nx, int32_t ny, float solid_fr
                                           float rmax, uint64_t seed, uint8_t *host_flags,
                                           float *achieved);
 
+/* ---------------------------------------------------------------- mesh front end (D3Q27_REF)
+ * The reference derives the D3Q27_REF cell flags and reflection tables from a closed triangle
+ * mesh with CGAL (Model.cpp, Geometry.cpp, Lattice.cpp:228-477).  These calls restate that
+ * pipeline on the host; they need no GPU and touch no context.  Lattice index z + Z*(y + Y*x),
+ * cell positions spacing * (x, y, z) in float, as the reference. */
+typedef struct lbm_mesh lbm_mesh;
+
+typedef struct lbm_mesh_info {
+    int64_t vertices;
+    int64_t faces;
+    int32_t triangle_mesh;   /* every face has 3 vertices */
+    int32_t closed;          /* no border edge: Model::isModelClosed (Model.cpp:46-49) */
+    int32_t valid;           /* triangle mesh and closed: !Model::checkError() (Model.h) */
+    int32_t reserved;
+    float bbox_min[3];       /* Model::bounding_box (Model.cpp:70-73) */
+    float bbox_max[3];
+} lbm_mesh_info;
+
+/* Wavefront OBJ, 'v' and 'f' records (f: 1-based or negative indices, "i/t/n" forms; other
+ * records and '#' comments ignored).  Replaces Model::importModel (Model.cpp:22-44); a missing
+ * file is an error here (the reference keeps an empty model). */
+LBM_API lbm_status lbm_mesh_load_obj(const char *path, lbm_mesh **out);
+/* The same from arrays: vertices[3*nv]; face k has face_sizes[k] >= 3 vertices, listed 0-based
+ * one face after another in face_indices. */
+LBM_API lbm_status lbm_mesh_create(const float *vertices, int64_t nv, const int32_t *face_sizes,
+                                   int64_t nf, const int32_t *face_indices, lbm_mesh **out);
+LBM_API void lbm_mesh_destroy(lbm_mesh *m);
+LBM_API lbm_status lbm_mesh_get_info(const lbm_mesh *m, lbm_mesh_info *out);
+/* Model::isPointInsideModel (Model.cpp:51-63): *inside = 1 inside or on the surface, 0 outside
+ * or when the mesh is not a closed triangle mesh. */
+LBM_API lbm_status lbm_mesh_point_inside(const lbm_mesh *m, const float point[3], int32_t *inside);
+/* Model::reflectionVector (Model.cpp:75-91): (p1 - p2) / |p1 - p2| rotated by pi about the normal
+ * of the first face hit by the ray from p1 through p2; (0, 0, 0) when the ray hits nothing. */
+LBM_API lbm_status lbm_mesh_reflection_vector(const lbm_mesh *m, const float p1[3], const float p2[3],
+                                              float out[3]);
+/* rotateVectorAroundAxis (Geometry.cpp:22-42): quaternion rotation of v about axis by angle. */
+LBM_API void lbm_rotate_vector(const float axis[3], const float v[3], float angle, float out[3]);
+/* Lattice::distributeVector (Lattice.cpp:262-321): the 27 directions q ranked by
+ * 2 - |v - c_q / |c_q||, highest first, equal scores by the larger q first. */
+LBM_API void lbm_distribute_vector(const float v[3], float score_out[27], int32_t dir_out[27]);
+/* Lattice::insertModel (Lattice.cpp:228-260): sets LBM_INTERNAL on the cells whose position is
+ * inside the mesh and clears it on the others; other flag bits are kept.  A mesh whose bounding
+ * box leaves [0, X*spacing] x [0, Y*spacing] x [0, Z*spacing] changes nothing (*applied = 0), as
+ * in the reference. */
+LBM_API lbm_status lbm_mesh_rasterize(const lbm_mesh *m, int32_t X, int32_t Y, int32_t Z, float spacing,
+                                      uint8_t *host_flags, int32_t *applied);
+/* Lattice::preProcessModel (Lattice.cpp:323-426): reflection tables for the LBM_INTERNAL cells
+ * next to non-internal cells, in the reference's cell order, ready for lbm_set_reflection_tables.
+ * With host_cells and host_records NULL only *count is set.  Otherwise capacity must be >=
+ * *count; host_cells[i] / host_records[i] (struct ReflectionValues) are written and LBM_REFLECTED
+ * is set on those cells.  The reference reads the neighbour in a chosen direction by its linear
+ * index without a range check; an index outside the lattice counts as not internal here. */
+LBM_API lbm_status lbm_mesh_reflection_tables(const lbm_mesh *m, int32_t X, int32_t Y, int32_t Z,
+                                              float spacing, uint8_t *host_flags, int64_t capacity,
+                                              int32_t *host_cells, void *host_records, int64_t *count);
+
 #ifdef __cplusplus
 }
 #endif

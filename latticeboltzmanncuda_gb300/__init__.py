@@ -18,7 +18,8 @@ from .capi import (BF16S, D2Q9, D3Q27_REF, F16S, F32, F64, FLUID, FORCE_MOMENTUM
                    OP_REFLECT, OP_STREAM, ORDER_CLI, ORDER_STREAM_COLLIDE, REFLECTED,
                    REFLECTION_VALUES, SOURCE, WALL, LBMError, check, ptr)
 
-__all__ = ["Lattice", "gen_channel", "gen_cavity", "gen_disks_fraction", "LBMError", "capi"]
+__all__ = ["Lattice", "Batch", "Mesh", "serve", "gen_channel", "gen_cavity", "gen_disks_fraction", "rotate_vector",
+           "distribute_vector", "LBMError", "capi"]
 
 
 def _mode(mode):
@@ -229,6 +230,101 @@ def gen_disks_fraction(flags, solid_fraction, rmin, rmax, seed):
     check(capi.lib().lbm_gen_disks_fraction(int(nx), int(ny), float(solid_fraction), float(rmin), float(rmax),
                                             ctypes.c_uint64(int(seed)), ptr(flags), ctypes.byref(ach)))
     return flags, float(ach.value)
+
+
+class Mesh:
+    """A triangle mesh for the D3Q27_REF geometry front end (Model, Model.cpp:22-91; host only)."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def load_obj(cls, path):
+        h = ctypes.c_void_p()
+        check(capi.lib().lbm_mesh_load_obj(str(path).encode(), ctypes.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_arrays(cls, vertices, faces):
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+        sizes = np.ascontiguousarray([len(f) for f in faces], dtype=np.int32)
+        idx = np.ascontiguousarray([i for f in faces for i in f], dtype=np.int32)
+        h = ctypes.c_void_p()
+        check(capi.lib().lbm_mesh_create(ptr(v), int(len(v)), ptr(sizes), int(len(sizes)), ptr(idx), ctypes.byref(h)))
+        return cls(h)
+
+    def close(self):
+        if self._h:
+            capi.lib().lbm_mesh_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def info(self) -> dict:
+        i = capi.MeshInfo()
+        check(capi.lib().lbm_mesh_get_info(self._h, ctypes.byref(i)))
+        return {"vertices": i.vertices, "faces": i.faces, "triangle_mesh": bool(i.triangle_mesh),
+                "closed": bool(i.closed), "valid": bool(i.valid), "bbox_min": tuple(i.bbox_min),
+                "bbox_max": tuple(i.bbox_max)}
+
+    def point_inside(self, p) -> bool:
+        pt = (ctypes.c_float * 3)(*[float(v) for v in p])
+        out = ctypes.c_int32()
+        check(capi.lib().lbm_mesh_point_inside(self._h, pt, ctypes.byref(out)))
+        return bool(out.value)
+
+    def reflection_vector(self, p1, p2):
+        a = (ctypes.c_float * 3)(*[float(v) for v in p1])
+        b = (ctypes.c_float * 3)(*[float(v) for v in p2])
+        out = (ctypes.c_float * 3)()
+        check(capi.lib().lbm_mesh_reflection_vector(self._h, a, b, out))
+        return np.array(out[:], dtype=np.float32)
+
+    def rasterize(self, dims, spacing, flags=None):
+        """Lattice::insertModel: returns (flags[X*Y*Z] with LBM_INTERNAL set/cleared, applied)."""
+        X, Y, Z = (int(d) for d in dims)
+        fl = np.zeros(X * Y * Z, np.uint8) if flags is None else np.ascontiguousarray(flags, dtype=np.uint8).reshape(-1).copy()
+        applied = ctypes.c_int32()
+        check(capi.lib().lbm_mesh_rasterize(self._h, X, Y, Z, float(spacing), ptr(fl), ctypes.byref(applied)))
+        return fl, bool(applied.value)
+
+    def reflection_tables(self, dims, spacing, flags):
+        """Lattice::preProcessModel: returns (cells, records, flags with LBM_REFLECTED added)."""
+        X, Y, Z = (int(d) for d in dims)
+        fl = np.ascontiguousarray(flags, dtype=np.uint8).reshape(-1).copy()
+        n = ctypes.c_int64()
+        L = capi.lib()
+        check(L.lbm_mesh_reflection_tables(self._h, X, Y, Z, float(spacing), ptr(fl), 0, None, None, ctypes.byref(n)))
+        cells = np.zeros(n.value, np.int32)
+        recs = np.zeros(n.value, REFLECTION_VALUES)
+        if n.value:
+            check(L.lbm_mesh_reflection_tables(self._h, X, Y, Z, float(spacing), ptr(fl), n.value, ptr(cells), ptr(recs),
+                                               ctypes.byref(n)))
+        return cells, recs, fl
+
+
+def rotate_vector(axis, v, angle):
+    """rotateVectorAroundAxis (Geometry.cpp:22-42)."""
+    a = (ctypes.c_float * 3)(*[float(x) for x in axis])
+    b = (ctypes.c_float * 3)(*[float(x) for x in v])
+    out = (ctypes.c_float * 3)()
+    capi.lib().lbm_rotate_vector(a, b, ctypes.c_float(float(angle)), out)
+    return np.array(out[:], dtype=np.float32)
+
+
+def distribute_vector(v):
+    """Lattice::distributeVector (Lattice.cpp:262-321): (scores[27], directions[27]), best first."""
+    a = (ctypes.c_float * 3)(*[float(x) for x in v])
+    score = np.zeros(27, np.float32)
+    dirs = np.zeros(27, np.int32)
+    capi.lib().lbm_distribute_vector(a, ptr(score), ptr(dirs))
+    return score, dirs
 
 
 def _desc_for(nx, ny, tau, periodic=0, body_force=(0.0, 0.0), wall_velocity=(0.0, 0.0)):

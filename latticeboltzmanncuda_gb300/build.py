@@ -23,7 +23,8 @@ OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "liblbm_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["common.cu", "capi.cu", "d2q9.cu", "d3q27.cu", "geometry.cpp", "noalloc.cu", "batch.cu", "server.cpp"]
+SOURCES = ["common.cu", "capi.cu", "d2q9.cu", "d3q27.cu", "geometry.cpp", "mesh.cpp", "noalloc.cu", "batch.cu",
+           "server.cpp"]
 
 
 def nvcc() -> str:
@@ -34,7 +35,8 @@ def nvcc() -> str:
 
 
 def _flags(debug: bool):
-    f = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden",
+    # host code: no floating-point contraction, so x86-64 and aarch64 builds give the same results
+    f = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
          "-I", INCLUDE, "-I", CSRC, "--expt-relaxed-constexpr"]
     if debug:
         f += ["-DLBM_CHECK_BOUNDS"]

@@ -84,6 +84,12 @@ class ServerStats(ctypes.Structure):
                 ("peak_bytes", ctypes.c_int64), ("peak_slots", ctypes.c_int32), ("rejected", ctypes.c_int32)]
 
 
+class MeshInfo(ctypes.Structure):
+    _fields_ = [("vertices", ctypes.c_int64), ("faces", ctypes.c_int64), ("triangle_mesh", ctypes.c_int32),
+                ("closed", ctypes.c_int32), ("valid", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("bbox_min", ctypes.c_float * 3), ("bbox_max", ctypes.c_float * 3)]
+
+
 # exported symbols and their signatures: (name, restype, argtypes)
 _P, _I32, _I64, _U64, _F = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64, ctypes.c_float
 _S = ctypes.c_int
@@ -141,6 +147,16 @@ SIGNATURES = [
     ("lbm_gen_channel", _S, [_I32, _I32, _I32, _F, _F, _U64, _P, _P]),
     ("lbm_gen_cavity", _S, [_I32, _I32, _P]),
     ("lbm_gen_disks_fraction", _S, [_I32, _I32, _F, _F, _F, _U64, _P, _P]),
+    ("lbm_mesh_load_obj", _S, [ctypes.c_char_p, _P]),
+    ("lbm_mesh_create", _S, [_P, _I64, _P, _I64, _P, _P]),
+    ("lbm_mesh_destroy", None, [_P]),
+    ("lbm_mesh_get_info", _S, [_P, _P]),
+    ("lbm_mesh_point_inside", _S, [_P, _P, _P]),
+    ("lbm_mesh_reflection_vector", _S, [_P, _P, _P, _P]),
+    ("lbm_rotate_vector", None, [_P, _P, _F, _P]),
+    ("lbm_distribute_vector", None, [_P, _P, _P]),
+    ("lbm_mesh_rasterize", _S, [_P, _I32, _I32, _I32, _F, _P, _P]),
+    ("lbm_mesh_reflection_tables", _S, [_P, _I32, _I32, _I32, _F, _P, _I64, _P, _P, _P]),
 ]
 
 _lib = None

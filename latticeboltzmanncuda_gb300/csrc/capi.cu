@@ -19,11 +19,7 @@ namespace {
 constexpr uint8_t F_GATHER = 8;
 
 // D3Q27 directions (SimCalcFuncs.cu:12), host copy for the gather-list construction
-constexpr int C27[27][3] = {
-    {0, 0, 0},   {-1, 0, 0},  {0, -1, 0},  {0, 0, -1},  {0, 0, 1},    {0, 1, 0},    {1, 0, 0},
-    {-1, -1, 0}, {-1, 0, -1}, {-1, 0, 1},  {-1, 1, 0},  {0, -1, -1},  {0, -1, 1},   {0, 1, -1},
-    {0, 1, 1},   {1, -1, 0},  {1, 0, -1},  {1, 0, 1},   {1, 1, 0},    {-1, -1, -1}, {-1, -1, 1},
-    {-1, 1, -1}, {-1, 1, 1},  {1, -1, -1}, {1, -1, 1},  {1, 1, -1},   {1, 1, 1}};
+constexpr auto &C27 = lbm::kD3Q27;
 
 #define CHECK_CTX(ctx)                                                              \
     do {                                                                            \

@@ -11,6 +11,20 @@
 
 namespace lbm {
 
+// D3Q27 directions in the reference's population order (SimCalcFuncs.cu:12, Constants.cpp:6),
+// host copy; the inverse of direction q is the q' with c_q' = -c_q (Constants.cpp:7).
+constexpr int kD3Q27[27][3] = {
+    {0, 0, 0},   {-1, 0, 0},  {0, -1, 0},  {0, 0, -1},  {0, 0, 1},    {0, 1, 0},    {1, 0, 0},
+    {-1, -1, 0}, {-1, 0, -1}, {-1, 0, 1},  {-1, 1, 0},  {0, -1, -1},  {0, -1, 1},   {0, 1, -1},
+    {0, 1, 1},   {1, -1, 0},  {1, 0, -1},  {1, 0, 1},   {1, 1, 0},    {-1, -1, -1}, {-1, -1, 1},
+    {-1, 1, -1}, {-1, 1, 1},  {1, -1, -1}, {1, -1, 1},  {1, 1, -1},   {1, 1, 1}};
+constexpr int d3q27_inverse(int q) {
+    for (int p = 0; p < 27; ++p)
+        if (kD3Q27[p][0] == -kD3Q27[q][0] && kD3Q27[p][1] == -kD3Q27[q][1] && kD3Q27[p][2] == -kD3Q27[q][2])
+            return p;
+    return -1;
+}
+
 // D3Q27_REF gather entry: population `src_pop` of reflecting cell `src_cell` is scattered with
 // weight `w` into population `dst_pop` of the target cell (the reference's push of
 // SimCalcFuncs.cu:164-186 turned into a pull).  `src_stream` is the cell the reflecting cell's
