@@ -4,8 +4,9 @@
  * This is the drop-in boundary for the reference's collide-stream path.  The reference exposes
  * that path as the C++ class Lattice (simulation/include/Lattice.h:40-106) on top of the launch
  * wrappers RunCudaFunctions::run_* (simulation/include/SimCalcFuncs.cuh:13-25); a C++
- * compatibility layer with those names is built on this ABI (see the package's simulation/
- * directory), and other languages bind these functions directly (ctypes, cgo, JNI).
+ * compatibility layer with those names is built on this ABI (latticeboltzmanncuda_gb300/compat:
+ * liblbm_compat.so and the reference's command line), and other languages bind these functions
+ * directly (ctypes, cgo, JNI).
  *
  * Conventions
  *   - Every function returns an lbm_status; lbm_last_error() gives the message of the last
@@ -169,12 +170,24 @@ LBM_API lbm_status lbm_set_flow(lbm_ctx *ctx, const uint8_t *host_mask, const fl
  * (Lattice::retrieve_reflection_data, Lattice.cpp:438-443). */
 LBM_API lbm_status lbm_set_force(lbm_ctx *ctx, const float host_in[3], int32_t enabled);
 LBM_API lbm_status lbm_get_force(lbm_ctx *ctx, float host_out[3]);
+/* Turn accumulation on or off keeping the running sum (the reference's plain reflection pass,
+ * run_calculate_reflections, adds no force); lbm_force_accumulation reports the current state. */
+LBM_API lbm_status lbm_set_force_accumulation(lbm_ctx *ctx, int32_t enabled);
+LBM_API int32_t lbm_force_accumulation(const lbm_ctx *ctx);
 
 /* ---------------------------------------------------------------- stepping */
 /* Advance nsteps fused time steps (one read and one write of the populations per step). */
 LBM_API lbm_status lbm_step(lbm_ctx *ctx, int32_t nsteps);
 /* D3Q27_REF: one separate pass (LBM_OP_*), as the reference's Lattice::simulate* methods. */
 LBM_API lbm_status lbm_apply(lbm_ctx *ctx, int32_t op);
+/* D3Q27_REF: the step order of later lbm_step() calls (LBM_ORDER_*), e.g. the stream-collide of
+ * Lattice::simulateLattice and the CLI loop on one lattice. */
+LBM_API lbm_status lbm_set_order(lbm_ctx *ctx, int32_t order);
+/* D3Q27_REF: lbm_step(nsteps) that also records the accumulated force after every step,
+ * host_series[3*s + k] = component k after step s + 1, with one device-to-host copy at the end.
+ * Replaces the force print of the reference CLI loop (LatticeBoltzmannCuda.cpp:78-93), which
+ * copies ReflectionData back and synchronises once per step. */
+LBM_API lbm_status lbm_step_force_series(lbm_ctx *ctx, int32_t nsteps, float *host_series);
 
 /* D2Q9 launch shape.  The first lbm_step() picks it with a built-in autotuner: every candidate
  * (cells per thread 1/2/4/8 as the storage type allows, block widths 32..256, 1..4 rows per block)

@@ -176,6 +176,16 @@ class Lattice:
     def apply(self, op):
         self._call("lbm_apply", int(op))
 
+    def set_order(self, order):
+        """D3Q27_REF: step order of later step() calls (ORDER_STREAM_COLLIDE or ORDER_CLI)."""
+        self._call("lbm_set_order", int(order))
+
+    def step_force_series(self, nsteps):
+        """D3Q27_REF: step nsteps and return the accumulated force after every step, float32[nsteps, 3]."""
+        out = np.zeros((int(nsteps), 3), np.float32)
+        self._call("lbm_step_force_series", int(nsteps), ptr(out))
+        return out
+
     def autotune(self, retune=False):
         """Run the launch-shape tuner; returns (cells_per_thread, block_threads, rows_per_block, l2_policy)."""
         self._call("lbm_autotune", int(bool(retune)))

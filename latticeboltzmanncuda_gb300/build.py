@@ -21,6 +21,9 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "liblbm_gb300.so")
+COMPAT = os.path.join(PKG, "compat")
+COMPAT_LIB = os.path.join(PKG, "liblbm_compat.so")
+CLI = os.path.join(PKG, "bin", "LatticeBoltzmannCuda")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["common.cu", "capi.cu", "d2q9.cu", "d3q27.cu", "geometry.cpp", "mesh.cpp", "noalloc.cu", "batch.cu",
@@ -65,6 +68,7 @@ def build(force: bool = False, debug: bool = False, verbose: bool = False) -> st
     if not force and os.path.exists(LIB) and os.path.exists(stamp):
         with open(stamp) as fh:
             if fh.read().strip() == digest:
+                build_compat()
                 return LIB
     cc = nvcc()
     flags = _flags(debug)
@@ -89,9 +93,50 @@ def build(force: bool = False, debug: bool = False, verbose: bool = False) -> st
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_compat(force=True)
     with open(stamp, "w") as fh:
         fh.write(digest)
     return LIB
+
+
+def _cxx() -> str:
+    for cand in (os.environ.get("CXX"), shutil.which("g++"), shutil.which("c++")):
+        if cand:
+            return cand
+    raise RuntimeError("no C++ compiler found for the compatibility layer")
+
+
+def build_compat(force: bool = False) -> str:
+    """The reference's C++ API (compat/include, compat/src/compat.cpp) as liblbm_compat.so on top of
+    liblbm_gb300.so, and the reference's command line as bin/LatticeBoltzmannCuda."""
+    srcs = [os.path.join(COMPAT, "src", f) for f in ("compat.cpp", "LatticeBoltzmannCuda.cpp")]
+    hdrs = [os.path.join(COMPAT, "include", f) for f in sorted(os.listdir(os.path.join(COMPAT, "include")))]
+    stamp = os.path.join(OUT_DIR, "compat.stamp")
+    digest = _digest(srcs + hdrs + [os.path.join(INCLUDE, "lbm_capi.h")], "compat")
+    if not force and os.path.exists(COMPAT_LIB) and os.path.exists(CLI) and os.path.exists(stamp):
+        with open(stamp) as fh:
+            if fh.read().strip() == digest:
+                return COMPAT_LIB
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "include")
+    common = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-I", os.path.join(COMPAT, "include"),
+              "-I", INCLUDE, "-I", cuda_inc]
+    os.makedirs(os.path.dirname(CLI), exist_ok=True)
+    steps = [
+        [_cxx(), *common, "-shared", srcs[0], "-o", COMPAT_LIB + ".tmp", "-L", PKG, "-llbm_gb300",
+         "-Wl,-rpath,$ORIGIN"],
+        [_cxx(), *common, srcs[1], "-o", CLI + ".tmp", "-L", PKG, "-llbm_compat", "-llbm_gb300",
+         "-Wl,-rpath,$ORIGIN/.."],
+    ]
+    for cmd, out in zip(steps, (COMPAT_LIB, CLI)):
+        if cmd is steps[1]:
+            os.replace(COMPAT_LIB + ".tmp", COMPAT_LIB)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compatibility layer build failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(CLI + ".tmp", CLI)
+    with open(stamp, "w") as fh:
+        fh.write(digest)
+    return COMPAT_LIB
 
 
 def main():

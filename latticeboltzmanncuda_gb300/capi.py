@@ -116,6 +116,10 @@ SIGNATURES = [
     ("lbm_get_force", _S, [_P, _P]),
     ("lbm_step", _S, [_P, _I32]),
     ("lbm_apply", _S, [_P, _I32]),
+    ("lbm_set_order", _S, [_P, _I32]),
+    ("lbm_set_force_accumulation", _S, [_P, _I32]),
+    ("lbm_force_accumulation", _I32, [_P]),
+    ("lbm_step_force_series", _S, [_P, _I32, _P]),
     ("lbm_autotune", _S, [_P, _I32]),
     ("lbm_set_launch", _S, [_P, _I32, _I32, _I32, _I32]),
     ("lbm_set_sweep_alternation", _S, [_P, _I32]),

@@ -531,6 +531,19 @@ LBM_API lbm_status lbm_set_force(lbm_ctx *ctx, const float in[3], int32_t enable
     return sync(ctx, "upload force");
 }
 
+LBM_API lbm_status lbm_set_force_accumulation(lbm_ctx *ctx, int32_t enabled) {
+    CHECK_CTX(ctx);
+    if (ctx->desc.mode != LBM_D3Q27_REF) return fail(ctx, LBM_ERR_UNSUPPORTED, "force accumulation is D3Q27_REF only");
+    lbm_status st = use_device(ctx);
+    if (st != LBM_OK) return st;
+    ctx->force_on = enabled != 0;
+    if (ctx->force_on && (st = ensure_scratch(ctx, std::max<size_t>((size_t)((ctx->ntgt + 127) / 128) * 3, 512 * 4))) != LBM_OK)
+        return st;
+    return LBM_OK;
+}
+
+LBM_API int32_t lbm_force_accumulation(const lbm_ctx *ctx) { return ctx && ctx->force_on ? 1 : 0; }
+
 LBM_API lbm_status lbm_get_force(lbm_ctx *ctx, float out[3]) {
     CHECK_CTX(ctx);
     if (!out) return fail(ctx, LBM_ERR_INVALID, "null output");
@@ -557,6 +570,37 @@ LBM_API lbm_status lbm_step(lbm_ctx *ctx, int32_t nsteps) {
         CUDA_TRY(ctx, d3q27_step(ctx, nsteps), "D3Q27 step");
     }
     ctx->steps_done += nsteps;
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_step_force_series(lbm_ctx *ctx, int32_t nsteps, float *host_series) {
+    CHECK_CTX(ctx);
+    if (ctx->desc.mode != LBM_D3Q27_REF) return fail(ctx, LBM_ERR_UNSUPPORTED, "force series are D3Q27_REF only");
+    if (nsteps < 0 || (nsteps > 0 && !host_series)) return fail(ctx, LBM_ERR_INVALID, "bad nsteps or null series");
+    if (nsteps == 0) return LBM_OK;
+    lbm_status st = use_device(ctx);
+    if (st != LBM_OK) return st;
+    if ((st = d3_prepare(ctx)) != LBM_OK) return st;
+    double *series_d = nullptr;
+    const size_t bytes = (size_t)nsteps * 3 * sizeof(double);
+    if ((st = dalloc(ctx, (void **)&series_d, bytes, "force series")) != LBM_OK) return st;
+    std::vector<double> h((size_t)nsteps * 3);
+    cudaError_t e = d3q27_step(ctx, nsteps, series_d);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), series_d, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dfree(ctx, series_d, bytes);
+    if (e != cudaSuccess) return fail(ctx, e == cudaErrorMemoryAllocation ? LBM_ERR_OOM : LBM_ERR_CUDA,
+                                      std::string("D3Q27 step with force series: ") + cudaGetErrorString(e));
+    for (size_t i = 0; i < h.size(); ++i) host_series[i] = (float)h[i];
+    ctx->steps_done += nsteps;
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_set_order(lbm_ctx *ctx, int32_t order) {
+    CHECK_CTX(ctx);
+    if (ctx->desc.mode != LBM_D3Q27_REF) return fail(ctx, LBM_ERR_UNSUPPORTED, "step orders are D3Q27_REF only");
+    if (order != LBM_ORDER_STREAM_COLLIDE && order != LBM_ORDER_CLI) return fail(ctx, LBM_ERR_INVALID, "unknown step order");
+    ctx->desc.order = order;
     return LBM_OK;
 }
 

@@ -10,12 +10,14 @@ thread_local std::string g_thread_error;
 
 // out[k] (+)= sum over b of partials[b*ncomp + k], one thread per component, in block order
 __global__ void finalize_kernel(const double *__restrict__ partials, int nblocks, int ncomp, double *out,
-                                int accumulate) {
+                                int accumulate, double *also) {
     const int k = threadIdx.x;
     if (k >= ncomp) return;
     double s = 0.0;
     for (int b = 0; b < nblocks; ++b) s += partials[(int64_t)b * ncomp + k];
-    out[k] = accumulate ? out[k] + s : s;
+    const double v = accumulate ? out[k] + s : s;
+    out[k] = v;
+    if (also) also[k] = v;
 }
 }  // namespace
 
@@ -72,8 +74,8 @@ lbm_status ensure_scratch(lbm_ctx *ctx, size_t n) {
 }
 
 cudaError_t finalize_sums(cudaStream_t s, const double *partials, int nblocks, int ncomp, double *out,
-                          bool accumulate) {
-    finalize_kernel<<<1, 32, 0, s>>>(partials, nblocks, ncomp, out, accumulate ? 1 : 0);
+                          bool accumulate, double *also) {
+    finalize_kernel<<<1, 32, 0, s>>>(partials, nblocks, ncomp, out, accumulate ? 1 : 0, also);
     return cudaGetLastError();
 }
 

@@ -335,7 +335,7 @@ GatherArgs gather_args(lbm_ctx *ctx) {
     return g;
 }
 
-cudaError_t launch_gather(lbm_ctx *ctx, const StepArgs &a, int mode) {
+cudaError_t launch_gather(lbm_ctx *ctx, const StepArgs &a, int mode, double *force_copy = nullptr) {
     if (ctx->ntgt == 0) return cudaSuccess;
     GatherArgs g = gather_args(ctx);
     const int threads = 128;
@@ -346,12 +346,12 @@ cudaError_t launch_gather(lbm_ctx *ctx, const StepArgs &a, int mode) {
         gather_kernel<1><<<nb, threads, 0, ctx->stream>>>(a, g);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !g.partials) return e;
-    return finalize_sums(ctx->stream, g.partials, (int)nb, 3, ctx->force_acc_d, true);
+    return finalize_sums(ctx->stream, g.partials, (int)nb, 3, ctx->force_acc_d, true, force_copy);
 }
 
 }  // namespace
 
-cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps) {
+cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps, double *series_d) {
     const int threads = 256;
     for (int s = 0; s < nsteps; ++s) {
         StepArgs a;
@@ -365,8 +365,14 @@ cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps) {
         fused_kernel<<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
+        double *copy = series_d ? series_d + 3 * (int64_t)s : nullptr;
+        const bool reduced = a.cli && ctx->ntgt > 0 && ctx->force_on;  // the force changes this step
         if (a.cli) {
-            e = launch_gather(ctx, a, 0);
+            e = launch_gather(ctx, a, 0, copy);
+            if (e != cudaSuccess) return e;
+        }
+        if (copy && !reduced) {
+            e = cudaMemcpyAsync(copy, ctx->force_acc_d, 3 * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
             if (e != cudaSuccess) return e;
         }
         ctx->cur ^= 1;

@@ -148,7 +148,8 @@ cudaError_t d2q9_load(lbm_ctx *ctx, const void *src_d, int src_dtype, int aos);
 cudaError_t d2q9_store(lbm_ctx *ctx, void *dst_d, int dst_dtype, int aos);
 
 // D3Q27_REF launchers (d3q27.cu)
-cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps);
+// series_d (optional): the accumulated force after step s is written to series_d[3s..3s+2]
+cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps, double *series_d = nullptr);
 cudaError_t d3q27_apply(lbm_ctx *ctx, int op);
 cudaError_t d3q27_moments(lbm_ctx *ctx, float *rho_d, float *ux_d, float *uy_d, float *uz_d);
 cudaError_t d3q27_conservation(lbm_ctx *ctx, double *out_d);
@@ -156,7 +157,8 @@ cudaError_t d3q27_load(lbm_ctx *ctx, const void *src_d, int src_dtype, int aos);
 cudaError_t d3q27_store(lbm_ctx *ctx, void *dst_d, int dst_dtype, int aos);
 
 // reduction finaliser (common.cu): out[k] (+)= sum_b partials[b*ncomp + k], fixed order
+// out[k] (+)= sum over blocks of partials[b][k]; the result is also written to also[k] if given
 cudaError_t finalize_sums(cudaStream_t s, const double *partials, int nblocks, int ncomp, double *out,
-                          bool accumulate = false);
+                          bool accumulate = false, double *also = nullptr);
 
 }  // namespace lbm

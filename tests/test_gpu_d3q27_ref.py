@@ -274,3 +274,117 @@ def test_rejects_bad_tables():
             L.set_reflection_tables([13, 13], np.zeros(2, lbm.REFLECTION_VALUES))
         with pytest.raises(lbm.LBMError):
             L.set_reflection_tables([99], np.zeros(1, lbm.REFLECTION_VALUES))
+
+
+# ------------------------------------------------------------------ mesh front end + library
+@pytest.mark.parametrize("with_force", [False, True])
+def test_reflections_from_mesh(golden, with_force):
+    """CalculationsTest.cpp:107-197 with the flags and tables built by the mesh front end
+    (insertModel + preProcessModel) and the reflection pass on the GPU; the force meets the
+    reference's own 1e-6 bound."""
+    from test_mesh_front_end import golden_mesh
+    dims = (3, 3, 3)
+    m = golden_mesh(golden, "cube_angled.obj")
+    flags, _ = m.rasterize(dims, 0.5)
+    cells, recs, flags = m.reflection_tables(dims, 0.5, flags)
+    f = np.zeros((27, 27), np.float32)
+    f[cell(dims, 1, 1, 1), 1] = 1.0
+    name = "CalculationsTest.TestReflectionsData" if with_force else "CalculationsTest.TestReflections"
+    lines = (186, 187, 188, 190) if with_force else (141, 142, 143, 145)
+    with lattice(dims) as L:
+        L.set_flags(flags)
+        L.load_populations(f)
+        L.set_reflection_tables(cells, recs)
+        if with_force:
+            L.set_force((0, 0, 0), True)
+        L.apply(lbm.OP_REFLECT)
+        out = L.retrieve_populations()
+        force = L.get_force()
+    for (x, y, z, q), line in zip(((2, 1, 2, 17), (1, 1, 2, 4), (2, 2, 2, 26), (1, 1, 1, 1)), lines):
+        near(out[cell(dims, x, y, z), q], known(golden, name, line))
+    if with_force:
+        for k, line in enumerate((194, 195, 196)):
+            near(force[k], known(golden, "CalculationsTest.TestReflectionsData", line))
+
+
+def test_sphere_mesh_steps_match_oracle():
+    """A sphere mesh rasterised on 20^3, its tables from the front end, 5 CLI-order steps with the
+    force: library vs CPU oracle."""
+    from refcases import icosphere
+    dims = (20, 20, 20)
+    verts, faces = icosphere(2, 0.3, (0.5, 0.5, 0.5))
+    m = lbm.Mesh.from_arrays(verts, faces)
+    flags, applied = m.rasterize(dims, 1 / 19)
+    assert applied
+    cells, recs, flags = m.reflection_tables(dims, 1 / 19, flags)
+    assert len(cells) > 100
+    n = 20 ** 3
+    rng = np.random.default_rng(8)
+    f = (rng.random((n, 27), dtype=np.float32) * 0.05).astype(np.float32)
+    flags[: 20 * 20] |= SOURCE
+    induced = (rng.random(27) * 1e-3).astype(np.float32)
+    tab_idx = np.full(n, -1, np.int32)
+    tab_idx[cells] = np.arange(len(cells), dtype=np.int32)
+    force_ref = np.zeros(3, np.float32)
+    ref = oracle.d3q27_run(dims, f, flags, 0.8, 5, order=lbm.ORDER_CLI, tab_idx=tab_idx, tabs=recs,
+                           induced=induced, force=force_ref, force_mode=lbm.FORCE_REFERENCE)
+    with lattice(dims, tau=0.8, order=lbm.ORDER_CLI) as L:
+        L.set_flags(flags)
+        L.load_populations(f)
+        L.set_reflection_tables(cells, recs)
+        L.set_flow(flags & SOURCE, induced)
+        L.set_force((0, 0, 0), True)
+        L.step(5)
+        got = L.retrieve_populations()
+        force = L.get_force()
+    close(got, ref)
+    assert np.max(np.abs(force - force_ref)) <= 1e-5 * max(1e-30, float(np.max(np.abs(force_ref))))
+
+
+def test_force_series_equals_per_step_reads():
+    """lbm_step_force_series records the same running force as one lbm_step + lbm_get_force per
+    step (the reference CLI's print loop), and leaves the same populations."""
+    dims = (9, 7, 9)
+    f, flags, cells, recs, induced = random_lattice(dims, 31)
+    start = np.array([0.25, 0.0, -0.5], np.float32)
+
+    def make():
+        L = lattice(dims, tau=0.8, order=lbm.ORDER_CLI)
+        L.set_flags(flags)
+        L.load_populations(f)
+        L.set_reflection_tables(cells, recs)
+        L.set_flow(flags & SOURCE, induced)
+        L.set_force(start, True)
+        return L
+
+    with make() as A, make() as B:
+        series = A.step_force_series(7)
+        per_step = []
+        for _ in range(7):
+            B.step(1)
+            per_step.append(B.get_force())
+        assert np.array_equal(series, np.array(per_step, np.float32))
+        assert np.array_equal(A.retrieve_populations(), B.retrieve_populations())
+        assert not np.array_equal(series[0], start)
+
+
+def test_set_order_switches_the_fused_step():
+    dims = (6, 5, 6)
+    f, flags, cells, recs, induced = random_lattice(dims, 41)
+    with lattice(dims, tau=0.9) as L:
+        L.set_flags(flags)
+        L.load_populations(f)
+        L.set_reflection_tables(cells, recs)
+        L.set_flow(flags & SOURCE, induced)
+        L.step(2)
+        L.set_order(lbm.ORDER_CLI)
+        L.step(3)
+        got = L.retrieve_populations()
+        with pytest.raises(lbm.LBMError):
+            L.set_order(7)
+    tab_idx = np.full(f.shape[0], -1, np.int32)
+    tab_idx[cells] = np.arange(len(cells), dtype=np.int32)
+    ref = oracle.d3q27_run(dims, f, flags, 0.9, 2, order=lbm.ORDER_STREAM_COLLIDE, tab_idx=tab_idx, tabs=recs,
+                           induced=induced)
+    ref = oracle.d3q27_run(dims, ref, flags, 0.9, 3, order=lbm.ORDER_CLI, tab_idx=tab_idx, tabs=recs, induced=induced)
+    close(got, ref)

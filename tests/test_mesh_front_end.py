@@ -12,7 +12,7 @@ import pytest
 import latticeboltzmanncuda_gb300 as lbm
 import oracle
 from conftest import known
-from refcases import INTERNAL, REFLECTED, cell
+from refcases import INTERNAL, REFLECTED, cell, icosphere
 
 
 def golden_mesh(golden, name):
@@ -207,31 +207,6 @@ def test_reflection_table_structure(golden):
             for d in used:
                 nb = cell(dims, x + oracle.C27[d][0], y + oracle.C27[d][1], z + oracle.C27[d][2])
                 assert not flags[nb] & INTERNAL
-
-
-def icosphere(level=3, r=1.0, c=(0.0, 0.0, 0.0)):
-    t = (1 + 5 ** 0.5) / 2
-    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
-         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
-    v = [np.array(p, float) / np.linalg.norm(p) for p in v]
-    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
-         (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
-         (8, 6, 7), (9, 8, 1)]
-    for _ in range(level):
-        cache, nf = {}, []
-
-        def mid(a, b):
-            k = (min(a, b), max(a, b))
-            if k not in cache:
-                p = v[a] + v[b]
-                v.append(p / np.linalg.norm(p))
-                cache[k] = len(v) - 1
-            return cache[k]
-        for a, b, cc in f:
-            ab, bc, ca = mid(a, b), mid(b, cc), mid(cc, a)
-            nf += [(a, ab, ca), (b, bc, ab), (cc, ca, bc), (ab, bc, ca)]
-        f = nf
-    return np.array(v) * r + np.array(c), f
 
 
 def test_point_in_sphere_mesh_matches_geometry():
