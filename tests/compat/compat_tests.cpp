@@ -29,6 +29,15 @@ static void got(const char* test, int line, double v) { printf("{\"test\": \"%s\
 static void mismatches(const char* test, int line, long n) { printf("{\"test\": \"%s\", \"line\": %d, \"mismatches\": %ld}\n", test, line, n); }
 static std::string mesh(const char* name) { return g_dir + "/" + name; }
 
+// The reference's tests load `new LatticePoint[n]` without initialising it and rely on fresh heap
+// memory reading as zero; here the arrays are zeroed explicitly.
+static LatticePoint* zeroed(size_t n)
+{
+    LatticePoint* a = new LatticePoint[n];
+    memset(static_cast<void*>(a), 0, sizeof(LatticePoint) * n);
+    return a;
+}
+
 static int at(Lattice& l, int x, int y, int z)
 {
     dim3 d = l.getDimensions();
@@ -41,8 +50,7 @@ static void TestStreaming()
     dim3 threads(1, 2, 1), blocks(1, 1, 1);
     Lattice lattice(1, 2, 1, blocks, threads, FluidData(1.0, 1.0), 0.1);
     LatticeData data(lattice.getCudaDataPointer(), lattice.getDimensions());
-    LatticePoint* a = new LatticePoint[2];
-    memset(a, 0, sizeof(LatticePoint) * 2);
+    LatticePoint* a = zeroed(2);
     a[0].particle_distribution[5] = 2.0;
     lattice.load_data(a);
     RunCudaFunctions::run_prime_points(blocks, threads, data);
@@ -57,8 +65,7 @@ static void TestCollision()
 {
     dim3 threads(1, 1, 1), blocks(1, 1, 1);
     Lattice lattice(1, 1, 1, blocks, threads, FluidData(1.0, 1.0), 0.1);
-    LatticePoint* a = new LatticePoint[1];
-    memset(a, 0, sizeof(LatticePoint));
+    LatticePoint* a = zeroed(1);
     a[0].particle_distribution[0] = 2.0;
     lattice.load_data(a);
     lattice.simulateCollision();
@@ -74,8 +81,7 @@ static void TestFull()
 {
     dim3 threads(1, 2, 1), blocks(1, 1, 1);
     Lattice lattice(1, 2, 1, blocks, threads, FluidData(1.0, 1.0), 0.1);
-    LatticePoint* a = new LatticePoint[2];
-    memset(a, 0, sizeof(LatticePoint) * 2);
+    LatticePoint* a = zeroed(2);
     a[0].particle_distribution[5] = 2.0;
     lattice.load_data(a);
     lattice.simulateLattice();
@@ -124,7 +130,7 @@ static void TestFlowGeneration(bool plane)
     dim3 threads(3, 3, 3), blocks(1, 1, 1);
     Lattice lattice(3, 3, 3, blocks, threads, FluidData(1.0, 1.0), 0.5);
     LatticeData data(lattice.getCudaDataPointer(), lattice.getDimensions());
-    LatticePoint* a = new LatticePoint[27];
+    LatticePoint* a = zeroed(27);
     lattice.load_data(a);
     delete[] a;
     RunCudaFunctions::run_prime_points(blocks, threads, data);
@@ -159,7 +165,7 @@ static void TestCoordsMatch()
 {
     dim3 threads(10, 10, 10), blocks(10, 10, 10);
     Lattice lattice(100, 100, 100, blocks, threads, FluidData(1.0, 1.0), 0.1);
-    LatticePoint* a = new LatticePoint[100 * 100 * 100];
+    LatticePoint* a = zeroed(100 * 100 * 100);
     int counter = 0;
     for (int x = 0; x < 100; ++x)
         for (int y = 0; y < 100; ++y)
@@ -191,7 +197,7 @@ static void TestCoordinatesWithModel()
 {
     dim3 threads(1, 1, 1), blocks(10, 10, 10);
     Lattice lattice(10, 10, 10, blocks, threads, FluidData(1.0, 1.0), 0.1);
-    LatticePoint* a = new LatticePoint[10 * 10 * 10];
+    LatticePoint* a = zeroed(10 * 10 * 10);
     lattice.load_data(a);
     delete[] a;
     lattice.insertModel(mesh("compat_cube.obj"));
@@ -222,7 +228,7 @@ static void TestReflection()
 {
     dim3 threads(3, 3, 3), blocks(1, 1, 1);
     Lattice lattice(3, 3, 3, blocks, threads, FluidData(1.0, 1.0), 0.5);
-    LatticePoint* a = new LatticePoint[27];
+    LatticePoint* a = zeroed(27);
     lattice.load_data(a);
     delete[] a;
     lattice.insertModel(mesh("cube_angled.obj"));
