@@ -148,7 +148,7 @@ def test_sphere_mesh_cli_matches_reference():
     reference's own kernels on the same flags and tables (X == Z, grid tiled exactly)."""
     from refcases import icosphere
     dims, threads = (24, 16, 24), (1, 16, 24)
-    verts, faces = icosphere(2, 0.3, (0.5, 0.5, 0.5))
+    verts, faces = icosphere(2, 0.25, (0.5, 0.34, 0.5))  # inside [0, 24/23] x [0, 16/23] x [0, 24/23]
     m = lbm.Mesh.from_arrays(verts, faces)
     spacing = 1 / 23
     flags, applied = m.rasterize(dims, spacing)
