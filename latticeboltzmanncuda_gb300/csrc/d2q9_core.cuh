@@ -331,6 +331,38 @@ __device__ __forceinline__ void equilibrium_h(R drho, R rho, R ux, R uy, R h[9])
     }
 }
 
+template <class S>
+struct is_half_store : std::false_type {};
+template <>
+struct is_half_store<__half> : std::true_type {};
+template <>
+struct is_half_store<__nv_bfloat16> : std::true_type {};
+
+// Conservative rounding for 16-bit storage.  Rounding the nine post-collision populations to FP16
+// or BF16 one by one leaves residuals in mass and momentum that are conserved by the dynamics and
+// so accumulate step after step (and a body-force increment smaller than half an ulp is lost every
+// step).  Here the rounding residuals r_q = h_q - round(h_q) of the rest and axis populations are
+// moved into the diagonal populations before those are rounded: in f space the residual mass and
+// momentum are spread over the four diagonals as a_d = (dm + c_d . dj) / 4, which in storage space
+// (h = s f / w, w_0 = 16 w_d, w_axis = 4 w_d) is  h_d += 4 r_0 + 2 (r_a + r_b)  with a, b the axis
+// populations with c_a + c_b = c_d.  What remains is the diagonals' own rounding, whose absolute
+// resolution is 4x (momentum) and 16x (mass) finer.
+template <class S, class R>
+__device__ __forceinline__ void conserve_rounding(R h[9]) {
+    R r[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        const R hr = Store<S>::to(Store<S>::from(h[q]));
+        r[q] = sub_(h[q], hr);
+        h[q] = hr;
+    }
+    const R r0x4 = mul_((R)4, r[0]);
+    h[5] = add_(h[5], fma_((R)2, add_(r[1], r[2]), r0x4));
+    h[6] = add_(h[6], fma_((R)2, add_(r[2], r[3]), r0x4));
+    h[7] = add_(h[7], fma_((R)2, add_(r[3], r[4]), r0x4));
+    h[8] = add_(h[8], fma_((R)2, add_(r[4], r[1]), r0x4));
+}
+
 // BGK collision with Guo forcing, in place, in storage space.  Opposite populations q, q' share
 // c_q . u with opposite signs, so the equilibrium and the forcing term split into a symmetric part
 // A and an antisymmetric part B per pair: h_q <- (1 - om) h_q + A + B, h_q' <- (1 - om) h_q' + A - B,
@@ -382,6 +414,7 @@ __device__ __forceinline__ void collide(R h[9], R om, Vec2<R> F) {
     pair(2, 4, uy, F.y);
     pair(5, 7, add_(ux, uy), add_(F.x, F.y));
     pair(8, 6, sub_(ux, uy), sub_(F.x, F.y));
+    if constexpr (is_half_store<S>::value) conserve_rounding<S, R>(h);
 }
 
 }  // namespace d2q9
