@@ -25,6 +25,7 @@
 
 #include "lbm_internal.h"
 #include "d2q9_core.cuh"
+#include "d2q9_stage.cuh"
 #include "d2q9_vec.cuh"
 #include "reduce.cuh"
 
@@ -117,6 +118,21 @@ __global__ void __launch_bounds__(256) step_vec_kernel(const S *__restrict__ src
     const int y = reverse ? ny - 1 - row : row;
     const int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * V;
     d2q9::step_vec<S, V, FORCE, int, POL>(src, dst, links, x0, y, nx, ny, pitch, plane, periodic, prm);
+}
+
+// 16-bit storage: block (bx, by) sweeps strip bx (cells bx*W .. bx*W+W-1) over rows
+// [by*rows, by*rows + rows); with `reverse` the blocks take the strips and row runs in reverse order.
+template <class S, bool FORCE>
+__global__ void __launch_bounds__(d2q9::stage::THREADS) stage_kernel(const S *__restrict__ src, S *__restrict__ dst,
+                                                                    const uint16_t *__restrict__ links, int nx, int ny,
+                                                                    int pitch, int plane, int periodic, D2Q9Params prm,
+                                                                    int rows, int reverse) {
+    __shared__ d2q9::stage::Ring<S> ring;
+    const int bx = reverse ? (int)(gridDim.x - 1 - blockIdx.x) : (int)blockIdx.x;
+    const int by = reverse ? (int)(gridDim.y - 1 - blockIdx.y) : (int)blockIdx.y;
+    const int ya = by * rows;
+    d2q9::stage::sweep<S, FORCE>(ring, src, dst, links, bx * d2q9::stage::W, ya, min(ya + rows, ny), nx, ny, pitch,
+                                 plane, periodic, prm);
 }
 
 template <class S>
@@ -289,6 +305,17 @@ cudaError_t launch_one(lbm_ctx *ctx, const Shape &sh, const S *src, S *dst, int 
         return cudaGetLastError();
     }
     const int pitch = (int)ctx->pitch, plane = (int)ctx->plane;
+    if (sh.v == 0) {
+        if constexpr (sizeof(S) == 2) {
+            const dim3 sgrid((unsigned)((d.nx + d2q9::stage::W - 1) / d2q9::stage::W), (unsigned)((d.ny + sh.ty - 1) / sh.ty));
+            if (force)
+                stage_kernel<S, true><<<sgrid, d2q9::stage::THREADS, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, sh.ty, reverse);
+            else
+                stage_kernel<S, false><<<sgrid, d2q9::stage::THREADS, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, sh.ty, reverse);
+            return cudaGetLastError();
+        }
+        return cudaErrorInvalidValue;
+    }
 #define LBM_VEC_LAUNCH(VV, PP)                                                                                  \
     if (force) step_vec_kernel<S, VV, true, PP><<<grid, block, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, reverse); \
     else step_vec_kernel<S, VV, false, PP><<<grid, block, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, reverse);
@@ -313,6 +340,8 @@ template <class S>
 std::vector<Shape> candidates(const lbm_ctx *ctx) {
     std::vector<Shape> c = {{1, 256, 1, 0}, {1, 128, 2, 0}};
     if (!small_index(ctx)) return c;
+    if (sizeof(S) == 2)  // the shared-memory row sweep, runs of 8 .. 64 rows per block
+        for (int rows : {8, 16, 32, 64}) c.push_back({0, d2q9::stage::THREADS, rows, 0});
     for (int v : {2, 4, 8}) {
         if (!vec_ok<S>(v) || ctx->pitch % v) continue;
         const int per_row = (int)(ctx->pitch / v);
@@ -369,7 +398,7 @@ void load_tune_file() {
         if (end == std::string::npos) break;
         const std::string key = txt.substr(pos + 1, end - pos - 1);
         Shape sh{0, 0, 0, 0};
-        if (std::sscanf(txt.c_str() + end + 1, " : [ %d , %d , %d , %d ]", &sh.v, &sh.tx, &sh.ty, &sh.pol) == 4 && sh.v > 0 &&
+        if (std::sscanf(txt.c_str() + end + 1, " : [ %d , %d , %d , %d ]", &sh.v, &sh.tx, &sh.ty, &sh.pol) == 4 && sh.v >= 0 &&
             sh.tx > 0 && sh.ty > 0)
             g_tune_cache[key] = sh;
         pos = end + 1;
@@ -504,6 +533,9 @@ cudaError_t d2q9_init_equilibrium(lbm_ctx *ctx, const float *rho_d, const float 
 }
 
 bool d2q9_shape_valid(const lbm_ctx *ctx, int v, int tx, int ty, int pol) {
+    if (v == 0)  // shared-memory row sweep: 16-bit storage, fixed block width, 1 .. 1024 rows per block
+        return (ctx->desc.dtype == LBM_F16S || ctx->desc.dtype == LBM_BF16S) && tx == d2q9::stage::THREADS && ty >= 1 &&
+               ty <= 1024 && pol == 0 && small_index(ctx);
     if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256 || pol < 0 || pol > 2) return false;
     if (v == 1) return pol == 0;
     if (!small_index(ctx) || ctx->pitch % v) return false;

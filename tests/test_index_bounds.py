@@ -93,3 +93,79 @@ def test_replay_catches_an_unclamped_left_neighbour():
     x0 = np.array([(3 * 32) * V])  # lane 0 of the fourth warp, beyond the 160-wide row
     bad = 8 * plane + (ny - 1) * pitch + (x0 - 1)
     assert bad.max() >= 9 * plane
+
+
+# ------------------------------------------------------------------ shared-memory row sweep
+# csrc/d2q9_stage.cuh: THREADS = 128 threads, strips of W = 256 cells, slot rows of SEG = W + 16
+# elements, NSLOT = 8 slots, 16-byte (8-element) chunks.
+THREADS, W, SEG, NSLOT = 128, 256, 272, 8
+
+
+def stage_offsets(nx, ny, rows, periodic):
+    """Every global element offset and shared-memory index the row sweep touches, over all blocks."""
+    pitch = (nx + 31) // 32 * 32
+    plane = pitch * ny
+    gread, gwrite, lread, smem = [], [], [], []
+    nbx, nby = (nx + W - 1) // W, (ny + rows - 1) // rows
+    t = np.arange(THREADS)
+    for bx in range(nbx):
+        x0 = bx * W
+        for by in range(nby):
+            ya = by * rows
+            yb = min(ya + rows, ny)
+            # copies: positions 0 .. nrows+1, rows ya-1 .. yb, chunk i of 9 * SEG / 8
+            for p in range(yb - ya + 2):
+                row = ya - 1 + p
+                valid = True
+                if row < 0 or row >= ny:
+                    if periodic & 2:
+                        row = row + ny if row < 0 else row - ny
+                    else:
+                        valid = False
+                i = np.arange(9 * SEG // 8)
+                q, j = i // (SEG // 8), i % (SEG // 8)
+                gx = x0 - 8 + 8 * j
+                ok = valid & (gx >= 0) & (gx + 8 <= pitch)
+                src = q * plane + row * pitch + gx
+                gread.append(np.concatenate([src[ok], src[ok] + 7]))  # the 8 elements of a chunk
+                slot = p % NSLOT
+                smem.append(np.concatenate([slot * 9 * SEG + q * SEG + 8 * j, slot * 9 * SEG + q * SEG + 8 * j + 7]))
+            # compute: threads whose first cell is inside the row
+            xa = x0 + 2 * t
+            act = xa < nx
+            for y in range(ya, yb):
+                c = y * pitch + xa[act]
+                lread.append(np.concatenate([c, c + 1]))  # the 4-byte link load
+                for q in range(9):
+                    gwrite.append(np.concatenate([q * plane + c, q * plane + c + 1]))
+                lx = 2 * t[act] + 8
+                smem.append(np.concatenate([lx - 1, lx + 2]))  # neighbours of the two cells
+                if periodic & 1:
+                    ym = y - 1 if y > 0 else (ny - 1 if periodic & 2 else 0)
+                    yp = y + 1 if y < ny - 1 else (0 if periodic & 2 else ny - 1)
+                    for xc in (xa[act], xa[act] + 1):
+                        for q, r in ((1, y), (5, ym), (8, yp)):
+                            m = xc == 0
+                            gread.append(q * plane + r * pitch + np.where(m, nx - 1, 0)[m])
+                        for q, r in ((3, y), (6, ym), (7, yp)):
+                            m = xc == nx - 1
+                            gread.append(q * plane + r * pitch + np.zeros_like(xc)[m])
+    cat = lambda a: np.concatenate(a) if a else np.zeros(0, int)
+    return cat(gread), cat(gwrite), cat(lread), cat(smem), plane
+
+
+@pytest.mark.parametrize("nx,ny", SIZES + [(256, 5), (257, 40), (511, 33)])
+def test_row_sweep_addresses_stay_in_buffers(nx, ny):
+    for rows, periodic in itertools.product((1, 8, 32, 64), range(4)):
+        gread, gwrite, lread, smem, plane = stage_offsets(nx, ny, rows, periodic)
+        for a, hi in ((gread, 9 * plane), (gwrite, 9 * plane), (lread, plane), (smem, NSLOT * 9 * SEG)):
+            if a.size:
+                assert a.min() >= 0 and a.max() < hi, (nx, ny, rows, periodic, a.min(), a.max(), hi)
+
+
+def test_row_sweep_slot_reuse_never_overwrites_a_live_row():
+    """Iteration k reads positions k, k+1, k+2 and refills the slot of position k + NSLOT - 1,
+    which is the slot of position k - 1: no slot is refilled while a live row sits in it."""
+    for k in range(200):
+        live = {(k + d) % NSLOT for d in range(3)}
+        assert (k + NSLOT - 1) % NSLOT not in live
