@@ -199,9 +199,9 @@ LBM_API lbm_status lbm_step_force_series(lbm_ctx *ctx, int32_t nsteps, float *ho
  * 32; block_threads * rows_per_block <= 256) and the L2 eviction hints of the vectorised path
  * (l2_policy 0: none; 1: loads evict-first, stores evict-last; 2: loads evict-first; the scalar
  * path, cells_per_thread 1, takes 0 only).  cells_per_thread 0 selects the shared-memory row
- * sweep of FP16/BF16 storage: blocks of block_threads = 128 threads each sweep a strip of 256
+ * sweep of FP16/BF16 storage: blocks of block_threads = 128 threads each sweep a strip of 512
  * cells over rows_per_block rows (1 .. 1024), staging source rows through shared memory with
- * asynchronous copies; l2_policy 0. */
+ * asynchronous copies; for it l2_policy selects the ring depth (0: 4 rows, 1: 8 rows). */
 LBM_API lbm_status lbm_autotune(lbm_ctx *ctx, int32_t retune);
 LBM_API lbm_status lbm_set_launch(lbm_ctx *ctx, int32_t cells_per_thread, int32_t block_threads,
                                   int32_t rows_per_block, int32_t l2_policy);

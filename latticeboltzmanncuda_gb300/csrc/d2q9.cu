@@ -122,17 +122,33 @@ __global__ void __launch_bounds__(256) step_vec_kernel(const S *__restrict__ src
 
 // 16-bit storage: block (bx, by) sweeps strip bx (cells bx*W .. bx*W+W-1) over rows
 // [by*rows, by*rows + rows); with `reverse` the blocks take the strips and row runs in reverse order.
-template <class S, bool FORCE>
+template <class S, bool FORCE, int NSLOT>
 __global__ void __launch_bounds__(d2q9::stage::THREADS) stage_kernel(const S *__restrict__ src, S *__restrict__ dst,
                                                                     const uint16_t *__restrict__ links, int nx, int ny,
                                                                     int pitch, int plane, int periodic, D2Q9Params prm,
                                                                     int rows, int reverse) {
-    __shared__ d2q9::stage::Ring<S> ring;
+    extern __shared__ __align__(16) uint16_t ring[];
     const int bx = reverse ? (int)(gridDim.x - 1 - blockIdx.x) : (int)blockIdx.x;
     const int by = reverse ? (int)(gridDim.y - 1 - blockIdx.y) : (int)blockIdx.y;
     const int ya = by * rows;
-    d2q9::stage::sweep<S, FORCE>(ring, src, dst, links, bx * d2q9::stage::W, ya, min(ya + rows, ny), nx, ny, pitch,
-                                 plane, periodic, prm);
+    d2q9::stage::sweep<S, FORCE, NSLOT>(ring, src, dst, links, bx * d2q9::stage::W, ya, min(ya + rows, ny), nx, ny,
+                                        pitch, plane, periodic, prm);
+}
+
+// launch the row sweep with a ring of NSLOT slots (dynamic shared memory beyond 48 KB is opted in
+// on the current device before the launch)
+template <class S, bool FORCE, int NSLOT>
+cudaError_t launch_stage(dim3 grid, cudaStream_t st, const S *src, S *dst, const uint16_t *links, int nx, int ny,
+                         int pitch, int plane, int periodic, const D2Q9Params &prm, int rows, int reverse) {
+    constexpr size_t bytes = d2q9::stage::ring_bytes<NSLOT>();
+    if (bytes > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(stage_kernel<S, FORCE, NSLOT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)bytes);
+        if (e != cudaSuccess) return e;
+    }
+    stage_kernel<S, FORCE, NSLOT><<<grid, d2q9::stage::THREADS, bytes, st>>>(src, dst, links, nx, ny, pitch, plane,
+                                                                               periodic, prm, rows, reverse);
+    return cudaGetLastError();
 }
 
 template <class S>
@@ -305,14 +321,15 @@ cudaError_t launch_one(lbm_ctx *ctx, const Shape &sh, const S *src, S *dst, int 
         return cudaGetLastError();
     }
     const int pitch = (int)ctx->pitch, plane = (int)ctx->plane;
-    if (sh.v == 0) {
+    if (sh.v == 0) {  // row sweep; pol selects the ring depth: 0 -> 4 slots, 1 -> 8 slots
         if constexpr (sizeof(S) == 2) {
             const dim3 sgrid((unsigned)((d.nx + d2q9::stage::W - 1) / d2q9::stage::W), (unsigned)((d.ny + sh.ty - 1) / sh.ty));
-            if (force)
-                stage_kernel<S, true><<<sgrid, d2q9::stage::THREADS, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, sh.ty, reverse);
-            else
-                stage_kernel<S, false><<<sgrid, d2q9::stage::THREADS, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, sh.ty, reverse);
-            return cudaGetLastError();
+            const uint16_t *L = ctx->links_d;
+            if (sh.pol == 1)
+                return force ? launch_stage<S, true, 8>(sgrid, st, src, dst, L, d.nx, d.ny, pitch, plane, d.periodic, prm, sh.ty, reverse)
+                             : launch_stage<S, false, 8>(sgrid, st, src, dst, L, d.nx, d.ny, pitch, plane, d.periodic, prm, sh.ty, reverse);
+            return force ? launch_stage<S, true, 4>(sgrid, st, src, dst, L, d.nx, d.ny, pitch, plane, d.periodic, prm, sh.ty, reverse)
+                         : launch_stage<S, false, 4>(sgrid, st, src, dst, L, d.nx, d.ny, pitch, plane, d.periodic, prm, sh.ty, reverse);
         }
         return cudaErrorInvalidValue;
     }
@@ -340,8 +357,9 @@ template <class S>
 std::vector<Shape> candidates(const lbm_ctx *ctx) {
     std::vector<Shape> c = {{1, 256, 1, 0}, {1, 128, 2, 0}};
     if (!small_index(ctx)) return c;
-    if (sizeof(S) == 2)  // the shared-memory row sweep, runs of 8 .. 64 rows per block
-        for (int rows : {8, 16, 32, 64}) c.push_back({0, d2q9::stage::THREADS, rows, 0});
+    if (sizeof(S) == 2)  // the shared-memory row sweep: runs of 8 .. 64 rows per block, rings of 4 or 8 slots
+        for (int rows : {8, 16, 32, 64})
+            for (int ring = 0; ring < 2; ++ring) c.push_back({0, d2q9::stage::THREADS, rows, ring});
     for (int v : {2, 4, 8}) {
         if (!vec_ok<S>(v) || ctx->pitch % v) continue;
         const int per_row = (int)(ctx->pitch / v);
@@ -533,9 +551,9 @@ cudaError_t d2q9_init_equilibrium(lbm_ctx *ctx, const float *rho_d, const float 
 }
 
 bool d2q9_shape_valid(const lbm_ctx *ctx, int v, int tx, int ty, int pol) {
-    if (v == 0)  // shared-memory row sweep: 16-bit storage, fixed block width, 1 .. 1024 rows per block
+    if (v == 0)  // shared-memory row sweep: 16-bit storage, fixed block width, 1 .. 1024 rows per block, ring 0/1
         return (ctx->desc.dtype == LBM_F16S || ctx->desc.dtype == LBM_BF16S) && tx == d2q9::stage::THREADS && ty >= 1 &&
-               ty <= 1024 && pol == 0 && small_index(ctx);
+               ty <= 1024 && (pol == 0 || pol == 1) && small_index(ctx);
     if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256 || pol < 0 || pol > 2) return false;
     if (v == 1) return pol == 0;
     if (!small_index(ctx) || ctx->pitch % v) return false;

@@ -96,16 +96,20 @@ def test_replay_catches_an_unclamped_left_neighbour():
 
 
 # ------------------------------------------------------------------ shared-memory row sweep
-# csrc/d2q9_stage.cuh: THREADS = 128 threads, strips of W = 256 cells, slot rows of SEG = W + 16
-# elements, NSLOT = 8 slots, 16-byte (8-element) chunks.
-THREADS, W, SEG, NSLOT = 128, 256, 272, 8
+# csrc/d2q9_stage.cuh: 128 threads x 4 cells = strips of W = 512, plane rows of SEG = W + 16
+# elements staged as 16-byte (8-element) chunks, link words after the nine planes of a slot.
+THREADS, CPT = 128, 4
+W = THREADS * CPT
+SEG = W + 16
+CHUNKS, LCHUNKS = SEG // 8, W // 8
+LINKS, SLOT = 9 * SEG, 9 * SEG + W
 
 
-def stage_offsets(nx, ny, rows, periodic):
+def stage_offsets(nx, ny, rows, periodic, nslot):
     """Every global element offset and shared-memory index the row sweep touches, over all blocks."""
     pitch = (nx + 31) // 32 * 32
     plane = pitch * ny
-    gread, gwrite, lread, smem = [], [], [], []
+    gread, lread, gwrite, smem = [], [], [], []
     nbx, nby = (nx + W - 1) // W, (ny + rows - 1) // rows
     t = np.arange(THREADS)
     for bx in range(nbx):
@@ -113,59 +117,65 @@ def stage_offsets(nx, ny, rows, periodic):
         for by in range(nby):
             ya = by * rows
             yb = min(ya + rows, ny)
-            # copies: positions 0 .. nrows+1, rows ya-1 .. yb, chunk i of 9 * SEG / 8
-            for p in range(yb - ya + 2):
+            for p in range(yb - ya + 2):  # copies of rows ya-1 .. yb
                 row = ya - 1 + p
-                valid = True
                 if row < 0 or row >= ny:
-                    if periodic & 2:
-                        row = row + ny if row < 0 else row - ny
-                    else:
-                        valid = False
-                i = np.arange(9 * SEG // 8)
-                q, j = i // (SEG // 8), i % (SEG // 8)
-                gx = x0 - 8 + 8 * j
-                ok = valid & (gx >= 0) & (gx + 8 <= pitch)
-                src = q * plane + row * pitch + gx
-                gread.append(np.concatenate([src[ok], src[ok] + 7]))  # the 8 elements of a chunk
-                slot = p % NSLOT
-                smem.append(np.concatenate([slot * 9 * SEG + q * SEG + 8 * j, slot * 9 * SEG + q * SEG + 8 * j + 7]))
-            # compute: threads whose first cell is inside the row
-            xa = x0 + 2 * t
-            act = xa < nx
-            for y in range(ya, yb):
-                c = y * pitch + xa[act]
-                lread.append(np.concatenate([c, c + 1]))  # the 4-byte link load
+                    if not periodic & 2:
+                        continue
+                    row = row + ny if row < 0 else row - ny
+                base = (p % nslot) * SLOT
+                tp = t[t < CHUNKS]
+                gx = x0 - 8 + 8 * tp
+                ok = (gx >= 0) & (gx + 8 <= pitch)
                 for q in range(9):
-                    gwrite.append(np.concatenate([q * plane + c, q * plane + c + 1]))
-                lx = 2 * t[act] + 8
-                smem.append(np.concatenate([lx - 1, lx + 2]))  # neighbours of the two cells
+                    g = q * plane + row * pitch + gx[ok]
+                    gread += [g, g + 7]
+                    smem += [base + q * SEG + 8 * tp[ok], base + q * SEG + 8 * tp[ok] + 7]
+                lt = t - (THREADS - LCHUNKS)
+                lt = lt[lt >= 0]
+                gl = x0 + 8 * lt
+                okl = gl + 8 <= pitch
+                lread += [row * pitch + gl[okl], row * pitch + gl[okl] + 7]
+                smem += [base + LINKS + 8 * lt[okl], base + LINKS + 8 * lt[okl] + 7]
+            xa = x0 + CPT * t
+            act = xa < nx
+            lx = 8 + CPT * t[act]
+            for k, y in enumerate(range(ya, yb)):
+                c = y * pitch + xa[act]
+                for q in range(9):
+                    gwrite += [q * plane + c, q * plane + c + CPT - 1]  # one 8-byte store
+                for d in range(3):
+                    base = ((k + d) % nslot) * SLOT
+                    smem += [base + 8 * SEG + lx - 1, base + 8 * SEG + lx + CPT]  # reads lx-1 .. lx+4 of a plane
+                    smem += [base + LINKS + CPT * t[act], base + LINKS + CPT * t[act] + CPT - 1]
                 if periodic & 1:
                     ym = y - 1 if y > 0 else (ny - 1 if periodic & 2 else 0)
                     yp = y + 1 if y < ny - 1 else (0 if periodic & 2 else ny - 1)
-                    for xc in (xa[act], xa[act] + 1):
-                        for q, r in ((1, y), (5, ym), (8, yp)):
-                            m = xc == 0
-                            gread.append(q * plane + r * pitch + np.where(m, nx - 1, 0)[m])
-                        for q, r in ((3, y), (6, ym), (7, yp)):
-                            m = xc == nx - 1
-                            gread.append(q * plane + r * pitch + np.zeros_like(xc)[m])
+                    cells = np.concatenate([xa[act] + cc for cc in range(CPT)])
+                    for q, r in ((1, y), (5, ym), (8, yp)):
+                        gread.append(q * plane + r * pitch + np.full(int((cells == 0).sum()), nx - 1))
+                    for q, r in ((3, y), (6, ym), (7, yp)):
+                        gread.append(q * plane + r * pitch + np.zeros(int((cells == nx - 1).sum()), int))
     cat = lambda a: np.concatenate(a) if a else np.zeros(0, int)
-    return cat(gread), cat(gwrite), cat(lread), cat(smem), plane
+    return cat(gread), cat(lread), cat(gwrite), cat(smem), plane
 
 
-@pytest.mark.parametrize("nx,ny", SIZES + [(256, 5), (257, 40), (511, 33)])
+@pytest.mark.parametrize("nx,ny", SIZES + [(512, 5), (513, 40), (1023, 33)])
 def test_row_sweep_addresses_stay_in_buffers(nx, ny):
-    for rows, periodic in itertools.product((1, 8, 32, 64), range(4)):
-        gread, gwrite, lread, smem, plane = stage_offsets(nx, ny, rows, periodic)
-        for a, hi in ((gread, 9 * plane), (gwrite, 9 * plane), (lread, plane), (smem, NSLOT * 9 * SEG)):
+    for rows, periodic, nslot in itertools.product((1, 8, 64), range(4), (4, 8)):
+        gread, lread, gwrite, smem, plane = stage_offsets(nx, ny, rows, periodic, nslot)
+        for a, hi in ((gread, 9 * plane), (lread, plane), (gwrite, 9 * plane), (smem, nslot * SLOT)):
             if a.size:
-                assert a.min() >= 0 and a.max() < hi, (nx, ny, rows, periodic, a.min(), a.max(), hi)
+                assert a.min() >= 0 and a.max() < hi, (nx, ny, rows, periodic, nslot, a.min(), a.max(), hi)
 
 
-def test_row_sweep_slot_reuse_never_overwrites_a_live_row():
-    """Iteration k reads positions k, k+1, k+2 and refills the slot of position k + NSLOT - 1,
-    which is the slot of position k - 1: no slot is refilled while a live row sits in it."""
+@pytest.mark.parametrize("nslot", [4, 8])
+def test_row_sweep_slot_reuse_never_overwrites_a_live_row(nslot):
+    """Iteration k reads positions k, k+1, k+2 and refills the slot of position k + nslot - 1,
+    which is the slot of position k - 1: no slot is refilled while a live row sits in it; and
+    waiting until at most nslot - 4 copy groups are pending leaves positions <= k + 2 landed."""
     for k in range(200):
-        live = {(k + d) % NSLOT for d in range(3)}
-        assert (k + NSLOT - 1) % NSLOT not in live
+        live = {(k + d) % nslot for d in range(3)}
+        assert (k + nslot - 1) % nslot not in live
+        committed = (nslot - 1) + k  # prologue groups + one per earlier iteration
+        assert committed - (nslot - 4) >= k + 3
