@@ -549,44 +549,87 @@ def run_tgv(args):
     return 0
 
 
+def sphere_mesh(level, r, c):
+    """Closed triangle mesh of a sphere: an icosahedron with every face split in four `level`
+    times, vertices pushed onto the sphere of radius r about c."""
+    t = (1 + 5 ** 0.5) / 2
+    v = [np.array(p, float) for p in ((-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t),
+                                      (0, -1, -t), (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1))]
+    v = [p / np.linalg.norm(p) for p in v]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+             (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(level):
+        mids, out = {}, []
+
+        def mid(a, b):
+            k = (min(a, b), max(a, b))
+            if k not in mids:
+                p = v[a] + v[b]
+                v.append(p / np.linalg.norm(p))
+                mids[k] = len(v) - 1
+            return mids[k]
+        for a, b, d in faces:
+            ab, bd, da = mid(a, b), mid(b, d), mid(d, a)
+            out += [(a, ab, da), (b, bd, ab), (d, da, bd), (ab, bd, da)]
+        faces = out
+    return np.array(v) * r + np.asarray(c, float), faces
+
+
 def d3q27_case(n):
     """n^3 lattice in the reference CLI's set-up (LatticeBoltzmannCuda.cpp:53-73): populations 0.001
-    with f6 = 0.002, the same vector injected on the plane x = 0, plus a solid sphere of radius n/6
-    at the centre (internal cells)."""
+    with f6 = 0.002, the same vector injected on the plane x = 0, and a sphere model of radius n/6
+    at the centre turned into internal cells and reflection tables by the mesh front end
+    (Lattice::insertModel + preProcessModel)."""
+    import latticeboltzmanncuda_gb300 as lbm
     cells = n ** 3
     f = np.full((cells, 27), 0.001, np.float32)
     f[:, 6] = 0.002
-    x, y, z = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
-    inside = ((x - n / 2) ** 2 + (y - n / 2) ** 2 + (z - n / 2) ** 2 <= (n / 6) ** 2).ravel()
-    flags = np.where(inside, 1, 0).astype(np.uint8)
-    plane = (x == 0).ravel()
+    spacing = 1.0 / n
+    verts, faces = sphere_mesh(3, 1 / 6, (0.5, 0.5, 0.5))
+    with lbm.Mesh.from_arrays(verts, faces) as m:
+        flags, _ = m.rasterize((n, n, n), spacing)
+        cells_t, recs, flags = m.reflection_tables((n, n, n), spacing, flags)
+    x = np.arange(cells) // (n * n)
+    plane = x == 0
     induced = f[0].copy()
-    return f, flags, plane, induced
+    return f, flags, plane, induced, cells_t, recs
 
 
 def run_d3q27(args):
-    """The reference-compatible D3Q27 step (stream, reflect, collide, flow) on n^3 through the
-    library: MLUPS and the HBM roofline at 216 algorithmic bytes per cell update."""
+    """The reference-compatible D3Q27 step (stream, reflect, collide, flow, with the reflection
+    force accumulated as the reference CLI does) on n^3 through the library: MLUPS and the HBM
+    roofline at 216 algorithmic bytes per cell update, for the float-float equilibrium (default)
+    and for the FP64 expression."""
     import torch
     import latticeboltzmanncuda_gb300 as lbm
 
     n, steps = args.d3_n, args.d3_steps
-    f, flags, plane, induced = d3q27_case(n)
+    f, flags, plane, induced, cells_t, recs = d3q27_case(n)
     cells = n ** 3
     stream = torch.cuda.Stream()
-    with lbm.Lattice(n, n, n, mode="d3q27_ref", tau=0.8, order=lbm.ORDER_CLI, stream=stream.cuda_stream) as L:
-        L.set_flags(flags)
-        L.set_flow(plane, induced)
-        L.load_populations(f)
-        L.step(args.warmup)
-        t = _timed(stream, lambda: L.step(steps))
-    mlups = cells * steps / t / 1e6
+    res = {}
+    for fp64 in (False, True):
+        with lbm.Lattice(n, n, n, mode="d3q27_ref", tau=0.8, order=lbm.ORDER_CLI, stream=stream.cuda_stream) as L:
+            L.set_equilibrium_evaluation(fp64)
+            L.set_flags(flags)
+            L.set_reflection_tables(cells_t, recs)
+            L.set_flow(plane, induced)
+            L.load_populations(f)
+            L.set_force((0, 0, 0), True)
+            L.step(args.warmup)
+            t = _timed(stream, lambda: L.step(steps))
+            res[fp64] = (cells * steps / t / 1e6, L.retrieve_populations())
+    mlups = res[False][0]
     peak, kind = peaks()
     achieved = mlups * 216 / 1000
     line = {"metric": "MLUPS", "workload": "d3q27", "value": round(mlups, 1), "unit": "MLUPS", "steps": steps,
-            "higher_is_better": True, "dtype": "f32 (FP64 equilibrium)", "data": "synthetic",
-            "config": {"workload": f"D3Q27 reference step {n}^3, order stream-reflect-collide-flow, tau 0.8, "
-                                   f"solid sphere r = n/6, source plane x = 0", "cells": cells},
+            "higher_is_better": True, "dtype": "f32 (equilibrium as the reference's FP64 value)", "data": "synthetic",
+            "config": {"workload": f"D3Q27 reference step {n}^3, order stream-reflect-collide-flow with force, tau 0.8, "
+                                   f"sphere model r = n/6 ({len(cells_t)} reflecting cells), source plane x = 0",
+                       "cells": cells},
+            "fp64_equilibrium": {"mlups": round(res[True][0], 1),
+                                 "bitwise_equal": bool(np.array_equal(res[False][1], res[True][1]))},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_kind": kind, "bytes_per_update": 216}}
     print(json.dumps(line), flush=True)
@@ -600,7 +643,7 @@ def run_d3q27_reference(args):
     from oracle import refkern
 
     n, steps = args.d3_n, args.d3_steps
-    f, flags, plane, induced = d3q27_case(n)
+    f, flags, plane, induced, cells_t, recs = d3q27_case(n)
     cells = n ** 3
     line = {"impl": "reference", "metric": "MLUPS", "workload": "d3q27", "unit": "MLUPS", "higher_is_better": True,
             "data": "synthetic", "config": {"workload": f"D3Q27 reference step {n}^3 (as --workload d3q27)"}}
@@ -609,18 +652,25 @@ def run_d3q27_reference(args):
             raise RuntimeError("reference kernels not built")
         pts = np.zeros(cells, refkern.LATTICE_POINT)
         pts["f"] = f
-        pts["isInternal"] = flags != 0
+        pts["isInternal"] = (flags & 1) != 0
+        pts["isReflected"] = (flags & 2) != 0
         tz = min(n, 64)
         shape = (1, max(1, min(n, 512 // tz)), tz)
-        refkern.run((n, n, n), pts, "SRCF", nsteps=1, tau=0.8, flow_criterion=2, induced=induced, threads=shape)
-        refkern.run((n, n, n), pts, "SRCF", nsteps=steps, tau=0.8, flow_criterion=2, induced=induced, threads=shape)
+        kw = dict(tau=0.8, tab_cells=cells_t, tab_records=recs, flow_criterion=2, induced=induced, threads=shape)
+        refkern.run((n, n, n), pts, "SRCF", nsteps=1, **kw)
+        refkern.run((n, n, n), pts, "SRCF", nsteps=steps, **kw)
         line["value"] = round(cells * steps / refkern.last_seconds() / 1e6, 1)
+        # without the force: the reference's force reads DIRECTIONS / SPLIT at slot indices up to 80
+        # (SimCalcFuncs.cu:181-183), past the end of its 27-entry tables, for mesh tables
         line["reference_gpu_kernels"] = {"mlups": line["value"], "seconds": refkern.last_seconds(),
-                                         "block": list(shape)}
+                                         "block": list(shape), "force": False}
     except Exception as e:  # no GPU or no cubin: the CPU port alone
         line["reference_gpu_kernels"] = {"unavailable": str(e)[:200]}
     t0 = time.perf_counter()
-    oracle.d3q27_run((n, n, n), f, flags | np.where(plane, 4, 0).astype(np.uint8), 0.8, 2, order=1, induced=induced)
+    tab_idx = np.full(cells, -1, np.int32)
+    tab_idx[cells_t] = np.arange(len(cells_t), dtype=np.int32)
+    oracle.d3q27_run((n, n, n), f, flags | np.where(plane, 4, 0).astype(np.uint8), 0.8, 2, order=1, tab_idx=tab_idx,
+                     tabs=recs, induced=induced)
     cpu = cells * 2 / (time.perf_counter() - t0) / 1e6
     line["cpu_baseline"] = {"value": round(cpu, 2), "unit": "MLUPS", "cores": oracle.num_threads(), "kind": "port",
                             "sample": f"{n}^3, 2 steps"}

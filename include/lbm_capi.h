@@ -180,6 +180,18 @@ LBM_API int32_t lbm_force_accumulation(const lbm_ctx *ctx);
 LBM_API lbm_status lbm_step(lbm_ctx *ctx, int32_t nsteps);
 /* D3Q27_REF: one separate pass (LBM_OP_*), as the reference's Lattice::simulate* methods. */
 LBM_API lbm_status lbm_apply(lbm_ctx *ctx, int32_t op);
+/* D3Q27_REF equilibrium evaluation.  The reference evaluates eq_i in FP64 and rounds it to FP32
+ * (SimCalcFuncs.cu:122-155).  Both modes give that value bit for bit:
+ *   LBM_EQ_FLOAT_FLOAT (default)  float-float arithmetic with a proven error bound, falling back to
+ *                                 the FP64 expression when the bound cannot decide the FP32 rounding
+ *   LBM_EQ_FP64                   the FP64 expression for every direction (GB300's FP64 rate bounds
+ *                                 the step) */
+enum { LBM_EQ_FLOAT_FLOAT = 0, LBM_EQ_FP64 = 1 };
+LBM_API lbm_status lbm_set_equilibrium_evaluation(lbm_ctx *ctx, int32_t mode);
+/* Diagnostic: both evaluations on `samples` pseudo-random (rho, u) draws x 27 directions on
+ * `device`; out[0] = float-float results accepted by the bound that differ from FP64 (must be 0),
+ * out[1] = evaluations settled by the FP64 fallback. */
+LBM_API lbm_status lbm_d3q27_equilibrium_selftest(int64_t samples, uint64_t seed, int32_t device, int64_t out[2]);
 /* D3Q27_REF: the step order of later lbm_step() calls (LBM_ORDER_*), e.g. the stream-collide of
  * Lattice::simulateLattice and the CLI loop on one lattice. */
 LBM_API lbm_status lbm_set_order(lbm_ctx *ctx, int32_t order);

@@ -176,6 +176,10 @@ class Lattice:
     def apply(self, op):
         self._call("lbm_apply", int(op))
 
+    def set_equilibrium_evaluation(self, fp64):
+        """D3Q27_REF: False = float-float with FP64 fallback (default), True = FP64 throughout."""
+        self._call("lbm_set_equilibrium_evaluation", 1 if fp64 else 0)
+
     def set_order(self, order):
         """D3Q27_REF: step order of later step() calls (ORDER_STREAM_COLLIDE or ORDER_CLI)."""
         self._call("lbm_set_order", int(order))

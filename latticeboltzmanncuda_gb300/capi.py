@@ -20,6 +20,7 @@ F32, F16S, BF16S, F64 = 0, 1, 2, 3
 FLUID, WALL, MOVING_WALL = 0, 1, 2
 INTERNAL, REFLECTED, SOURCE = 1, 2, 4
 ORDER_STREAM_COLLIDE, ORDER_CLI = 0, 1
+EQ_FLOAT_FLOAT, EQ_FP64 = 0, 1
 OP_STREAM, OP_REFLECT, OP_COLLIDE, OP_FLOW = 1, 2, 4, 8
 FORCE_REFERENCE, FORCE_MOMENTUM_EXCHANGE = 0, 1
 
@@ -117,6 +118,8 @@ SIGNATURES = [
     ("lbm_step", _S, [_P, _I32]),
     ("lbm_apply", _S, [_P, _I32]),
     ("lbm_set_order", _S, [_P, _I32]),
+    ("lbm_set_equilibrium_evaluation", _S, [_P, _I32]),
+    ("lbm_d3q27_equilibrium_selftest", _S, [_I64, _U64, _I32, _P]),
     ("lbm_set_force_accumulation", _S, [_P, _I32]),
     ("lbm_force_accumulation", _I32, [_P]),
     ("lbm_step_force_series", _S, [_P, _I32, _P]),

@@ -596,6 +596,31 @@ LBM_API lbm_status lbm_step_force_series(lbm_ctx *ctx, int32_t nsteps, float *ho
     return LBM_OK;
 }
 
+LBM_API lbm_status lbm_set_equilibrium_evaluation(lbm_ctx *ctx, int32_t mode) {
+    CHECK_CTX(ctx);
+    if (ctx->desc.mode != LBM_D3Q27_REF) return fail(ctx, LBM_ERR_UNSUPPORTED, "equilibrium evaluation is D3Q27_REF only");
+    if (mode != LBM_EQ_FLOAT_FLOAT && mode != LBM_EQ_FP64) return fail(ctx, LBM_ERR_INVALID, "unknown equilibrium evaluation");
+    ctx->eq_fp64 = mode == LBM_EQ_FP64;
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_d3q27_equilibrium_selftest(int64_t samples, uint64_t seed, int32_t device, int64_t out[2]) {
+    if (samples < 0 || !out) return set_thread_error(LBM_ERR_INVALID, "lbm_d3q27_equilibrium_selftest: bad argument");
+    cudaError_t e = cudaSetDevice(device);
+    unsigned long long *d = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(&d, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = d3q27_eq_selftest(samples, seed, d, nullptr);
+    unsigned long long h[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess)
+        return set_thread_error(LBM_ERR_CUDA, std::string("lbm_d3q27_equilibrium_selftest: ") + cudaGetErrorString(e));
+    out[0] = (int64_t)h[0];
+    out[1] = (int64_t)h[1];
+    return LBM_OK;
+}
+
 LBM_API lbm_status lbm_set_order(lbm_ctx *ctx, int32_t order) {
     CHECK_CTX(ctx);
     if (ctx->desc.mode != LBM_D3Q27_REF) return fail(ctx, LBM_ERR_UNSUPPORTED, "step orders are D3Q27_REF only");

@@ -63,8 +63,74 @@ __device__ __forceinline__ void pull(const float *__restrict__ src, const Dims &
     }
 }
 
+// ------------------------------------------------------------------------- equilibrium
+// The reference evaluates eq_i = W_i * rho * (1 + 3 ct + 4.5 ct^2 - 1.5 usq) in FP64 from FP32 ct,
+// usq and rho, and rounds it to FP32 (SimCalcFuncs.cu:122-155).  3 ct, 4.5 ct * ct and 1.5 usq
+// are exact in FP64, so that value is E = fl64(fl64(W rho) * fl64(fl64(fl64(1 + A) + B) - C)),
+// whichever way the compiler contracts the expression.  GB300 runs FP64 at a small fraction of its
+// FP32 rate, which made the FP64 pipe the bound of this step.  eq_fast() evaluates E in float-float
+// arithmetic (error-free two-sum / FMA two-product transformations, Dekker 1971, Knuth TAOCP 4.2.2)
+// to within 2^-42 * |W rho| * (1 + |A| + B + C) of the FP64 value, rounds it to FP32, and accepts
+// the result only when that error bound keeps the FP64 value strictly inside the same FP32 rounding
+// interval; otherwise (about one evaluation in 10^5) it evaluates the FP64 expression itself.
+// Either way the result is the reference's FP64-evaluated equilibrium, bit for bit.
+// the four weights (SimCalcFuncs.cu:126,135,144,153) in FP64, and split into FP32 hi + lo
+__host__ __device__ constexpr double kW(int k) {
+    return k == 0 ? 8.0 / 27.0 : (k == 1 ? 2.0 / 27.0 : (k == 2 ? 1.0 / 54.0 : 1.0 / 216.0));
+}
+__host__ __device__ constexpr float kWhi(int k) { return (float)kW(k); }
+__host__ __device__ constexpr float kWlo(int k) { return (float)(kW(k) - (double)(float)kW(k)); }
+__host__ __device__ constexpr int wclass(int i) { return i == 0 ? 0 : (i < 7 ? 1 : (i < 19 ? 2 : 3)); }
+
+// s + e == a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bv = __fsub_rn(s, a);
+    const float av = __fsub_rn(s, bv);
+    e = __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
+}
+
+// the reference's expression, FP64 (the fallback and the LBM_EQ_FP64 path)
+__device__ __forceinline__ float eq_fp64(int k, float density, float ct, float usq) {
+    return (float)(kW(k) * density * (1 + (3.0 * ct) + (4.5 * ct * ct) - (1.5 * usq)));
+}
+
+// ph + pl: W_k * rho within 2^-47; c1 + c1e == 1.5 usq exactly.  Returns the FP32 rounding of the
+// float-float value; ok says whether it is proven equal to the FP64 evaluation.
+__device__ __forceinline__ float eq_ff(float ph, float pl, float c1, float c1e, float ct, bool &ok) {
+    const float a = __fmul_rn(3.0f, ct), ae = __fmaf_rn(3.0f, ct, -a);      // A = 3 ct
+    const float p = __fmul_rn(ct, ct), pe = __fmaf_rn(ct, ct, -p);         // ct^2
+    const float b = __fmul_rn(4.5f, p), be = __fmaf_rn(4.5f, p, -b);       // B = 4.5 ct^2 = b + be + 4.5 pe
+    float s1, e1, s2, e2, th, e3;
+    two_sum(a, b, s1, e1);
+    two_sum(s1, -c1, s2, e2);
+    const float lo = __fadd_rn(__fadd_rn(__fsub_rn(__fadd_rn(__fadd_rn(ae, be), __fmul_rn(4.5f, pe)), c1e), e1), e2);
+    two_sum(1.0f, s2, th, e3);
+    const float tl = __fadd_rn(e3, lo);                                   // T = th + tl
+    const float eh = __fmul_rn(ph, th);
+    const float el = __fmaf_rn(ph, tl, __fmaf_rn(pl, th, __fmaf_rn(ph, th, -eh)));
+    const float r = __fadd_rn(eh, el);
+    const float d = __fadd_rn(__fsub_rn(eh, r), el);                      // (eh + el) - r
+    const float m = __fmul_rn(__fmul_rn(fabsf(ph), __fadd_rn(__fadd_rn(__fadd_rn(1.0f, fabsf(a)), b), c1)), 0x1p-42f);
+    const uint32_t rb = __float_as_uint(r) & 0x7fffffffu;
+    const uint32_t ex = rb & 0x7f800000u;
+    // half the smaller gap next to r (2^e * 2^-24, or 2^-25 at a power of two)
+    const float half_gap = __fmul_rn(__uint_as_float(ex), (rb & 0x7fffffu) ? 0x1p-24f : 0x1p-25f);
+    ok = ex >= (67u << 23) && ex < 0x7f800000u && __fadd_rn(fabsf(d), m) < half_gap;
+    return r;
+}
+
+__device__ __forceinline__ float eq_fast(int k, float ph, float pl, float c1, float c1e, float density, float ct,
+                                         float usq) {
+    bool ok;
+    const float r = eq_ff(ph, pl, c1, c1e, ct, ok);
+    return ok ? r : eq_fp64(k, density, ct, usq);
+}
+
 // calculate_collision (SimCalcFuncs.cu:98-156): FP32 density and SPLIT-weighted velocity, FP64
-// equilibrium rounded to FP32, f += (eq - f) / tau in FP32.
+// equilibrium rounded to FP32 (eq_fast, or the FP64 expression itself when EQ64), f += (eq - f) /
+// tau in FP32.
+template <bool EQ64>
 __device__ __forceinline__ void collide(float v[27], float tau) {
     float density = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
 #pragma unroll
@@ -80,11 +146,21 @@ __device__ __forceinline__ void collide(float v[27], float tau) {
         uz /= density;
     }
     const float usq = (ux * ux) + (uy * uy) + (uz * uz);
+    float ph[4], pl[4];
+    const float c1 = __fmul_rn(1.5f, usq), c1e = __fmaf_rn(1.5f, usq, -c1);
+    if (!EQ64) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            ph[k] = __fmul_rn(kWhi(k), density);
+            pl[k] = __fmaf_rn(kWlo(k), density, __fmaf_rn(kWhi(k), density, -ph[k]));
+        }
+    }
 #pragma unroll
     for (int i = 0; i < 27; ++i) {
-        const double wgt = i == 0 ? (8.0 / 27.0) : (i < 7 ? (2.0 / 27.0) : (i < 19 ? (1.0 / 54.0) : (1.0 / 216.0)));
-        const float ct = ((float)c_dir[i][0] * ux) + ((float)c_dir[i][1] * uy) + ((float)c_dir[i][2] * uz);
-        const float eq = (float)(wgt * density * (1 + (3.0 * ct) + (4.5 * ct * ct) - (1.5 * usq)));
+        // c_i . u: the products by -1, 0, 1 are exact, so the two rounded adds fix the value
+        const float ct = __fadd_rn(__fadd_rn((float)c_dir[i][0] * ux, (float)c_dir[i][1] * uy), (float)c_dir[i][2] * uz);
+        const int k = wclass(i);
+        const float eq = EQ64 ? eq_fp64(k, density, ct, usq) : eq_fast(k, ph[k], pl[k], c1, c1e, density, ct, usq);
         v[i] = v[i] + (eq - v[i]) / tau;
     }
 }
@@ -99,6 +175,7 @@ struct StepArgs {
     int cli;               // 1: stream, reflect, collide, flow; 0: stream, collide
 };
 
+template <bool EQ64>
 __global__ void __launch_bounds__(256) fused_kernel(StepArgs a) {
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= a.d.n) return;
@@ -112,7 +189,7 @@ __global__ void __launch_bounds__(256) fused_kernel(StepArgs a) {
 #pragma unroll
         for (int j = 0; j < 27; ++j) v[j] = 0.0f;
     }
-    collide(v, a.tau);
+    collide<EQ64>(v, a.tau);
     if (a.cli && a.induced && (fl & F_SOURCE)) {
 #pragma unroll
         for (int j = 0; j < 27; ++j) v[j] = v[j] + __ldg(a.induced + j);
@@ -143,7 +220,7 @@ __device__ __forceinline__ void force_term(float m, const GatherEntry &e, int mo
 
 // mode 0: fused step (values of the reflecting cells are their streamed populations);
 // mode 1: the reference's separate reflection pass (values read in place, no collision).
-template <int MODE>
+template <int MODE, bool EQ64>
 __global__ void __launch_bounds__(128) gather_kernel(StepArgs a, GatherArgs g) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     double facc[3] = {0.0, 0.0, 0.0};
@@ -176,7 +253,7 @@ __global__ void __launch_bounds__(128) gather_kernel(StepArgs a, GatherArgs g) {
             for (int j = 0; j < 27; ++j) v[j] = 0.0f;
         }
         if (MODE == 0) {
-            collide(v, a.tau);
+            collide<EQ64>(v, a.tau);
             if (a.induced && (fl & F_SOURCE)) {
 #pragma unroll
                 for (int j = 0; j < 27; ++j) v[j] = v[j] + __ldg(a.induced + j);
@@ -212,13 +289,14 @@ __global__ void reflect_copy_kernel(const float *__restrict__ src, float *__rest
     for (int j = 0; j < 27; ++j) dst[(int64_t)j * d.n + c] = zero ? 0.0f : __ldg(src + (int64_t)j * d.n + c);
 }
 
+template <bool EQ64>
 __global__ void collide_kernel(float *__restrict__ f, Dims d, float tau) {
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= d.n) return;
     float v[27];
 #pragma unroll
     for (int j = 0; j < 27; ++j) v[j] = f[(int64_t)j * d.n + c];
-    collide(v, tau);
+    collide<EQ64>(v, tau);
 #pragma unroll
     for (int j = 0; j < 27; ++j) f[(int64_t)j * d.n + c] = v[j];
 }
@@ -340,16 +418,62 @@ cudaError_t launch_gather(lbm_ctx *ctx, const StepArgs &a, int mode, double *for
     GatherArgs g = gather_args(ctx);
     const int threads = 128;
     const unsigned nb = blocks_for(ctx->ntgt, threads);
-    if (mode == 0)
-        gather_kernel<0><<<nb, threads, 0, ctx->stream>>>(a, g);
+    if (mode == 0 && ctx->eq_fp64)
+        gather_kernel<0, true><<<nb, threads, 0, ctx->stream>>>(a, g);
+    else if (mode == 0)
+        gather_kernel<0, false><<<nb, threads, 0, ctx->stream>>>(a, g);
     else
-        gather_kernel<1><<<nb, threads, 0, ctx->stream>>>(a, g);
+        gather_kernel<1, false><<<nb, threads, 0, ctx->stream>>>(a, g);  // no collision in mode 1
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !g.partials) return e;
     return finalize_sums(ctx->stream, g.partials, (int)nb, 3, ctx->force_acc_d, true, force_copy);
 }
 
+// Both equilibrium evaluations on n pseudo-random (rho, u) samples, all 27 directions: counts the
+// results that differ (out[0]) and the evaluations eq_fast settled by its FP64 fallback (out[1]).
+__global__ void eq_selftest_kernel(int64_t n, uint64_t seed, unsigned long long *out) {
+    unsigned long long bad = 0, fell = 0;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+        // SplitMix64 stream per sample; magnitudes spread over decades, velocities up to |u| ~ 2
+        uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(s + 1);
+        float r[5];
+        for (int k = 0; k < 5; ++k) {
+            z += 0x9E3779B97F4A7C15ull;
+            uint64_t t = z;
+            t = (t ^ (t >> 30)) * 0xBF58476D1CE4E5B9ull;
+            t = (t ^ (t >> 27)) * 0x94D049BB133111EBull;
+            t ^= t >> 31;
+            r[k] = (float)(t >> 40) * 0x1p-24f;  // [0, 1)
+        }
+        const float scale = exp2f(floorf(r[4] * 16.0f) - 8.0f);
+        const float rho = (0.01f + 2.0f * r[0]) * scale;
+        const float umax = (s & 3) == 0 ? 2.0f : ((s & 3) == 1 ? 0.3f : ((s & 3) == 2 ? 0.05f : 1e-3f));
+        const float ux = (2.0f * r[1] - 1.0f) * umax, uy = (2.0f * r[2] - 1.0f) * umax;
+        const float uz = (2.0f * r[3] - 1.0f) * umax * ((s & 4) ? 1.0f : 0.0f);
+        const float usq = (ux * ux) + (uy * uy) + (uz * uz);
+        const float c1 = __fmul_rn(1.5f, usq), c1e = __fmaf_rn(1.5f, usq, -c1);
+        for (int i = 0; i < 27; ++i) {
+            const int k = wclass(i);
+            const float ph = __fmul_rn(kWhi(k), rho);
+            const float pl = __fmaf_rn(kWlo(k), rho, __fmaf_rn(kWhi(k), rho, -ph));
+            const float ct = __fadd_rn(__fadd_rn((float)c_dir[i][0] * ux, (float)c_dir[i][1] * uy), (float)c_dir[i][2] * uz);
+            bool ok;
+            const float a = eq_ff(ph, pl, c1, c1e, ct, ok);
+            const float b = eq_fp64(k, rho, ct, usq);
+            bad += ok && __float_as_uint(a) != __float_as_uint(b);
+            fell += !ok;
+        }
+    }
+    atomicAdd(out, bad);
+    atomicAdd(out + 1, fell);
+}
+
 }  // namespace
+
+cudaError_t d3q27_eq_selftest(int64_t n, uint64_t seed, unsigned long long *out_d, cudaStream_t st) {
+    eq_selftest_kernel<<<1216, 256, 0, st>>>(n, seed, out_d);
+    return cudaGetLastError();
+}
 
 cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps, double *series_d) {
     const int threads = 256;
@@ -362,7 +486,10 @@ cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps, double *series_d) {
         a.tau = ctx->desc.tau;
         a.cli = ctx->desc.order == LBM_ORDER_CLI;
         a.induced = (a.cli && ctx->flow_on) ? ctx->induced_d : nullptr;
-        fused_kernel<<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
+        if (ctx->eq_fp64)
+            fused_kernel<true><<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
+        else
+            fused_kernel<false><<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         double *copy = series_d ? series_d + 3 * (int64_t)s : nullptr;
@@ -408,7 +535,10 @@ cudaError_t d3q27_apply(lbm_ctx *ctx, int op) {
             break;
         }
         case LBM_OP_COLLIDE:
-            collide_kernel<<<nb, threads, 0, ctx->stream>>>(cur(ctx), d, ctx->desc.tau);
+            if (ctx->eq_fp64)
+                collide_kernel<true><<<nb, threads, 0, ctx->stream>>>(cur(ctx), d, ctx->desc.tau);
+            else
+                collide_kernel<false><<<nb, threads, 0, ctx->stream>>>(cur(ctx), d, ctx->desc.tau);
             e = cudaGetLastError();
             break;
         case LBM_OP_FLOW:

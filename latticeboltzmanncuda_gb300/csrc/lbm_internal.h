@@ -105,6 +105,7 @@ struct lbm_ctx {
     std::vector<uint8_t> flags_h;    // D3Q27_REF: host copy of the user flag bits
     std::vector<std::pair<int32_t, lbm::ReflRecord>> tables_h;
     bool d3_dirty = true;            // gather lists / device flags need a rebuild
+    bool eq_fp64 = false;            // D3Q27_REF: evaluate the equilibrium in FP64 throughout
 
     lbm::Scratch scratch;
     double *result_d = nullptr;      // small device result buffer (16 doubles)
@@ -150,6 +151,7 @@ cudaError_t d2q9_store(lbm_ctx *ctx, void *dst_d, int dst_dtype, int aos);
 // D3Q27_REF launchers (d3q27.cu)
 // series_d (optional): the accumulated force after step s is written to series_d[3s..3s+2]
 cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps, double *series_d = nullptr);
+cudaError_t d3q27_eq_selftest(int64_t n, uint64_t seed, unsigned long long *out_d, cudaStream_t st);
 cudaError_t d3q27_apply(lbm_ctx *ctx, int op);
 cudaError_t d3q27_moments(lbm_ctx *ctx, float *rho_d, float *ux_d, float *uy_d, float *uz_d);
 cudaError_t d3q27_conservation(lbm_ctx *ctx, double *out_d);

@@ -388,3 +388,37 @@ def test_set_order_switches_the_fused_step():
                            induced=induced)
     ref = oracle.d3q27_run(dims, ref, flags, 0.9, 3, order=lbm.ORDER_CLI, tab_idx=tab_idx, tabs=recs, induced=induced)
     close(got, ref)
+
+
+# ------------------------------------------------------------------ equilibrium evaluation
+def test_equilibrium_selftest():
+    """The float-float equilibrium, wherever its error bound accepts it, equals the reference's
+    FP64 evaluation bit for bit, over 54 million evaluations with rho over 16 decades and |u| up
+    to 2; the FP64 fallback settles a small fraction."""
+    import ctypes
+    out = (ctypes.c_int64 * 2)()
+    lbm.capi.check(lbm.capi.lib().lbm_d3q27_equilibrium_selftest(2_000_000, 20261203, 0, out))
+    evaluations = 2_000_000 * 27
+    assert out[0] == 0, out[0]
+    assert out[1] < evaluations * 1e-3, out[1]
+
+
+@pytest.mark.parametrize("order", [lbm.ORDER_STREAM_COLLIDE, lbm.ORDER_CLI])
+def test_float_float_steps_equal_fp64_steps(order):
+    dims = (12, 9, 12)
+    f, flags, cells, recs, induced = random_lattice(dims, 77)
+    f = f * 20.0  # larger populations and velocities than the default lattice
+    outs, forces = [], []
+    for fp64 in (False, True):
+        with lattice(dims, tau=0.7, order=order) as L:
+            L.set_equilibrium_evaluation(fp64)
+            L.set_flags(flags)
+            L.load_populations(f)
+            L.set_reflection_tables(cells, recs)
+            L.set_flow(flags & SOURCE, induced)
+            L.set_force((0, 0, 0), True)
+            L.step(9)
+            outs.append(L.retrieve_populations())
+            forces.append(L.get_force())
+    assert np.array_equal(outs[0], outs[1])
+    assert np.array_equal(forces[0], forces[1])
