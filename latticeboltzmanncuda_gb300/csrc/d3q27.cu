@@ -38,21 +38,56 @@ __constant__ float c_split[27] = {0.0f,        1.0f,        1.0f,        1.0f,  
                                   0.5f,        1.0f / 3.0f, 1.0f / 3.0f, 1.0f / 3.0f, 1.0f / 3.0f, 1.0f / 3.0f,
                                   1.0f / 3.0f, 1.0f / 3.0f, 1.0f / 3.0f};
 
+// Unsigned 32-bit division by an invariant divisor with one multiply-high, two shifts and two adds
+// (Granlund and Montgomery, "Division by invariant integers using multiplication", PLDI 1994,
+// section 4): with l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1,
+// n / d = (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0), t = mulhi(m, n), for every 32-bit n.
+struct FastDiv {
+    uint32_t d, m;
+    int s1, s2;
+    static FastDiv make(uint32_t d) {
+        int l = 0;
+        while (l < 32 && (1ull << l) < d) ++l;
+        FastDiv f;
+        f.d = d;
+        f.m = (uint32_t)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+        f.s1 = l < 1 ? l : 1;
+        f.s2 = l > 1 ? l - 1 : 0;
+        return f;
+    }
+    __device__ __forceinline__ uint32_t div(uint32_t n) const {
+        const uint32_t t = __umulhi(m, n);
+        return (t + ((n - t) >> s1)) >> s2;
+    }
+};
+
 struct Dims {
     int X, Y, Z;
     int64_t n;
+    FastDiv dz, dy;  // division by Z and by Y
 };
 
+// cell index -> (x, y, z); cells < 2^31, so the index fits 32 bits
 __device__ __forceinline__ void decode(const Dims &d, int64_t c, int &x, int &y, int &z) {
-    z = (int)(c % d.Z);
-    int64_t t = c / d.Z;
-    y = (int)(t % d.Y);
-    x = (int)(t / d.Y);
+    const uint32_t u = (uint32_t)c;
+    const uint32_t t = d.dz.div(u);
+    z = (int)(u - t * (uint32_t)d.Z);
+    const uint32_t xq = d.dy.div(t);
+    y = (int)(t - xq * (uint32_t)d.Y);
+    x = (int)xq;
 }
 
 // pull streaming with zero fill (SimCalcFuncs.cu:79-96): v[j] = f_j(x - c_j), 0 outside
 __device__ __forceinline__ void pull(const float *__restrict__ src, const Dims &d, int64_t c, int x, int y, int z,
                                      float v[27]) {
+    if (x > 0 && y > 0 && z > 0 && x < d.X - 1 && y < d.Y - 1 && z < d.Z - 1) {
+        // interior cell: every neighbour exists
+        const int64_t sy = d.Z, sx = (int64_t)d.Z * d.Y;
+#pragma unroll
+        for (int j = 0; j < 27; ++j)
+            v[j] = __ldg(src + (int64_t)j * d.n + c - (int64_t)c_dir[j][2] - sy * c_dir[j][1] - sx * c_dir[j][0]);
+        return;
+    }
 #pragma unroll
     for (int j = 0; j < 27; ++j) {
         const int sx = x - c_dir[j][0], sy = y - c_dir[j][1], sz = z - c_dir[j][2];
@@ -394,7 +429,8 @@ __global__ void store_kernel(const float *__restrict__ f, H *__restrict__ host, 
 }
 
 inline Dims dims(const lbm_ctx *ctx) {
-    return Dims{ctx->desc.nx, ctx->desc.ny, ctx->desc.nz, ctx->cells};
+    return Dims{ctx->desc.nx, ctx->desc.ny, ctx->desc.nz, ctx->cells, FastDiv::make((uint32_t)ctx->desc.nz),
+                FastDiv::make((uint32_t)ctx->desc.ny)};
 }
 
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }

@@ -179,3 +179,25 @@ def test_row_sweep_slot_reuse_never_overwrites_a_live_row(nslot):
         assert (k + nslot - 1) % nslot not in live
         committed = (nslot - 1) + k  # prologue groups + one per earlier iteration
         assert committed - (nslot - 4) >= k + 3
+
+
+def test_invariant_division_formula():
+    """The D3Q27 kernels turn cell indices into (x, y, z) by the multiply-high division of
+    csrc/d3q27.cu (FastDiv, Granlund-Montgomery 1994): checked against integer division for every
+    divisor up to 2000, powers of two and neighbours, random divisors and numerators up to 2^32-1."""
+    import random
+
+    def fastdiv(n, d):
+        l = 0
+        while l < 32 and (1 << l) < d:
+            l += 1
+        m = ((1 << 32) * ((1 << l) - d) // d + 1) & 0xFFFFFFFF
+        t = (m * n) >> 32
+        return (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0)
+
+    rng = random.Random(1)
+    divisors = list(range(1, 2000)) + [rng.randrange(1, 2 ** 31) for _ in range(500)]
+    divisors += [2 ** k + e for k in range(1, 31) for e in (-1, 0, 1)]
+    for d in divisors:
+        for n in [0, 1, d - 1, d, d + 1, 2 * d - 1, 2 ** 31 - 1, 2 ** 32 - 1] + [rng.randrange(2 ** 32) for _ in range(50)]:
+            assert fastdiv(n, d) == n // d, (n, d)
