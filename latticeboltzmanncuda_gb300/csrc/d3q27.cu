@@ -155,18 +155,13 @@ __device__ __forceinline__ float eq_ff(float ph, float pl, float c1, float c1e, 
     return r;
 }
 
-__device__ __forceinline__ float eq_fast(int k, float ph, float pl, float c1, float c1e, float density, float ct,
-                                         float usq) {
-    bool ok;
-    const float r = eq_ff(ph, pl, c1, c1e, ct, ok);
-    return ok ? r : eq_fp64(k, density, ct, usq);
-}
-
 // calculate_collision (SimCalcFuncs.cu:98-156): FP32 density and SPLIT-weighted velocity, FP64
-// equilibrium rounded to FP32 (eq_fast, or the FP64 expression itself when EQ64), f += (eq - f) /
-// tau in FP32.
+// equilibrium rounded to FP32, f += (eq - f) / tau in FP32.  EQ64: the FP64 expression for every
+// direction.  Otherwise the float-float evaluation; if its bound cannot decide any direction of the
+// cell (about one cell in 10^4), the function returns false and leaves v undefined, and the caller
+// recomputes the cell with EQ64 -- keeping the FP64 code off the common path.
 template <bool EQ64>
-__device__ __forceinline__ void collide(float v[27], float tau) {
+__device__ __forceinline__ bool collide(float v[27], float tau) {
     float density = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
 #pragma unroll
     for (int i = 0; i < 27; ++i) {
@@ -190,14 +185,23 @@ __device__ __forceinline__ void collide(float v[27], float tau) {
             pl[k] = __fmaf_rn(kWlo(k), density, __fmaf_rn(kWhi(k), density, -ph[k]));
         }
     }
+    bool all_ok = true;
 #pragma unroll
     for (int i = 0; i < 27; ++i) {
         // c_i . u: the products by -1, 0, 1 are exact, so the two rounded adds fix the value
         const float ct = __fadd_rn(__fadd_rn((float)c_dir[i][0] * ux, (float)c_dir[i][1] * uy), (float)c_dir[i][2] * uz);
         const int k = wclass(i);
-        const float eq = EQ64 ? eq_fp64(k, density, ct, usq) : eq_fast(k, ph[k], pl[k], c1, c1e, density, ct, usq);
+        float eq;
+        if (EQ64) {
+            eq = eq_fp64(k, density, ct, usq);
+        } else {
+            bool ok;
+            eq = eq_ff(ph[k], pl[k], c1, c1e, ct, ok);
+            all_ok = all_ok && ok;
+        }
         v[i] = v[i] + (eq - v[i]) / tau;
     }
+    return all_ok;
 }
 
 struct StepArgs {
@@ -210,27 +214,39 @@ struct StepArgs {
     int cli;               // 1: stream, reflect, collide, flow; 0: stream, collide
 };
 
+// one cell of the fused step: pull, zero internal cells, collide, flow source, store
 template <bool EQ64>
-__global__ void __launch_bounds__(256) fused_kernel(StepArgs a) {
-    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (c >= a.d.n) return;
-    const uint8_t fl = a.flags[c];
-    if (a.cli && (fl & F_GATHER)) return;  // written by gather_kernel
-    int x, y, z;
-    decode(a.d, c, x, y, z);
+__device__ __forceinline__ bool fused_cell(const StepArgs &a, int64_t c, int x, int y, int z, uint8_t fl) {
     float v[27];
     pull(a.src, a.d, c, x, y, z, v);
     if (a.cli && (fl & F_INTERNAL)) {
 #pragma unroll
         for (int j = 0; j < 27; ++j) v[j] = 0.0f;
     }
-    collide<EQ64>(v, a.tau);
+    if (!collide<EQ64>(v, a.tau)) return false;
     if (a.cli && a.induced && (fl & F_SOURCE)) {
 #pragma unroll
         for (int j = 0; j < 27; ++j) v[j] = v[j] + __ldg(a.induced + j);
     }
 #pragma unroll
     for (int j = 0; j < 27; ++j) a.dst[(int64_t)j * a.d.n + c] = v[j];
+    return true;
+}
+
+// the rare cell whose float-float equilibrium the bound could not decide, recomputed in FP64
+__device__ __noinline__ void fused_cell_fp64(StepArgs a, int64_t c, int x, int y, int z, uint8_t fl) {
+    fused_cell<true>(a, c, x, y, z, fl);
+}
+
+template <bool EQ64>
+__global__ void __launch_bounds__(256, 2) fused_kernel(StepArgs a) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= a.d.n) return;
+    const uint8_t fl = a.flags[c];
+    if (a.cli && (fl & F_GATHER)) return;  // written by gather_kernel
+    int x, y, z;
+    decode(a.d, c, x, y, z);
+    if (!fused_cell<EQ64>(a, c, x, y, z, fl)) fused_cell_fp64(a, c, x, y, z, fl);
 }
 
 struct GatherArgs {
@@ -255,7 +271,8 @@ __device__ __forceinline__ void force_term(float m, const GatherEntry &e, int mo
 
 // mode 0: fused step (values of the reflecting cells are their streamed populations);
 // mode 1: the reference's separate reflection pass (values read in place, no collision).
-template <int MODE, bool EQ64>
+// The cells next to reflecting cells (a thin layer) evaluate the equilibrium in FP64 directly.
+template <int MODE>
 __global__ void __launch_bounds__(128) gather_kernel(StepArgs a, GatherArgs g) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     double facc[3] = {0.0, 0.0, 0.0};
@@ -288,7 +305,7 @@ __global__ void __launch_bounds__(128) gather_kernel(StepArgs a, GatherArgs g) {
             for (int j = 0; j < 27; ++j) v[j] = 0.0f;
         }
         if (MODE == 0) {
-            collide<EQ64>(v, a.tau);
+            collide<true>(v, a.tau);
             if (a.induced && (fl & F_SOURCE)) {
 #pragma unroll
                 for (int j = 0; j < 27; ++j) v[j] = v[j] + __ldg(a.induced + j);
@@ -331,7 +348,11 @@ __global__ void collide_kernel(float *__restrict__ f, Dims d, float tau) {
     float v[27];
 #pragma unroll
     for (int j = 0; j < 27; ++j) v[j] = f[(int64_t)j * d.n + c];
-    collide<EQ64>(v, tau);
+    if (!collide<EQ64>(v, tau)) {  // undecided by the float-float bound: the cell again in FP64
+#pragma unroll
+        for (int j = 0; j < 27; ++j) v[j] = f[(int64_t)j * d.n + c];
+        collide<true>(v, tau);
+    }
 #pragma unroll
     for (int j = 0; j < 27; ++j) f[(int64_t)j * d.n + c] = v[j];
 }
@@ -454,12 +475,10 @@ cudaError_t launch_gather(lbm_ctx *ctx, const StepArgs &a, int mode, double *for
     GatherArgs g = gather_args(ctx);
     const int threads = 128;
     const unsigned nb = blocks_for(ctx->ntgt, threads);
-    if (mode == 0 && ctx->eq_fp64)
-        gather_kernel<0, true><<<nb, threads, 0, ctx->stream>>>(a, g);
-    else if (mode == 0)
-        gather_kernel<0, false><<<nb, threads, 0, ctx->stream>>>(a, g);
+    if (mode == 0)
+        gather_kernel<0><<<nb, threads, 0, ctx->stream>>>(a, g);
     else
-        gather_kernel<1, false><<<nb, threads, 0, ctx->stream>>>(a, g);  // no collision in mode 1
+        gather_kernel<1><<<nb, threads, 0, ctx->stream>>>(a, g);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !g.partials) return e;
     return finalize_sums(ctx->stream, g.partials, (int)nb, 3, ctx->force_acc_d, true, force_copy);
