@@ -17,6 +17,8 @@
 // lbm_apply() runs the reference's single passes (stream / reflect / collide / flow) separately.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "lbm_internal.h"
 #include "reduce.cuh"
 
@@ -61,6 +63,60 @@ struct FastDiv {
     }
 };
 
+// The same tables as compile-time functions, for loops that are unrolled over the 27 directions:
+// every direction-dependent operand folds to an immediate (products by 0 vanish, by +-1 become
+// additions or subtractions).
+__host__ __device__ constexpr int kd(int j, int a) {
+    constexpr int t[27][3] = {
+        {0, 0, 0},   {-1, 0, 0},  {0, -1, 0},  {0, 0, -1},  {0, 0, 1},    {0, 1, 0},    {1, 0, 0},
+        {-1, -1, 0}, {-1, 0, -1}, {-1, 0, 1},  {-1, 1, 0},  {0, -1, -1},  {0, -1, 1},   {0, 1, -1},
+        {0, 1, 1},   {1, -1, 0},  {1, 0, -1},  {1, 0, 1},   {1, 1, 0},    {-1, -1, -1}, {-1, -1, 1},
+        {-1, 1, -1}, {-1, 1, 1},  {1, -1, -1}, {1, -1, 1},  {1, 1, -1},   {1, 1, 1}};
+    return t[j][a];
+}
+__host__ __device__ constexpr float ks(int j) { return j == 0 ? 0.0f : (j < 7 ? 1.0f : (j < 19 ? 0.5f : 1.0f / 3.0f)); }
+
+// c_j . u = ((c_jx ux) + (c_jy uy)) + (c_jz uz) with the zero terms left out: the products by
+// -1, 0, 1 are exact and adding an exact zero changes no non-zero value, so this is the
+// reference's FP32 value (up to the sign of a zero result)
+template <int J>
+__device__ __forceinline__ float cdot(float ux, float uy, float uz) {
+    float s = 0.0f;
+    bool any = false;
+    const float u[3] = {ux, uy, uz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (kd(J, a) == 0) continue;
+        const float t = kd(J, a) > 0 ? u[a] : -u[a];
+        s = any ? __fadd_rn(s, t) : t;
+        any = true;
+    }
+    return s;
+}
+
+// SPLIT-weighted first moment (SimCalcFuncs.cu:109-113): m_a += f_j c_ja SPLIT_j over j, the zero
+// terms left out (an exact zero added to the running sum changes nothing for finite populations)
+template <int J>
+__device__ __forceinline__ void split_moment(float v, float &mx, float &my, float &mz) {
+    if (kd(J, 0)) mx += v * (float)kd(J, 0) * ks(J);
+    if (kd(J, 1)) my += v * (float)kd(J, 1) * ks(J);
+    if (kd(J, 2)) mz += v * (float)kd(J, 2) * ks(J);
+}
+
+template <int J>
+struct Unroll {
+    template <class F>
+    static __device__ __forceinline__ void run(F &&f) {
+        Unroll<J - 1>::run(f);
+        f(std::integral_constant<int, J - 1>{});
+    }
+};
+template <>
+struct Unroll<0> {
+    template <class F>
+    static __device__ __forceinline__ void run(F &&) {}
+};
+
 struct Dims {
     int X, Y, Z;
     int64_t n;
@@ -83,9 +139,13 @@ __device__ __forceinline__ void pull(const float *__restrict__ src, const Dims &
     if (x > 0 && y > 0 && z > 0 && x < d.X - 1 && y < d.Y - 1 && z < d.Z - 1) {
         // interior cell: every neighbour exists
         const int64_t sy = d.Z, sx = (int64_t)d.Z * d.Y;
-#pragma unroll
-        for (int j = 0; j < 27; ++j)
-            v[j] = __ldg(src + (int64_t)j * d.n + c - (int64_t)c_dir[j][2] - sy * c_dir[j][1] - sx * c_dir[j][0]);
+        Unroll<27>::run([&](auto jj) {
+            constexpr int j = decltype(jj)::value;
+            int64_t s = c - kd(j, 2);
+            if (kd(j, 1)) s = kd(j, 1) > 0 ? s - sy : s + sy;
+            if (kd(j, 0)) s = kd(j, 0) > 0 ? s - sx : s + sx;
+            v[j] = __ldg(src + (int64_t)j * d.n + s);
+        });
         return;
     }
 #pragma unroll
@@ -163,13 +223,11 @@ __device__ __forceinline__ float eq_ff(float ph, float pl, float c1, float c1e, 
 template <bool EQ64>
 __device__ __forceinline__ bool collide(float v[27], float tau) {
     float density = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
-#pragma unroll
-    for (int i = 0; i < 27; ++i) {
+    Unroll<27>::run([&](auto ii) {
+        constexpr int i = decltype(ii)::value;
         density += v[i];
-        ux += v[i] * (float)c_dir[i][0] * c_split[i];
-        uy += v[i] * (float)c_dir[i][1] * c_split[i];
-        uz += v[i] * (float)c_dir[i][2] * c_split[i];
-    }
+        split_moment<i>(v[i], ux, uy, uz);
+    });
     if (density != 0.0f) {
         ux /= density;
         uy /= density;
@@ -186,11 +244,10 @@ __device__ __forceinline__ bool collide(float v[27], float tau) {
         }
     }
     bool all_ok = true;
-#pragma unroll
-    for (int i = 0; i < 27; ++i) {
-        // c_i . u: the products by -1, 0, 1 are exact, so the two rounded adds fix the value
-        const float ct = __fadd_rn(__fadd_rn((float)c_dir[i][0] * ux, (float)c_dir[i][1] * uy), (float)c_dir[i][2] * uz);
-        const int k = wclass(i);
+    Unroll<27>::run([&](auto ii) {
+        constexpr int i = decltype(ii)::value;
+        const float ct = cdot<i>(ux, uy, uz);
+        constexpr int k = wclass(i);
         float eq;
         if (EQ64) {
             eq = eq_fp64(k, density, ct, usq);
@@ -200,7 +257,7 @@ __device__ __forceinline__ bool collide(float v[27], float tau) {
             all_ok = all_ok && ok;
         }
         v[i] = v[i] + (eq - v[i]) / tau;
-    }
+    });
     return all_ok;
 }
 
@@ -370,14 +427,12 @@ __global__ void moments_kernel(const float *__restrict__ f, Dims d, float *rho, 
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= d.n) return;
     float density = 0.0f, vx = 0.0f, vy = 0.0f, vz = 0.0f;
-#pragma unroll
-    for (int i = 0; i < 27; ++i) {
+    Unroll<27>::run([&](auto ii) {
+        constexpr int i = decltype(ii)::value;
         const float v = f[(int64_t)i * d.n + c];
         density += v;
-        vx += v * (float)c_dir[i][0] * c_split[i];
-        vy += v * (float)c_dir[i][1] * c_split[i];
-        vz += v * (float)c_dir[i][2] * c_split[i];
-    }
+        split_moment<i>(v, vx, vy, vz);
+    });
     if (density != 0.0f) {
         vx /= density;
         vy /= density;
@@ -512,7 +567,7 @@ __global__ void eq_selftest_kernel(int64_t n, uint64_t seed, unsigned long long 
             const float ph = __fmul_rn(kWhi(k), rho);
             const float pl = __fmaf_rn(kWlo(k), rho, __fmaf_rn(kWhi(k), rho, -ph));
             const float ct = __fadd_rn(__fadd_rn((float)c_dir[i][0] * ux, (float)c_dir[i][1] * uy), (float)c_dir[i][2] * uz);
-            bool ok;
+            bool ok;  // (c_i . u with the table in constant memory: the same value as cdot<i>)
             const float a = eq_ff(ph, pl, c1, c1e, ct, ok);
             const float b = eq_fp64(k, rho, ct, usq);
             bad += ok && __float_as_uint(a) != __float_as_uint(b);
