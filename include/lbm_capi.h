@@ -192,6 +192,11 @@ LBM_API lbm_status lbm_set_equilibrium_evaluation(lbm_ctx *ctx, int32_t mode);
  * `device`; out[0] = float-float results accepted by the bound that differ from FP64 (must be 0),
  * out[1] = evaluations settled by the FP64 fallback. */
 LBM_API lbm_status lbm_d3q27_equilibrium_selftest(int64_t samples, uint64_t seed, int32_t device, int64_t out[2]);
+/* Diagnostic: the D3Q27_REF step divides by tau with one correction of RN(x * RN(1/tau))
+ * (Markstein 1990) where that equals the IEEE division; this counts, over all 2^32 float inputs x,
+ * the quotients that would differ for this tau (the library checks each tau it uses the same way
+ * and keeps the IEEE division for a tau with any difference). */
+LBM_API lbm_status lbm_d3q27_division_check(float tau, int32_t device, int64_t *mismatches);
 /* D3Q27_REF: the step order of later lbm_step() calls (LBM_ORDER_*), e.g. the stream-collide of
  * Lattice::simulateLattice and the CLI loop on one lattice. */
 LBM_API lbm_status lbm_set_order(lbm_ctx *ctx, int32_t order);

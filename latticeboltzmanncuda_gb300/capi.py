@@ -120,6 +120,7 @@ SIGNATURES = [
     ("lbm_set_order", _S, [_P, _I32]),
     ("lbm_set_equilibrium_evaluation", _S, [_P, _I32]),
     ("lbm_d3q27_equilibrium_selftest", _S, [_I64, _U64, _I32, _P]),
+    ("lbm_d3q27_division_check", _S, [_F, _I32, _P]),
     ("lbm_set_force_accumulation", _S, [_P, _I32]),
     ("lbm_force_accumulation", _I32, [_P]),
     ("lbm_step_force_series", _S, [_P, _I32, _P]),

@@ -621,6 +621,24 @@ LBM_API lbm_status lbm_d3q27_equilibrium_selftest(int64_t samples, uint64_t seed
     return LBM_OK;
 }
 
+LBM_API lbm_status lbm_d3q27_division_check(float tau, int32_t device, int64_t *mismatches) {
+    if (!mismatches) return set_thread_error(LBM_ERR_INVALID, "lbm_d3q27_division_check: null output");
+    cudaError_t e = cudaSetDevice(device);
+    void *buf = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(&buf, 16);
+    if (e == cudaSuccess) e = cudaMemset(buf, 0, 16);
+    if (e == cudaSuccess)
+        e = d3q27_division_check(tau, reinterpret_cast<unsigned long long *>(static_cast<char *>(buf) + 8),
+                                 static_cast<float *>(buf), nullptr);
+    unsigned long long h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, static_cast<char *>(buf) + 8, sizeof(h), cudaMemcpyDeviceToHost);
+    if (buf) cudaFree(buf);
+    if (e != cudaSuccess)
+        return set_thread_error(LBM_ERR_CUDA, std::string("lbm_d3q27_division_check: ") + cudaGetErrorString(e));
+    *mismatches = (int64_t)h;
+    return LBM_OK;
+}
+
 LBM_API lbm_status lbm_set_order(lbm_ctx *ctx, int32_t order) {
     CHECK_CTX(ctx);
     if (ctx->desc.mode != LBM_D3Q27_REF) return fail(ctx, LBM_ERR_UNSUPPORTED, "step orders are D3Q27_REF only");

@@ -17,6 +17,10 @@
 // lbm_apply() runs the reference's single passes (stream / reflect / collide / flow) separately.
 #include <cuda_runtime.h>
 
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
 #include <type_traits>
 
 #include "lbm_internal.h"
@@ -215,13 +219,46 @@ __device__ __forceinline__ float eq_ff(float ph, float pl, float c1, float c1e, 
     return r;
 }
 
+// ------------------------------------------------------------------------- division by tau
+// The update divides by tau 27 times per cell (SimCalcFuncs.cu:128).  With y = RN(1/tau), the
+// quotient q = RN(x y) corrected once, RN(q + RN(x - tau q) y) (Markstein, IBM J. Res. Dev. 34(1),
+// 1990), is the correctly rounded x / tau; each tau the library uses is first checked against the
+// IEEE division for all 2^32 float inputs (tau_check), and the correction is used only for a tau
+// that passes, and only for |x| in [2^-96, 2^96] (elsewhere: the IEEE division).
+struct Tau {
+    float b;   // tau
+    float y;   // RN(1 / tau)
+    int fast;  // 1: tau passed the exhaustive check
+};
+
+__device__ __forceinline__ float div_tau(float x, const Tau &t) {
+    const float ax = fabsf(x);
+    if (t.fast && ax >= 0x1p-96f && ax <= 0x1p96f) {
+        const float q = __fmul_rn(x, t.y);
+        return __fmaf_rn(__fmaf_rn(-q, t.b, x), t.y, q);
+    }
+    return __fdiv_rn(x, t.b);
+}
+
+__global__ void tau_check_kernel(float b, float *y_out, unsigned long long *bad) {
+    const Tau t{b, __frcp_rn(b), 1};
+    if (blockIdx.x == 0 && threadIdx.x == 0) *y_out = t.y;
+    unsigned long long n = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < (1ull << 32); i += (uint64_t)gridDim.x * blockDim.x) {
+        const float x = __uint_as_float((uint32_t)i);
+        const float a = div_tau(x, t), e = __fdiv_rn(x, b);
+        n += __float_as_uint(a) != __float_as_uint(e) && !(a != a && e != e);
+    }
+    atomicAdd(bad, n);
+}
+
 // calculate_collision (SimCalcFuncs.cu:98-156): FP32 density and SPLIT-weighted velocity, FP64
 // equilibrium rounded to FP32, f += (eq - f) / tau in FP32.  EQ64: the FP64 expression for every
 // direction.  Otherwise the float-float evaluation; if its bound cannot decide any direction of the
 // cell (about one cell in 10^4), the function returns false and leaves v undefined, and the caller
 // recomputes the cell with EQ64 -- keeping the FP64 code off the common path.
 template <bool EQ64>
-__device__ __forceinline__ bool collide(float v[27], float tau) {
+__device__ __forceinline__ bool collide(float v[27], const Tau &tau) {
     float density = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
     Unroll<27>::run([&](auto ii) {
         constexpr int i = decltype(ii)::value;
@@ -256,7 +293,7 @@ __device__ __forceinline__ bool collide(float v[27], float tau) {
             eq = eq_ff(ph[k], pl[k], c1, c1e, ct, ok);
             all_ok = all_ok && ok;
         }
-        v[i] = v[i] + (eq - v[i]) / tau;
+        v[i] = v[i] + div_tau(eq - v[i], tau);
     });
     return all_ok;
 }
@@ -266,7 +303,7 @@ struct StepArgs {
     float *dst;
     const uint8_t *flags;
     Dims d;
-    float tau;
+    Tau tau;
     const float *induced;  // nullptr: no flow
     int cli;               // 1: stream, reflect, collide, flow; 0: stream, collide
 };
@@ -399,7 +436,7 @@ __global__ void reflect_copy_kernel(const float *__restrict__ src, float *__rest
 }
 
 template <bool EQ64>
-__global__ void collide_kernel(float *__restrict__ f, Dims d, float tau) {
+__global__ void collide_kernel(float *__restrict__ f, Dims d, Tau tau) {
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= d.n) return;
     float v[27];
@@ -514,6 +551,51 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
 float *cur(lbm_ctx *ctx) { return static_cast<float *>(ctx->f[ctx->cur]); }
 float *nxt(lbm_ctx *ctx) { return static_cast<float *>(ctx->f[ctx->cur ^ 1]); }
 
+// Tau of the context, with RN(1/tau) and the verdict of the exhaustive division check, cached per
+// tau value for the process (the check runs once per value, a few milliseconds on the GPU).
+Tau tau_of(lbm_ctx *ctx) {
+    static std::mutex mu;
+    static std::map<uint32_t, std::pair<float, int>> cache;
+    const float b = ctx->desc.tau;
+    uint32_t key;
+    std::memcpy(&key, &b, sizeof(key));
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) return Tau{b, it->second.first, it->second.second};
+    }
+    Tau t{b, 0.0f, 0};
+    const float ab = std::fabs(b);
+    if (!(ab >= 0x1p-60f && ab <= 0x1p60f)) return t;  // keep the IEEE division for extreme tau
+    void *buf = nullptr;
+    if (cudaMalloc(&buf, 16) != cudaSuccess) {
+        cudaGetLastError();
+        return t;
+    }
+    float *y_d = static_cast<float *>(buf);
+    unsigned long long *bad_d = reinterpret_cast<unsigned long long *>(static_cast<char *>(buf) + 8);
+    float y = 0.0f;
+    unsigned long long bad = 1;
+    cudaError_t e = cudaMemsetAsync(buf, 0, 16, ctx->stream);
+    if (e == cudaSuccess) {
+        tau_check_kernel<<<1216, 256, 0, ctx->stream>>>(b, y_d, bad_d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&y, y_d, sizeof(y), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, bad_d, sizeof(bad), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(buf);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return t;
+    }
+    t.y = y;
+    t.fast = bad == 0 ? 1 : 0;
+    std::lock_guard<std::mutex> g(mu);
+    cache[key] = {t.y, t.fast};
+    return t;
+}
+
 GatherArgs gather_args(lbm_ctx *ctx) {
     GatherArgs g;
     g.tgt = ctx->tgt_cells_d;
@@ -580,6 +662,11 @@ __global__ void eq_selftest_kernel(int64_t n, uint64_t seed, unsigned long long 
 
 }  // namespace
 
+cudaError_t d3q27_division_check(float tau, unsigned long long *bad_d, float *y_d, cudaStream_t st) {
+    tau_check_kernel<<<1216, 256, 0, st>>>(tau, y_d, bad_d);
+    return cudaGetLastError();
+}
+
 cudaError_t d3q27_eq_selftest(int64_t n, uint64_t seed, unsigned long long *out_d, cudaStream_t st) {
     eq_selftest_kernel<<<1216, 256, 0, st>>>(n, seed, out_d);
     return cudaGetLastError();
@@ -587,13 +674,15 @@ cudaError_t d3q27_eq_selftest(int64_t n, uint64_t seed, unsigned long long *out_
 
 cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps, double *series_d) {
     const int threads = 256;
+    const Tau tau = tau_of(ctx);
+    const Dims dm = dims(ctx);
     for (int s = 0; s < nsteps; ++s) {
         StepArgs a;
         a.src = cur(ctx);
         a.dst = nxt(ctx);
         a.flags = ctx->flags_d;
-        a.d = dims(ctx);
-        a.tau = ctx->desc.tau;
+        a.d = dm;
+        a.tau = tau;
         a.cli = ctx->desc.order == LBM_ORDER_CLI;
         a.induced = (a.cli && ctx->flow_on) ? ctx->induced_d : nullptr;
         if (ctx->eq_fp64)
@@ -637,7 +726,7 @@ cudaError_t d3q27_apply(lbm_ctx *ctx, int op) {
             a.dst = nxt(ctx);
             a.flags = ctx->flags_d;
             a.d = d;
-            a.tau = ctx->desc.tau;
+            a.tau = tau_of(ctx);
             a.induced = nullptr;
             a.cli = 1;
             e = launch_gather(ctx, a, 1);
@@ -646,9 +735,9 @@ cudaError_t d3q27_apply(lbm_ctx *ctx, int op) {
         }
         case LBM_OP_COLLIDE:
             if (ctx->eq_fp64)
-                collide_kernel<true><<<nb, threads, 0, ctx->stream>>>(cur(ctx), d, ctx->desc.tau);
+                collide_kernel<true><<<nb, threads, 0, ctx->stream>>>(cur(ctx), d, tau_of(ctx));
             else
-                collide_kernel<false><<<nb, threads, 0, ctx->stream>>>(cur(ctx), d, ctx->desc.tau);
+                collide_kernel<false><<<nb, threads, 0, ctx->stream>>>(cur(ctx), d, tau_of(ctx));
             e = cudaGetLastError();
             break;
         case LBM_OP_FLOW:

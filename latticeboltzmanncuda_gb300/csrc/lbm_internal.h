@@ -152,6 +152,7 @@ cudaError_t d2q9_store(lbm_ctx *ctx, void *dst_d, int dst_dtype, int aos);
 // series_d (optional): the accumulated force after step s is written to series_d[3s..3s+2]
 cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps, double *series_d = nullptr);
 cudaError_t d3q27_eq_selftest(int64_t n, uint64_t seed, unsigned long long *out_d, cudaStream_t st);
+cudaError_t d3q27_division_check(float tau, unsigned long long *bad_d, float *y_d, cudaStream_t st);
 cudaError_t d3q27_apply(lbm_ctx *ctx, int op);
 cudaError_t d3q27_moments(lbm_ctx *ctx, float *rho_d, float *ux_d, float *uy_d, float *uz_d);
 cudaError_t d3q27_conservation(lbm_ctx *ctx, double *out_d);

@@ -422,3 +422,12 @@ def test_float_float_steps_equal_fp64_steps(order):
             forces.append(L.get_force())
     assert np.array_equal(outs[0], outs[1])
     assert np.array_equal(forces[0], forces[1])
+
+
+@pytest.mark.parametrize("tau", [0.5, 0.51, 0.55, 0.6, 0.7, 0.8, 0.9, 1.0, 1.2, 1.7, 3.0, 0.6180339887, 1e-3, 250.0])
+def test_division_by_tau_matches_ieee_for_every_input(tau):
+    """One Markstein correction of RN(x RN(1/tau)) gives the IEEE quotient for all 2^32 float x."""
+    import ctypes
+    bad = ctypes.c_int64(-1)
+    lbm.capi.check(lbm.capi.lib().lbm_d3q27_division_check(ctypes.c_float(tau), 0, ctypes.byref(bad)))
+    assert bad.value == 0
