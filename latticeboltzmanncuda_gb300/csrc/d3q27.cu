@@ -78,6 +78,12 @@ __host__ __device__ constexpr int kd(int j, int a) {
         {-1, 1, -1}, {-1, 1, 1},  {1, -1, -1}, {1, -1, 1},  {1, 1, -1},   {1, 1, 1}};
     return t[j][a];
 }
+__host__ __device__ constexpr int opp27(int j) {
+    int r = 0;
+    for (int p = 0; p < 27; ++p)
+        if (kd(p, 0) == -kd(j, 0) && kd(p, 1) == -kd(j, 1) && kd(p, 2) == -kd(j, 2)) r = p;
+    return r;
+}
 __host__ __device__ constexpr float ks(int j) { return j == 0 ? 0.0f : (j < 7 ? 1.0f : (j < 19 ? 0.5f : 1.0f / 3.0f)); }
 
 // c_j . u = ((c_jx ux) + (c_jy uy)) + (c_jz uz) with the zero terms left out: the products by
@@ -99,12 +105,19 @@ __device__ __forceinline__ float cdot(float ux, float uy, float uz) {
 }
 
 // SPLIT-weighted first moment (SimCalcFuncs.cu:109-113): m_a += f_j c_ja SPLIT_j over j, the zero
-// terms left out (an exact zero added to the running sum changes nothing for finite populations)
+// terms left out (an exact zero added to the running sum changes nothing for finite populations).
+// Each term is one fused multiply-add, m_a = RN((f_j c_ja) SPLIT_j + m_a) (f_j c_ja is exact), written
+// with the explicit intrinsic so that every kernel rounds it the same way.
 template <int J>
 __device__ __forceinline__ void split_moment(float v, float &mx, float &my, float &mz) {
-    if (kd(J, 0)) mx += v * (float)kd(J, 0) * ks(J);
-    if (kd(J, 1)) my += v * (float)kd(J, 1) * ks(J);
-    if (kd(J, 2)) mz += v * (float)kd(J, 2) * ks(J);
+    if (kd(J, 0)) mx = __fmaf_rn(kd(J, 0) > 0 ? v : -v, ks(J), mx);
+    if (kd(J, 1)) my = __fmaf_rn(kd(J, 1) > 0 ? v : -v, ks(J), my);
+    if (kd(J, 2)) mz = __fmaf_rn(kd(J, 2) > 0 ? v : -v, ks(J), mz);
+}
+
+// |u|^2 = (ux ux + uy uy) + uz uz as two fused multiply-adds, the same in every kernel
+__device__ __forceinline__ float usq_of(float ux, float uy, float uz) {
+    return __fmaf_rn(uz, uz, __fmaf_rn(uy, uy, __fmul_rn(ux, ux)));
 }
 
 template <int J>
@@ -196,6 +209,42 @@ __device__ __forceinline__ float eq_fp64(int k, float density, float ct, float u
 
 // ph + pl: W_k * rho within 2^-47; c1 + c1e == 1.5 usq exactly.  Returns the FP32 rounding of the
 // float-float value; ok says whether it is proven equal to the FP64 evaluation.
+// E = (ph + pl) * (1 + s2 + lo) rounded to FP32, with the acceptance test against the bound m on
+// |E_ff - E_fp64| (see above)
+__device__ __forceinline__ float ff_finish(float ph, float pl, float m, float s2, float lo, bool &ok) {
+    float th, e3;
+    two_sum(1.0f, s2, th, e3);
+    const float tl = __fadd_rn(e3, lo);                                   // T = th + tl
+    const float eh = __fmul_rn(ph, th);
+    const float el = __fmaf_rn(ph, tl, __fmaf_rn(pl, th, __fmaf_rn(ph, th, -eh)));
+    const float r = __fadd_rn(eh, el);
+    const float d = __fadd_rn(__fsub_rn(eh, r), el);                      // (eh + el) - r
+    const uint32_t rb = __float_as_uint(r) & 0x7fffffffu;
+    const uint32_t ex = rb & 0x7f800000u;
+    // half the smaller gap next to r (2^e * 2^-24, or 2^-25 at a power of two)
+    const float half_gap = __fmul_rn(__uint_as_float(ex), (rb & 0x7fffffu) ? 0x1p-24f : 0x1p-25f);
+    ok = ex >= (67u << 23) && ex < 0x7f800000u && __fadd_rn(fabsf(d), m) < half_gap;
+    return r;
+}
+
+// The pair of opposite directions (c . u = ct and -ct) shares ct^2, B and the bound: mk = |ph| 2^-42,
+// c1p = 1 + 1.5 usq rounded (M = 1 + |A| + B + C up to rounding, well inside the bound's margin).
+__device__ __forceinline__ void eq_ff_pair(float ph, float pl, float mk, float c1, float c1e, float c1p, float ct,
+                                           float &rp, bool &okp, float &rn, bool &okn) {
+    const float a = __fmul_rn(3.0f, ct), ae = __fmaf_rn(3.0f, ct, -a);      // A = 3 ct (for -ct: -a, -ae)
+    const float p = __fmul_rn(ct, ct), pe = __fmaf_rn(ct, ct, -p);         // ct^2
+    const float b = __fmul_rn(4.5f, p), be = __fmaf_rn(4.5f, p, -b);       // B = 4.5 ct^2 = b + be + 4.5 pe
+    const float bb = __fsub_rn(__fadd_rn(be, __fmul_rn(4.5f, pe)), c1e);   // low parts of B - C
+    const float m = __fmul_rn(mk, __fadd_rn(__fadd_rn(c1p, fabsf(a)), b));
+    float s1, e1, s2, e2;
+    two_sum(a, b, s1, e1);
+    two_sum(s1, -c1, s2, e2);
+    rp = ff_finish(ph, pl, m, s2, __fadd_rn(__fadd_rn(__fadd_rn(ae, bb), e1), e2), okp);
+    two_sum(-a, b, s1, e1);
+    two_sum(s1, -c1, s2, e2);
+    rn = ff_finish(ph, pl, m, s2, __fadd_rn(__fadd_rn(__fadd_rn(-ae, bb), e1), e2), okn);
+}
+
 __device__ __forceinline__ float eq_ff(float ph, float pl, float c1, float c1e, float ct, bool &ok) {
     const float a = __fmul_rn(3.0f, ct), ae = __fmaf_rn(3.0f, ct, -a);      // A = 3 ct
     const float p = __fmul_rn(ct, ct), pe = __fmaf_rn(ct, ct, -p);         // ct^2
@@ -231,13 +280,19 @@ struct Tau {
     int fast;  // 1: tau passed the exhaustive check
 };
 
-__device__ __forceinline__ float div_tau(float x, const Tau &t) {
+// the corrected reciprocal product where it is the IEEE quotient (ok), for |x| in [2^-96, 2^96] or 0
+__device__ __forceinline__ float div_fast(float x, const Tau &t, bool &ok) {
     const float ax = fabsf(x);
-    if (t.fast && ax >= 0x1p-96f && ax <= 0x1p96f) {
-        const float q = __fmul_rn(x, t.y);
-        return __fmaf_rn(__fmaf_rn(-q, t.b, x), t.y, q);
-    }
-    return __fdiv_rn(x, t.b);
+    ok = t.fast && ax <= 0x1p96f && (ax >= 0x1p-96f || ax == 0.0f);
+    if (ax == 0.0f) return t.b > 0.0f ? x : -x;  // +-0 / tau
+    const float q = __fmul_rn(x, t.y);
+    return __fmaf_rn(__fmaf_rn(-q, t.b, x), t.y, q);
+}
+
+__device__ __forceinline__ float div_tau(float x, const Tau &t) {
+    bool ok;
+    const float q = div_fast(x, t, ok);
+    return ok ? q : __fdiv_rn(x, t.b);
 }
 
 __global__ void tau_check_kernel(float b, float *y_out, unsigned long long *bad) {
@@ -270,30 +325,52 @@ __device__ __forceinline__ bool collide(float v[27], const Tau &tau) {
         uy /= density;
         uz /= density;
     }
-    const float usq = (ux * ux) + (uy * uy) + (uz * uz);
-    float ph[4], pl[4];
-    const float c1 = __fmul_rn(1.5f, usq), c1e = __fmaf_rn(1.5f, usq, -c1);
-    if (!EQ64) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            ph[k] = __fmul_rn(kWhi(k), density);
-            pl[k] = __fmaf_rn(kWlo(k), density, __fmaf_rn(kWhi(k), density, -ph[k]));
-        }
+    const float usq = usq_of(ux, uy, uz);
+    if (EQ64) {
+        Unroll<27>::run([&](auto ii) {
+            constexpr int i = decltype(ii)::value;
+            v[i] = v[i] + div_tau(eq_fp64(wclass(i), density, cdot<i>(ux, uy, uz), usq) - v[i], tau);
+        });
+        return true;
     }
+    float ph[4], pl[4], mk[4];
+    const float c1 = __fmul_rn(1.5f, usq), c1e = __fmaf_rn(1.5f, usq, -c1), c1p = __fadd_rn(1.0f, c1);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        ph[k] = __fmul_rn(kWhi(k), density);
+        pl[k] = __fmaf_rn(kWlo(k), density, __fmaf_rn(kWhi(k), density, -ph[k]));
+        mk[k] = __fmul_rn(fabsf(ph[k]), 0x1p-42f);
+    }
+    // a cell with zero density and velocity (e.g. an internal, zeroed cell): the FP64 value is
+    // W * density * 1, a zero with the sign of the density
+    const bool still = density == 0.0f && usq == 0.0f;
+    const float zero = copysignf(0.0f, density);
     bool all_ok = true;
+    // division: the corrected reciprocal product only; an input outside its range (or a tau that
+    // failed the check) sends the cell to the FP64 recomputation like an undecided equilibrium
+    auto relax = [&](float &f, float eq) {
+        bool ok;
+        f = f + div_fast(eq - f, tau, ok);
+        all_ok = all_ok && ok;
+    };
+    {
+        bool ok;
+        const float eq = eq_ff(ph[0], pl[0], c1, c1e, 0.0f, ok);
+        all_ok = ok || still;
+        relax(v[0], still ? zero : eq);
+    }
     Unroll<27>::run([&](auto ii) {
         constexpr int i = decltype(ii)::value;
-        const float ct = cdot<i>(ux, uy, uz);
-        constexpr int k = wclass(i);
-        float eq;
-        if (EQ64) {
-            eq = eq_fp64(k, density, ct, usq);
-        } else {
-            bool ok;
-            eq = eq_ff(ph[k], pl[k], c1, c1e, ct, ok);
-            all_ok = all_ok && ok;
+        constexpr int j = opp27(i);
+        if constexpr (i > 0 && i < j) {
+            constexpr int k = wclass(i);
+            float rp, rn;
+            bool okp, okn;
+            eq_ff_pair(ph[k], pl[k], mk[k], c1, c1e, c1p, cdot<i>(ux, uy, uz), rp, okp, rn, okn);
+            all_ok = all_ok && ((okp && okn) || still);
+            relax(v[i], still ? zero : rp);
+            relax(v[j], still ? zero : rn);
         }
-        v[i] = v[i] + div_tau(eq - v[i], tau);
     });
     return all_ok;
 }
@@ -386,12 +463,12 @@ __global__ void __launch_bounds__(128) gather_kernel(StepArgs a, GatherArgs g) {
             const GatherEntry e = g.ent[k];
             const int64_t s = MODE == 0 ? (int64_t)e.src_stream : (int64_t)e.src_cell;
             const float val = s >= 0 ? __ldg(a.src + (int64_t)e.src_pop * a.d.n + s) : 0.0f;
-            const float m = val * e.w;
-            // v[e.dst_pop] += m, one add per contribution as the reference's atomicAdd
-            // (SimCalcFuncs.cu:177), selected over the register-resident array
+            const float m = __fmul_rn(val, e.w);
+            // v[e.dst_pop] += m, one rounded add of the rounded product per contribution as the
+            // reference's atomicAdd (SimCalcFuncs.cu:177), selected over the register-resident array
 #pragma unroll
             for (int j = 1; j < 27; ++j)
-                if (j == e.dst_pop) v[j] = v[j] + m;
+                if (j == e.dst_pop) v[j] = __fadd_rn(v[j], m);
             if (g.partials) force_term(m, e, g.force_mode, facc);
         }
         if (fl & F_INTERNAL) {
