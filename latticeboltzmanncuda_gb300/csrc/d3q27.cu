@@ -410,7 +410,7 @@ __device__ __noinline__ void fused_cell_fp64(StepArgs a, int64_t c, int x, int y
 }
 
 template <bool EQ64>
-__global__ void __launch_bounds__(256, 2) fused_kernel(StepArgs a) {
+__global__ void __launch_bounds__(256, 3) fused_kernel(StepArgs a) {
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= a.d.n) return;
     const uint8_t fl = a.flags[c];
