@@ -188,9 +188,10 @@ LBM_API lbm_status lbm_apply(lbm_ctx *ctx, int32_t op);
  *                                 the step) */
 enum { LBM_EQ_FLOAT_FLOAT = 0, LBM_EQ_FP64 = 1 };
 LBM_API lbm_status lbm_set_equilibrium_evaluation(lbm_ctx *ctx, int32_t mode);
-/* Diagnostic: both evaluations on `samples` pseudo-random (rho, u) draws x 27 directions on
- * `device`; out[0] = float-float results accepted by the bound that differ from FP64 (must be 0),
- * out[1] = evaluations settled by the FP64 fallback. */
+/* Diagnostic: both evaluations on `samples` pseudo-random (rho, u) draws (|u| up to 2) x the 27
+ * directions on `device`; out[0] = float-float results accepted by their bound that differ from
+ * FP64 (must be 0), out[1] = direction pairs left to the FP64 fallback among the draws with
+ * |u| <= 0.3. */
 LBM_API lbm_status lbm_d3q27_equilibrium_selftest(int64_t samples, uint64_t seed, int32_t device, int64_t out[2]);
 /* Diagnostic: the D3Q27_REF step divides by tau with one correction of RN(x * RN(1/tau))
  * (Markstein 1990) where that equals the IEEE division; this counts, over all 2^32 float inputs x,

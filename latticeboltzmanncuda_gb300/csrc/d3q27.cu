@@ -209,11 +209,18 @@ __device__ __forceinline__ float eq_fp64(int k, float density, float ct, float u
 
 // ph + pl: W_k * rho within 2^-47; c1 + c1e == 1.5 usq exactly.  Returns the FP32 rounding of the
 // float-float value; ok says whether it is proven equal to the FP64 evaluation.
+// s + e == a + b exactly when |a| >= |b| (Dekker's fast two-sum)
+__device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
 // E = (ph + pl) * (1 + s2 + lo) rounded to FP32, with the acceptance test against the bound m on
-// |E_ff - E_fp64| (see above)
+// |E_ff - E_fp64| (see above).  The sum 1 + s2 uses the fast two-sum, exact for |s2| <= 1; a larger
+// |s2| (|c . u| beyond about 0.27) is left to the FP64 recomputation.
 __device__ __forceinline__ float ff_finish(float ph, float pl, float m, float s2, float lo, bool &ok) {
     float th, e3;
-    two_sum(1.0f, s2, th, e3);
+    fast_two_sum(1.0f, s2, th, e3);
     const float tl = __fadd_rn(e3, lo);                                   // T = th + tl
     const float eh = __fmul_rn(ph, th);
     const float el = __fmaf_rn(ph, tl, __fmaf_rn(pl, th, __fmaf_rn(ph, th, -eh)));
@@ -223,7 +230,7 @@ __device__ __forceinline__ float ff_finish(float ph, float pl, float m, float s2
     const uint32_t ex = rb & 0x7f800000u;
     // half the smaller gap next to r (2^e * 2^-24, or 2^-25 at a power of two)
     const float half_gap = __fmul_rn(__uint_as_float(ex), (rb & 0x7fffffu) ? 0x1p-24f : 0x1p-25f);
-    ok = ex >= (67u << 23) && ex < 0x7f800000u && __fadd_rn(fabsf(d), m) < half_gap;
+    ok = ex >= (67u << 23) && ex < 0x7f800000u && __fadd_rn(fabsf(d), m) < half_gap && fabsf(s2) <= 1.0f;
     return r;
 }
 
@@ -236,13 +243,17 @@ __device__ __forceinline__ void eq_ff_pair(float ph, float pl, float mk, float c
     const float b = __fmul_rn(4.5f, p), be = __fmaf_rn(4.5f, p, -b);       // B = 4.5 ct^2 = b + be + 4.5 pe
     const float bb = __fsub_rn(__fadd_rn(be, __fmul_rn(4.5f, pe)), c1e);   // low parts of B - C
     const float m = __fmul_rn(mk, __fadd_rn(__fadd_rn(c1p, fabsf(a)), b));
+    // A + B by the fast two-sum, exact for |A| >= B (|ct| up to about 2/3); otherwise FP64
+    const bool ab = fabsf(a) >= b;
     float s1, e1, s2, e2;
-    two_sum(a, b, s1, e1);
+    fast_two_sum(a, b, s1, e1);
     two_sum(s1, -c1, s2, e2);
     rp = ff_finish(ph, pl, m, s2, __fadd_rn(__fadd_rn(__fadd_rn(ae, bb), e1), e2), okp);
-    two_sum(-a, b, s1, e1);
+    fast_two_sum(-a, b, s1, e1);
     two_sum(s1, -c1, s2, e2);
     rn = ff_finish(ph, pl, m, s2, __fadd_rn(__fadd_rn(__fadd_rn(-ae, bb), e1), e2), okn);
+    okp = okp && ab;
+    okn = okn && ab;
 }
 
 __device__ __forceinline__ float eq_ff(float ph, float pl, float c1, float c1e, float ct, bool &ok) {
@@ -698,8 +709,10 @@ cudaError_t launch_gather(lbm_ctx *ctx, const StepArgs &a, int mode, double *for
     return finalize_sums(ctx->stream, g.partials, (int)nb, 3, ctx->force_acc_d, true, force_copy);
 }
 
-// Both equilibrium evaluations on n pseudo-random (rho, u) samples, all 27 directions: counts the
-// results that differ (out[0]) and the evaluations eq_fast settled by its FP64 fallback (out[1]).
+// Both equilibrium evaluations on n pseudo-random (rho, u) samples, all directions: counts the
+// float-float results accepted by their bound that differ from FP64 (out[0]; the single evaluator
+// and both signs of the pair evaluator), and the pair evaluations left to the FP64 fallback among
+// samples with |u| <= 0.3 (out[1]).
 __global__ void eq_selftest_kernel(int64_t n, uint64_t seed, unsigned long long *out) {
     unsigned long long bad = 0, fell = 0;
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
@@ -721,6 +734,19 @@ __global__ void eq_selftest_kernel(int64_t n, uint64_t seed, unsigned long long 
         const float uz = (2.0f * r[3] - 1.0f) * umax * ((s & 4) ? 1.0f : 0.0f);
         const float usq = (ux * ux) + (uy * uy) + (uz * uz);
         const float c1 = __fmul_rn(1.5f, usq), c1e = __fmaf_rn(1.5f, usq, -c1);
+        // the pair evaluator of the step, both signs
+        for (int i = 1; i < 27; ++i) {
+            const int k = wclass(i);
+            const float ph = __fmul_rn(kWhi(k), rho);
+            const float pl = __fmaf_rn(kWlo(k), rho, __fmaf_rn(kWhi(k), rho, -ph));
+            const float ct = __fadd_rn(__fadd_rn((float)c_dir[i][0] * ux, (float)c_dir[i][1] * uy), (float)c_dir[i][2] * uz);
+            float rp, rn;
+            bool okp, okn;
+            eq_ff_pair(ph, pl, __fmul_rn(fabsf(ph), 0x1p-42f), c1, c1e, __fadd_rn(1.0f, c1), ct, rp, okp, rn, okn);
+            bad += okp && __float_as_uint(rp) != __float_as_uint(eq_fp64(k, rho, ct, usq));
+            bad += okn && __float_as_uint(rn) != __float_as_uint(eq_fp64(k, rho, -ct, usq));
+            fell += !okp && (s & 3) != 0;  // fallbacks counted for |u| <= 0.3 (flows the method is used for)
+        }
         for (int i = 0; i < 27; ++i) {
             const int k = wclass(i);
             const float ph = __fmul_rn(kWhi(k), rho);
@@ -730,7 +756,6 @@ __global__ void eq_selftest_kernel(int64_t n, uint64_t seed, unsigned long long 
             const float a = eq_ff(ph, pl, c1, c1e, ct, ok);
             const float b = eq_fp64(k, rho, ct, usq);
             bad += ok && __float_as_uint(a) != __float_as_uint(b);
-            fell += !ok;
         }
     }
     atomicAdd(out, bad);
