@@ -191,7 +191,7 @@ LBM_API lbm_status lbm_set_equilibrium_evaluation(lbm_ctx *ctx, int32_t mode);
 /* Diagnostic: both evaluations on `samples` pseudo-random (rho, u) draws (|u| up to 2) x the 27
  * directions on `device`; out[0] = float-float results accepted by their bound that differ from
  * FP64 (must be 0), out[1] = direction pairs left to the FP64 fallback among the draws with
- * |u| <= 0.3. */
+ * |u| <= 0.05. */
 LBM_API lbm_status lbm_d3q27_equilibrium_selftest(int64_t samples, uint64_t seed, int32_t device, int64_t out[2]);
 /* Diagnostic: the D3Q27_REF step divides by tau with one correction of RN(x * RN(1/tau))
  * (Markstein 1990) where that equals the IEEE division; this counts, over all 2^32 float inputs x,

@@ -392,14 +392,15 @@ def test_set_order_switches_the_fused_step():
 
 # ------------------------------------------------------------------ equilibrium evaluation
 def test_equilibrium_selftest():
-    """The float-float equilibrium, wherever its error bound accepts it, equals the reference's
-    FP64 evaluation bit for bit, over 54 million evaluations with rho over 16 decades and |u| up
-    to 2; the FP64 fallback settles a small fraction."""
+    """The float-float equilibrium (the single and the pair evaluator), wherever its error bound
+    accepts it, equals the reference's FP64 evaluation bit for bit, over about 100 million
+    evaluations with rho over 16 decades and |u| up to 2; for low-Mach draws (|u| <= 0.05) the
+    FP64 fallback settles under 0.1 % of them."""
     import ctypes
     out = (ctypes.c_int64 * 2)()
     lbm.capi.check(lbm.capi.lib().lbm_d3q27_equilibrium_selftest(2_000_000, 20261203, 0, out))
     assert out[0] == 0, out[0]
-    assert out[1] < 2_000_000 * 0.75 * 26 * 1e-3, out[1]
+    assert out[1] < 2_000_000 * 0.5 * 26 * 1e-3, out[1]
 
 
 @pytest.mark.parametrize("order", [lbm.ORDER_STREAM_COLLIDE, lbm.ORDER_CLI])
