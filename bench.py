@@ -187,6 +187,32 @@ def dist_setup():
     return ws, rank, local
 
 
+def rank_helpers(dist, dev):
+    """barrier() and max_over_ranks(x) for the replicas of a multi-rank run (dist None: one rank).
+    The timed region of every rank is bracketed by barrier(); the reported time is the maximum of
+    the ranks' times."""
+    import torch
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    return barrier, max_over_ranks
+
+
+def whole_job_mlups(world_size, units_per_rank, seconds):
+    """Aggregate throughput of weak-scaled replicas: every rank updates units_per_rank cells in the
+    slowest rank's time."""
+    return world_size * units_per_rank / seconds / 1e6
+
+
 # ----------------------------------------------------------------------------- arms
 def run_reference(args):
     ws, rank, _ = dist_setup()
@@ -248,16 +274,7 @@ def run_mine(args):
     info = L.info()
     bpu = info["bytes_per_update"]
 
-    def barrier():
-        if dist:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier, max_over_ranks = rank_helpers(dist, dev)
 
     # ---------------- device-resident
     for _ in range(args.warmup):
@@ -277,7 +294,7 @@ def run_mine(args):
         barrier()
     t = max_over_ranks(e0.elapsed_time(e1) / 1000.0)
     launches = args.steps * args.lbm_steps
-    value = ws * args.steps * args.lbm_steps * cells / t / 1e6
+    value = whole_job_mlups(ws, args.steps * args.lbm_steps * cells, t)
     avg_launch = t / launches
     achieved = bpu * cells / avg_launch / 1e9
     peak, peak_kind = peaks()
@@ -310,7 +327,7 @@ def run_mine(args):
         barrier()
         te = max_over_ranks(max(x0.elapsed_time(x1) / 1000.0, 0.0))
         te = max(te, max_over_ranks(wall))
-        e2e = {"value": round(ws * args.steps * args.lbm_steps * cells / te / 1e6, 3), "unit": "MLUPS",
+        e2e = {"value": round(whole_job_mlups(ws, args.steps * args.lbm_steps * cells, te), 3), "unit": "MLUPS",
                "h2d_bytes_per_step": int(flags_h.nbytes + f0.nbytes), "d2h_bytes_per_step": int(sum(o.nbytes for o in outs)),
                "ms_per_step": round(1000 * te / args.steps, 3)}
 
