@@ -120,24 +120,68 @@ struct RawPack<16> {
     using T = uint4;
 };
 
+// Two 16-bit values converted together (packed conversions, the same values as one at a time)
+template <class S>
+struct Pair;
+template <>
+struct Pair<__half> {
+    using P = __half2;
+    static __device__ __forceinline__ float2 to(P v) { return __half22float2(v); }
+    static __device__ __forceinline__ P from(float a, float b) { return __floats2half2_rn(a, b); }
+};
+template <>
+struct Pair<__nv_bfloat16> {
+    using P = __nv_bfloat162;
+    static __device__ __forceinline__ float2 to(P v) { return __bfloat1622float2(v); }
+    static __device__ __forceinline__ P from(float a, float b) { return __floats2bfloat162_rn(a, b); }
+};
+
+// raw V-element pack -> arithmetic values, and back
+template <class S, int V, class T>
+__device__ __forceinline__ void unpack(const T &raw, typename Store<S>::R (&out)[V]) {
+    if constexpr (sizeof(S) == 2 && V % 2 == 0) {
+        typename Pair<S>::P e[V / 2];
+        memcpy(e, &raw, sizeof(raw));
+#pragma unroll
+        for (int k = 0; k < V / 2; ++k) {
+            const float2 f = Pair<S>::to(e[k]);
+            out[2 * k] = f.x;
+            out[2 * k + 1] = f.y;
+        }
+    } else {
+        S e[V];
+        memcpy(e, &raw, sizeof(raw));
+#pragma unroll
+        for (int k = 0; k < V; ++k) out[k] = Store<S>::to(e[k]);
+    }
+}
+template <class S, int V, class T>
+__device__ __forceinline__ void pack(const typename Store<S>::R (&in)[V], T &raw) {
+    if constexpr (sizeof(S) == 2 && V % 2 == 0) {
+        typename Pair<S>::P e[V / 2];
+#pragma unroll
+        for (int k = 0; k < V / 2; ++k) e[k] = Pair<S>::from(in[2 * k], in[2 * k + 1]);
+        memcpy(&raw, e, sizeof(raw));
+    } else {
+        S e[V];
+#pragma unroll
+        for (int k = 0; k < V; ++k) e[k] = Store<S>::from(in[k]);
+        memcpy(&raw, e, sizeof(raw));
+    }
+}
+
 template <class S, int V>
 __device__ __forceinline__ void ld_pack(const S *__restrict__ p, typename Store<S>::R (&out)[V]) {
     using T = typename RawPack<sizeof(S) * V>::T;
     const T raw = __ldg(reinterpret_cast<const T *>(p));
-    S e[V];
-    memcpy(e, &raw, sizeof(raw));
-#pragma unroll
-    for (int k = 0; k < V; ++k) out[k] = Store<S>::to(e[k]);
+    unpack<S, V>(raw, out);
 }
 
 template <class S, int V>
 __device__ __forceinline__ void st_pack(S *__restrict__ p, const typename Store<S>::R (&in)[V]) {
     using T = typename RawPack<sizeof(S) * V>::T;
-    S e[V];
-#pragma unroll
-    for (int k = 0; k < V; ++k) e[k] = Store<S>::from(in[k]);
     T raw;
-    memcpy(&raw, e, sizeof(raw));
+    pack<S, V>(in, raw);
     *reinterpret_cast<T *>(p) = raw;
 }
 
@@ -198,10 +242,7 @@ __device__ __forceinline__ void ld_pack_pol(const S *__restrict__ p, typename St
     } else {
         using T = typename RawPack<sizeof(S) * V>::T;
         const T raw = ld_hint<T>(reinterpret_cast<const T *>(p), pol);
-        S e[V];
-        memcpy(e, &raw, sizeof(raw));
-#pragma unroll
-        for (int k = 0; k < V; ++k) out[k] = Store<S>::to(e[k]);
+        unpack<S, V>(raw, out);
     }
 }
 
@@ -211,11 +252,8 @@ __device__ __forceinline__ void st_pack_pol(S *__restrict__ p, const typename St
         st_pack<S, V>(p, in);
     } else {
         using T = typename RawPack<sizeof(S) * V>::T;
-        S e[V];
-#pragma unroll
-        for (int k = 0; k < V; ++k) e[k] = Store<S>::from(in[k]);
         T raw;
-        memcpy(&raw, e, sizeof(raw));
+        pack<S, V>(in, raw);
         st_hint(reinterpret_cast<T *>(p), raw, pol);
     }
 }
@@ -351,10 +389,17 @@ template <class S, class R>
 __device__ __forceinline__ void conserve_rounding(R h[9]) {
     R r[5];
 #pragma unroll
-    for (int q = 0; q < 5; ++q) {
-        const R hr = Store<S>::to(Store<S>::from(h[q]));
-        r[q] = sub_(h[q], hr);
-        h[q] = hr;
+    for (int q = 0; q < 4; q += 2) {  // round trips two at a time
+        const float2 hr = Pair<S>::to(Pair<S>::from(h[q], h[q + 1]));
+        r[q] = sub_(h[q], hr.x);
+        r[q + 1] = sub_(h[q + 1], hr.y);
+        h[q] = hr.x;
+        h[q + 1] = hr.y;
+    }
+    {
+        const R hr = Store<S>::to(Store<S>::from(h[4]));
+        r[4] = sub_(h[4], hr);
+        h[4] = hr;
     }
     const R r0x4 = mul_((R)4, r[0]);
     h[5] = add_(h[5], fma_((R)2, add_(r[1], r[2]), r0x4));
