@@ -108,8 +108,13 @@ __global__ void __launch_bounds__(256) step_kernel(const S *__restrict__ src, S 
     d2q9::scalar_cell<S, I>(src, dst, links, x, y, nx, ny, pitch, plane, periodic, prm, FORCE);
 }
 
+// Minimum resident blocks of 256 threads per SM asked of the register allocator, per vector width:
+// 8-wide 16-bit vectors need their ~128 registers; narrower vectors trade a few spilled registers
+// for more resident warps, which measured faster (the step is latency-bound at low occupancy).
+__host__ __device__ constexpr int vec_min_blocks(int v) { return v == 8 ? 2 : 4; }
+
 template <class S, int V, bool FORCE, int POL>
-__global__ void __launch_bounds__(256) step_vec_kernel(const S *__restrict__ src, S *__restrict__ dst,
+__global__ void __launch_bounds__(256, vec_min_blocks(V)) step_vec_kernel(const S *__restrict__ src, S *__restrict__ dst,
                                                        const uint16_t *__restrict__ links, int nx, int ny,
                                                        int pitch, int plane, int periodic, D2Q9Params prm,
                                                        int reverse) {
