@@ -462,22 +462,8 @@ def run_batch(args):
 
 def _serial_plain(reqs, dtype="f32"):
     """Serial plain solves in real time: requests in arrival order, one single-domain context each,
-    each solved to completion before the next starts.  Returns latencies and (cell updates, makespan).
-    The launch-shape tuner is switched off (the default 4-cell, 64-thread shape, within a few per cent
-    of the tuned FP32 step), so that no solve pays a tuning run the served path does not pay."""
+    each solved to completion before the next starts.  Returns latencies and (cell updates, makespan)."""
     import latticeboltzmanncuda_gb300 as lbm
-    saved = os.environ.get("LBM_AUTOTUNE")
-    os.environ["LBM_AUTOTUNE"] = "0"
-    try:
-        return _serial_plain_run(lbm, reqs, dtype)
-    finally:
-        if saved is None:
-            os.environ.pop("LBM_AUTOTUNE", None)
-        else:
-            os.environ["LBM_AUTOTUNE"] = saved
-
-
-def _serial_plain_run(lbm, reqs, dtype):
     t0 = time.perf_counter()
     lat, work = [], 0.0
     for r in sorted(reqs, key=lambda r: r.arrival):
@@ -530,8 +516,7 @@ def run_serve(args):
             "data": "synthetic",
             "config": {"workload": f"Poisson arrivals for {args.serve_duration} s per rate, side 128-2048 log-uniform, "
                                    f"aspect 1-4, solid 0-30 %, tau 0.52-1.2, steps 1k-50k log-uniform, 150 GB budget, "
-                                   f"round {args.round_steps} steps, seed {SEED}; plain solves with the default "
-                                   f"launch shape (no per-solve tuning)"},
+                                   f"round {args.round_steps} steps, seed {SEED}"},
             "sweep": [{k: (round(v, 4) if isinstance(v, float) else
                            ({kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()}
                             if isinstance(v, dict) else v)) for k, v in r.items()} for r in sweep]}
