@@ -121,7 +121,8 @@ struct lbm_batch {
     Tile *tiles_d = nullptr;
     size_t tiles_cap = 0;
     int ntiles = 0;
-    bool dirty = true;
+    bool dirty = true;        // descriptors need rewriting
+    bool tiles_dirty = true;  // the live set or the tile shape changed: the tile list too
     // tile shape
     int v = 4, tx = 32, ty = 4;
     bool tuned = false;
@@ -192,17 +193,31 @@ struct CtxView {
     }
 };
 
+// Slot buffers come from the device's stream-ordered memory pool on the batch stream: freeing a
+// slot does not synchronise the device (its memory returns to the pool once the work queued before
+// the free has run), and a later slot reuses the pooled memory without a new device allocation.
+void free_slot(lbm_batch *b, Slot &s) {
+    for (void *p : {(void *)s.f[0], (void *)s.f[1], (void *)s.links, (void *)s.flags})
+        if (p) cudaFreeAsync(p, b->stream);
+    s.f[0] = s.f[1] = nullptr;
+    s.links = nullptr;
+    s.flags = nullptr;
+}
+
 // steps slot s takes in a launch sequence of nsteps
 int64_t advance_of(const Slot &s, int64_t nsteps) { return s.limit < 0 ? nsteps : std::min(nsteps, s.limit); }
 
-// Descriptors and tiles for a launch sequence of nsteps (slots with a step budget stop early;
-// slots with no steps left get no tiles).
+// Descriptors and tiles for a launch sequence of nsteps.  The tile list changes only with the live
+// set or the shape (b->tiles_dirty); the descriptors carry each slot's stop step (slots with a step
+// budget stop early) and are rewritten for every launch sequence while some slot has a budget.
+// Tiles of a slot whose budget is used up stay in the list: their blocks return at once.
 lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
     bool limited = false;
     for (const Slot &s : b->slots) limited |= s.live && s.limit >= 0;
-    if (!b->dirty && !limited) return LBM_OK;
+    if (!b->dirty && !b->tiles_dirty && !limited) return LBM_OK;
     std::vector<SlotDesc> descs(b->slots.size());
     std::vector<Tile> tiles;
+    const bool retile = b->tiles_dirty;
     for (size_t i = 0; i < b->slots.size(); ++i) {
         const Slot &s = b->slots[i];
         SlotDesc &d = descs[i];
@@ -222,7 +237,7 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
         d.force = (s.desc.body_force[0] != 0.0f || s.desc.body_force[1] != 0.0f) ? 1 : 0;
         d.cur = s.cur;
         d.prm = d2q9_params(s.desc);
-        if (adv <= 0) continue;
+        if (!retile) continue;
         const int chunks = (s.pitch / b->v + b->tx - 1) / b->tx;
         for (int y0 = 0; y0 < s.desc.ny; y0 += b->ty)
             for (int xc = 0; xc < chunks; ++xc) tiles.push_back(Tile{(int)i, xc, y0, 0});
@@ -234,7 +249,7 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
         b->desc_cap = std::max<size_t>(descs.size(), 64);
         BCUDA(b, cudaMalloc(&b->desc_d, b->desc_cap * sizeof(SlotDesc)), "batch: descriptor table");
     }
-    if (tiles.size() > b->tiles_cap) {
+    if (retile && tiles.size() > b->tiles_cap) {
         if (b->tiles_d) cudaFree(b->tiles_d);
         b->tiles_d = nullptr;
         b->tiles_cap = std::max<size_t>(tiles.size() + tiles.size() / 4, 1024);
@@ -243,11 +258,14 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
     if (!descs.empty())
         BCUDA(b, cudaMemcpy(b->desc_d, descs.data(), descs.size() * sizeof(SlotDesc), cudaMemcpyHostToDevice),
               "batch: upload descriptors");
-    if (!tiles.empty())
-        BCUDA(b, cudaMemcpy(b->tiles_d, tiles.data(), tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice),
-              "batch: upload tiles");
-    b->ntiles = (int)tiles.size();
+    if (retile) {
+        if (!tiles.empty())
+            BCUDA(b, cudaMemcpy(b->tiles_d, tiles.data(), tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice),
+                  "batch: upload tiles");
+        b->ntiles = (int)tiles.size();
+    }
     b->dirty = false;
+    b->tiles_dirty = false;
     return LBM_OK;
 }
 
@@ -308,6 +326,7 @@ lbm_status tune(lbm_batch *b) {
         b->tx = c.tx;
         b->ty = c.ty;
         b->dirty = true;
+        b->tiles_dirty = true;
         lbm_status st = rebuild(b, 1);
         if (st != LBM_OK) return st;
         if (b->ntiles == 0) break;
@@ -330,6 +349,7 @@ lbm_status tune(lbm_batch *b) {
     b->tx = pick.tx;
     b->ty = pick.ty;
     b->dirty = true;
+    b->tiles_dirty = true;
     b->tuned = true;
     return LBM_OK;
 }
@@ -375,6 +395,14 @@ LBM_API lbm_status lbm_batch_create(int32_t dtype, int32_t device, void *stream,
         delete b;
         return lbm::set_thread_error(LBM_ERR_CUDA, std::string("lbm_batch_create: ") + cudaGetErrorString(e));
     }
+    // keep freed slot memory in the device's pool between requests instead of returning it to the
+    // driver at every synchronisation
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
     b->v = dtype == LBM_F64 ? 2 : 4;
     *out = b;
     return LBM_OK;
@@ -383,14 +411,9 @@ LBM_API lbm_status lbm_batch_create(int32_t dtype, int32_t device, void *stream,
 LBM_API lbm_status lbm_batch_destroy(lbm_batch *b) {
     if (!b) return LBM_OK;
     cudaSetDevice(b->device);
+    for (Slot &s : b->slots)
+        if (s.live) free_slot(b, s);
     if (b->stream) cudaStreamSynchronize(b->stream);
-    for (Slot &s : b->slots) {
-        if (!s.live) continue;
-        cudaFree(s.f[0]);
-        cudaFree(s.f[1]);
-        cudaFree(s.links);
-        cudaFree(s.flags);
-    }
     cudaFree(b->desc_d);
     cudaFree(b->tiles_d);
     cudaFree(b->staging);
@@ -425,15 +448,13 @@ LBM_API lbm_status lbm_batch_add(lbm_batch *b, const lbm_desc *desc, const uint8
     const size_t pop = (size_t)s.plane * 9 * dsize(b->dtype);
     s.bytes = (size_t)lbm_batch_slot_bytes(b->dtype, desc->nx, desc->ny);
     auto cleanup = [&]() {
-        cudaFree(s.f[0]);
-        cudaFree(s.f[1]);
-        cudaFree(s.links);
-        cudaFree(s.flags);
+        free_slot(b, s);
+        cudaStreamSynchronize(b->stream);
     };
-    cudaError_t e = cudaMalloc(&s.f[0], pop);
-    if (e == cudaSuccess) e = cudaMalloc(&s.f[1], pop);
-    if (e == cudaSuccess) e = cudaMalloc(&s.links, (size_t)s.plane * sizeof(uint16_t));
-    if (e == cudaSuccess) e = cudaMalloc(&s.flags, (size_t)desc->nx * desc->ny);
+    cudaError_t e = cudaMallocAsync(&s.f[0], pop, b->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(&s.f[1], pop, b->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(&s.links, (size_t)s.plane * sizeof(uint16_t), b->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(&s.flags, (size_t)desc->nx * desc->ny, b->stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
         cleanup();
@@ -480,6 +501,7 @@ LBM_API lbm_status lbm_batch_add(lbm_batch *b, const lbm_desc *desc, const uint8
     b->slots[id] = s;
     b->device_bytes += (int64_t)s.bytes;
     b->dirty = true;
+    b->tiles_dirty = true;
     *slot_out = id;
     return LBM_OK;
 }
@@ -487,14 +509,11 @@ LBM_API lbm_status lbm_batch_add(lbm_batch *b, const lbm_desc *desc, const uint8
 LBM_API lbm_status lbm_batch_remove(lbm_batch *b, int32_t slot) {
     Slot *s = get_slot(b, slot);
     if (!s) return bfail(b, LBM_ERR_INVALID, "lbm_batch_remove: no such slot");
-    BCUDA(b, cudaStreamSynchronize(b->stream), "lbm_batch_remove: synchronize");
-    cudaFree(s->f[0]);
-    cudaFree(s->f[1]);
-    cudaFree(s->links);
-    cudaFree(s->flags);
+    free_slot(b, *s);  // ordered after the queued steps that may still read the slot
     b->device_bytes -= (int64_t)s->bytes;
     *s = Slot();
     b->dirty = true;
+    b->tiles_dirty = true;
     return LBM_OK;
 }
 
@@ -508,6 +527,7 @@ LBM_API lbm_status lbm_batch_set_launch(lbm_batch *b, int32_t cells_per_thread, 
     b->ty = rows_per_block;
     b->tuned = true;
     b->dirty = true;
+    b->tiles_dirty = true;
     return LBM_OK;
 }
 
