@@ -48,6 +48,30 @@ __device__ __forceinline__ double fma_(double a, double b, double c) { return __
 __device__ __forceinline__ double mul_(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double add_(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub_(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float neg_(float a) { return -a; }
+__device__ __forceinline__ double neg_(double a) { return -a; }
+
+// Two cells at once on the packed FP32 pipe of sm_100+ (FFMA2 / FADD2 / FMUL2): every lane gets the
+// same IEEE round-to-nearest result as the scalar intrinsic, so a packed update is bit-identical to
+// two scalar ones while issuing half the arithmetic instructions.  a - b is computed as a + (-b),
+// which is the same IEEE value.
+__device__ __forceinline__ float2 fma_(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul_(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add_(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 neg_(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 sub_(float2 a, float2 b) { return __fadd2_rn(a, neg_(b)); }
+
+// lane type of an arithmetic type, and a uniform value broadcast to every lane
+template <class T>
+struct Lane {
+    using R = T;
+    static __device__ __forceinline__ T bc(R c) { return c; }
+};
+template <>
+struct Lane<float2> {
+    using R = float;
+    static __device__ __forceinline__ float2 bc(float c) { return make_float2(c, c); }
+};
 
 // storage traits: S is the stored type, R the arithmetic type; `to` / `from` convert raw values
 template <class S>
@@ -335,14 +359,15 @@ __device__ __forceinline__ void gather(const S *__restrict__ src, uint32_t L, in
 }
 
 // density deviation and momentum of populations in storage space
-template <class S, class R>
-__device__ __forceinline__ void moments(const R h[9], R &drho, R &mx, R &my) {
+template <class S, class T>
+__device__ __forceinline__ void moments(const T h[9], T &drho, T &mx, T &my) {
+    using R = typename Lane<T>::R;
     constexpr R s = hscale<S, R>();
-    const R w0 = w<R>(0) / s, ws = w<R>(1) / s, wd = w<R>(5) / s;
-    const R sf = add_(add_(h[1], h[3]), add_(h[2], h[4]));
-    const R sd = add_(add_(h[5], h[7]), add_(h[6], h[8]));
+    const T w0 = Lane<T>::bc(w<R>(0) / s), ws = Lane<T>::bc(w<R>(1) / s), wd = Lane<T>::bc(w<R>(5) / s);
+    const T sf = add_(add_(h[1], h[3]), add_(h[2], h[4]));
+    const T sd = add_(add_(h[5], h[7]), add_(h[6], h[8]));
     drho = fma_(wd, sd, fma_(ws, sf, mul_(w0, h[0])));
-    const R d57 = sub_(h[5], h[7]), d86 = sub_(h[8], h[6]);
+    const T d57 = sub_(h[5], h[7]), d86 = sub_(h[8], h[6]);
     mx = fma_(wd, add_(d57, d86), mul_(ws, sub_(h[1], h[3])));
     my = fma_(wd, sub_(d57, d86), mul_(ws, sub_(h[2], h[4])));
 }
@@ -352,6 +377,8 @@ template <class R>
 __device__ __forceinline__ R recip(R rho) {
     if constexpr (std::is_same<R, float>::value)
         return __fdividef(1.0f, rho);
+    else if constexpr (std::is_same<R, float2>::value)
+        return make_float2(__fdividef(1.0f, rho.x), __fdividef(1.0f, rho.y));
     else
         return __ddiv_rn(1.0, rho);
 }
@@ -385,27 +412,34 @@ struct is_half_store<__nv_bfloat16> : std::true_type {};
 // (h = s f / w, w_0 = 16 w_d, w_axis = 4 w_d) is  h_d += 4 r_0 + 2 (r_a + r_b)  with a, b the axis
 // populations with c_a + c_b = c_d.  What remains is the diagonals' own rounding, whose absolute
 // resolution is 4x (momentum) and 16x (mass) finer.
-template <class S, class R>
-__device__ __forceinline__ void conserve_rounding(R h[9]) {
-    R r[5];
+template <class S, class T>
+__device__ __forceinline__ void conserve_rounding(T h[9]) {
+    T r[5];
+    if constexpr (std::is_same<T, float2>::value) {
 #pragma unroll
-    for (int q = 0; q < 4; q += 2) {  // round trips two at a time
-        const float2 hr = Pair<S>::to(Pair<S>::from(h[q], h[q + 1]));
-        r[q] = sub_(h[q], hr.x);
-        r[q + 1] = sub_(h[q + 1], hr.y);
-        h[q] = hr.x;
-        h[q + 1] = hr.y;
-    }
-    {
-        const R hr = Store<S>::to(Store<S>::from(h[4]));
+        for (int q = 0; q < 5; ++q) {  // the two cells' values of population q round-trip together
+            const float2 hr = Pair<S>::to(Pair<S>::from(h[q].x, h[q].y));
+            r[q] = sub_(h[q], hr);
+            h[q] = hr;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 4; q += 2) {  // round trips two at a time
+            const float2 hr = Pair<S>::to(Pair<S>::from(h[q], h[q + 1]));
+            r[q] = sub_(h[q], hr.x);
+            r[q + 1] = sub_(h[q + 1], hr.y);
+            h[q] = hr.x;
+            h[q + 1] = hr.y;
+        }
+        const T hr = Store<S>::to(Store<S>::from(h[4]));
         r[4] = sub_(h[4], hr);
         h[4] = hr;
     }
-    const R r0x4 = mul_((R)4, r[0]);
-    h[5] = add_(h[5], fma_((R)2, add_(r[1], r[2]), r0x4));
-    h[6] = add_(h[6], fma_((R)2, add_(r[2], r[3]), r0x4));
-    h[7] = add_(h[7], fma_((R)2, add_(r[3], r[4]), r0x4));
-    h[8] = add_(h[8], fma_((R)2, add_(r[4], r[1]), r0x4));
+    const T two = Lane<T>::bc(2), r0x4 = mul_(Lane<T>::bc(4), r[0]);
+    h[5] = add_(h[5], fma_(two, add_(r[1], r[2]), r0x4));
+    h[6] = add_(h[6], fma_(two, add_(r[2], r[3]), r0x4));
+    h[7] = add_(h[7], fma_(two, add_(r[3], r[4]), r0x4));
+    h[8] = add_(h[8], fma_(two, add_(r[4], r[1]), r0x4));
 }
 
 // BGK collision with Guo forcing, in place, in storage space.  Opposite populations q, q' share
@@ -413,44 +447,51 @@ __device__ __forceinline__ void conserve_rounding(R h[9]) {
 // A and an antisymmetric part B per pair: h_q <- (1 - om) h_q + A + B, h_q' <- (1 - om) h_q' + A - B,
 //   A = om s (drho + rho (4.5 cu^2 - 1.5 u^2)) + s (1 - om/2) (9 cu cF - 3 u.F)
 //   B = 3 om s rho cu + 3 s (1 - om/2) cF
-template <class S, class R, bool FORCE>
-__device__ __forceinline__ void collide(R h[9], R om, Vec2<R> F) {
+// T is the scalar arithmetic type R, or float2 for two cells at once (uniform quantities -- omega,
+// the force and what depends only on them -- are computed in R and broadcast, which gives every
+// lane the scalar path's values).
+template <class S, class T, bool FORCE>
+__device__ __forceinline__ void collide_t(T h[9], typename Lane<T>::R om, Vec2<typename Lane<T>::R> F) {
+    using R = typename Lane<T>::R;
+    auto B = [](R c) { return Lane<T>::bc(c); };
     constexpr R s = hscale<S, R>();
-    R drho, mx, my;
-    moments<S, R>(h, drho, mx, my);
-    const R rho = add_((R)1, drho);
-    const R inv = recip(rho);
-    R ux, uy;
+    T drho, mx, my;
+    moments<S, T>(h, drho, mx, my);
+    const T rho = add_(B((R)1), drho);
+    const T inv = recip(rho);
+    T ux, uy;
     if (FORCE) {
-        ux = mul_(fma_((R)0.5, F.x, mx), inv);
-        uy = mul_(fma_((R)0.5, F.y, my), inv);
+        ux = mul_(fma_(B((R)0.5), B(F.x), mx), inv);
+        uy = mul_(fma_(B((R)0.5), B(F.y), my), inv);
     } else {
         ux = mul_(mx, inv);
         uy = mul_(my, inv);
     }
-    const R usq = mul_((R)1.5, fma_(ux, ux, mul_(uy, uy)));
-    const R om1 = sub_((R)1, om);
-    const R om_s_drho = mul_(om, mul_(s, drho));
-    const R om_s_rho = mul_(om, mul_(s, rho));
-    const R om_s_rho3 = mul_((R)3, om_s_rho);
-    R pre = 0, pre3 = 0, uF3 = 0;
+    const T usq = mul_(B((R)1.5), fma_(ux, ux, mul_(uy, uy)));
+    const T om1 = B(sub_((R)1, om));
+    const T omv = B(om);
+    const T om_s_drho = mul_(omv, mul_(B(s), drho));
+    const T om_s_rho = mul_(omv, mul_(B(s), rho));
+    const T om_s_rho3 = mul_(B((R)3), om_s_rho);
+    R pre = 0, pre3 = 0;
+    T uF3 = B((R)0);
     if (FORCE) {
         pre = mul_(s, fma_((R)-0.5, om, (R)1));
         pre3 = mul_((R)3, pre);
-        uF3 = mul_((R)3, fma_(ux, F.x, mul_(uy, F.y)));
+        uF3 = mul_(B((R)3), fma_(ux, B(F.x), mul_(uy, B(F.y))));
     }
     // rest population: h0eq = s (drho - rho usq), forcing s (1 - om/2) (-3 u.F)
     {
-        R a = fma_(-om_s_rho, usq, om_s_drho);
-        if (FORCE) a = fma_(-pre, uF3, a);
+        T a = fma_(neg_(om_s_rho), usq, om_s_drho);
+        if (FORCE) a = fma_(B(-pre), uF3, a);
         h[0] = fma_(om1, h[0], a);
     }
-    auto pair = [&](int q, int qb, R cu, R cF) {
-        R a = fma_(om_s_rho, fma_(mul_((R)4.5, cu), cu, -usq), om_s_drho);
-        R b = mul_(om_s_rho3, cu);
+    auto pair = [&](int q, int qb, T cu, R cF) {
+        T a = fma_(om_s_rho, fma_(mul_(B((R)4.5), cu), cu, neg_(usq)), om_s_drho);
+        T b = mul_(om_s_rho3, cu);
         if (FORCE) {
-            a = fma_(pre, fma_(mul_((R)9, cu), cF, -uF3), a);
-            b = fma_(pre3, cF, b);
+            a = fma_(B(pre), fma_(mul_(B((R)9), cu), B(cF), neg_(uF3)), a);
+            b = fma_(B(pre3), B(cF), b);
         }
         h[q] = fma_(om1, h[q], add_(a, b));
         h[qb] = fma_(om1, h[qb], sub_(a, b));
@@ -459,7 +500,12 @@ __device__ __forceinline__ void collide(R h[9], R om, Vec2<R> F) {
     pair(2, 4, uy, F.y);
     pair(5, 7, add_(ux, uy), add_(F.x, F.y));
     pair(8, 6, sub_(ux, uy), sub_(F.x, F.y));
-    if constexpr (is_half_store<S>::value) conserve_rounding<S, R>(h);
+    if constexpr (is_half_store<S>::value) conserve_rounding<S, T>(h);
+}
+
+template <class S, class R, bool FORCE>
+__device__ __forceinline__ void collide(R h[9], R om, Vec2<R> F) {
+    collide_t<S, R, FORCE>(h, om, F);
 }
 
 }  // namespace d2q9

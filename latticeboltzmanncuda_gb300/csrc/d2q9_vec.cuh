@@ -136,14 +136,30 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
         for (int k = 0; k < V; ++k) solid_any |= L[k] == LINK_SOLID;
     }
 
+    if constexpr (std::is_same<R, float>::value && V % 2 == 0) {
+        // FP32 arithmetic: cells k and k + 1 collide together on the packed FP32 pipe
 #pragma unroll
-    for (int k = 0; k < V; ++k) {
-        R h[9];
+        for (int k = 0; k < V; k += 2) {
+            float2 h[9];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) h[q] = f[q][k];
-        collide<S, R, FORCE>(h, omega<R>(prm), force<R>(prm));
+            for (int q = 0; q < 9; ++q) h[q] = make_float2(f[q][k], f[q][k + 1]);
+            collide_t<S, float2, FORCE>(h, omega<R>(prm), force<R>(prm));
 #pragma unroll
-        for (int q = 0; q < 9; ++q) f[q][k] = h[q];
+            for (int q = 0; q < 9; ++q) {
+                f[q][k] = h[q].x;
+                f[q][k + 1] = h[q].y;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < V; ++k) {
+            R h[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) h[q] = f[q][k];
+            collide<S, R, FORCE>(h, omega<R>(prm), force<R>(prm));
+#pragma unroll
+            for (int q = 0; q < 9; ++q) f[q][k] = h[q];
+        }
     }
 
     if (x0 >= nx) return;  // vector entirely in the row padding
