@@ -216,10 +216,12 @@ LBM_API lbm_status lbm_step_force_series(lbm_ctx *ctx, int32_t nsteps, float *ho
  * caches); lbm_set_launch() fixes a shape (cells_per_thread in 1,2,4,8; block_threads a multiple of
  * 32; block_threads * rows_per_block <= 256) and the L2 eviction hints of the vectorised path
  * (l2_policy 0: none; 1: loads evict-first, stores evict-last; 2: loads evict-first; the scalar
- * path, cells_per_thread 1, takes 0 only).  cells_per_thread 0 selects the shared-memory row
- * sweep of FP16/BF16 storage: blocks of block_threads = 128 threads each sweep a strip of 512
- * cells over rows_per_block rows (1 .. 1024), staging source rows through shared memory with
- * asynchronous copies; for it l2_policy selects the ring depth (0: 4 rows, 1: 8 rows). */
+ * path, cells_per_thread 1, takes 0 only).  cells_per_thread 0 selects the bulk-copy pipeline of
+ * FP16/BF16 storage: persistent blocks of block_threads = 160 threads (rows_per_block = 1), one
+ * warp staging the populations each row of a 512-cell strip pulls into a ring of shared-memory
+ * slots with cp.async.bulk, four warps updating the rows; for it l2_policy selects the ring (0: 4
+ * slots and 5 blocks per SM, 1: 4 slots and 4 blocks, 2: 6 slots and 3 blocks).  Its waits are
+ * bounded: if one gives up, the next call that synchronises the context returns LBM_ERR_TIMEOUT. */
 LBM_API lbm_status lbm_autotune(lbm_ctx *ctx, int32_t retune);
 LBM_API lbm_status lbm_set_launch(lbm_ctx *ctx, int32_t cells_per_thread, int32_t block_threads,
                                   int32_t rows_per_block, int32_t l2_policy);

@@ -63,6 +63,14 @@ lbm_status ensure_staging(lbm_ctx *ctx, size_t bytes) {
 
 lbm_status sync(lbm_ctx *ctx, const char *what) {
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream), what);
+    if (ctx->pipe_used) {
+        ctx->pipe_used = false;
+        const unsigned bits = d2q9_take_pipe_status(ctx);
+        if (bits)
+            return fail(ctx, LBM_ERR_TIMEOUT,
+                        std::string(what) + ": a bounded wait of the D2Q9 bulk-copy pipeline gave up; the populations "
+                                            "of the steps since the last synchronisation are not valid");
+    }
     return LBM_OK;
 }
 
@@ -240,7 +248,10 @@ LBM_API lbm_status lbm_create(const lbm_desc *desc, lbm_ctx **out) {
             return bail(set_thread_error(st, ctx->err));
         if ((st = dalloc(ctx, (void **)&ctx->links_d, (size_t)ctx->plane * sizeof(uint16_t), "links")) != LBM_OK)
             return bail(set_thread_error(st, ctx->err));
+        if ((st = dalloc(ctx, (void **)&ctx->pipe_status_d, 16, "pipeline status")) != LBM_OK)
+            return bail(set_thread_error(st, ctx->err));
         cudaError_t e = cudaMemsetAsync(ctx->flags_d, 0, (size_t)ctx->cells, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->pipe_status_d, 0, 16, ctx->stream);
         // link words of the row padding stay 0 (the vectorised step reads them)
         if (e == cudaSuccess) e = cudaMemsetAsync(ctx->links_d, 0, (size_t)ctx->plane * sizeof(uint16_t), ctx->stream);
         if (e == cudaSuccess) e = d2q9_build_links(ctx);
@@ -285,6 +296,7 @@ LBM_API lbm_status lbm_destroy(lbm_ctx *ctx) {
     for (int b = 0; b < 2; ++b) cudaFree(ctx->f[b]);
     cudaFree(ctx->flags_d);
     cudaFree(ctx->links_d);
+    cudaFree(ctx->pipe_status_d);
     cudaFree(ctx->tgt_cells_d);
     cudaFree(ctx->tgt_off_d);
     cudaFree(ctx->entries_d);

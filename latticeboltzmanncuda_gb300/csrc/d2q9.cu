@@ -25,7 +25,7 @@
 
 #include "lbm_internal.h"
 #include "d2q9_core.cuh"
-#include "d2q9_stage.cuh"
+#include "d2q9_bulk.cuh"
 #include "d2q9_vec.cuh"
 #include "reduce.cuh"
 
@@ -125,35 +125,68 @@ __global__ void __launch_bounds__(256, vec_min_blocks(V)) step_vec_kernel(const 
     d2q9::step_vec<S, V, FORCE, int, POL>(src, dst, links, x0, y, nx, ny, pitch, plane, periodic, prm);
 }
 
-// 16-bit storage: block (bx, by) sweeps strip bx (cells bx*W .. bx*W+W-1) over rows
-// [by*rows, by*rows + rows); with `reverse` the blocks take the strips and row runs in reverse order.
-template <class S, bool FORCE, int NSLOT>
-__global__ void __launch_bounds__(d2q9::stage::THREADS) stage_kernel(const S *__restrict__ src, S *__restrict__ dst,
-                                                                    const uint16_t *__restrict__ links, int nx, int ny,
-                                                                    int pitch, int plane, int periodic, D2Q9Params prm,
-                                                                    int rows, int reverse) {
-    extern __shared__ __align__(16) uint16_t ring[];
-    const int bx = reverse ? (int)(gridDim.x - 1 - blockIdx.x) : (int)blockIdx.x;
-    const int by = reverse ? (int)(gridDim.y - 1 - blockIdx.y) : (int)blockIdx.y;
-    const int ya = by * rows;
-    d2q9::stage::sweep<S, FORCE, NSLOT>(ring, src, dst, links, bx * d2q9::stage::W, ya, min(ya + rows, ny), nx, ny,
-                                        pitch, plane, periodic, prm);
+// 16-bit storage: the bulk-copy pipeline (d2q9_bulk.cuh), persistent blocks over (strip, row) tasks
+template <class S, int V, bool FORCE, int K, int MINB>
+__global__ void __launch_bounds__(d2q9::bulk::threads<V>(), MINB)
+    bulk_kernel(const S *__restrict__ src, S *__restrict__ dst, const uint16_t *__restrict__ links, int nx, int ny,
+                int pitch, int plane, int periodic, D2Q9Params prm, int reverse, unsigned *status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    d2q9::bulk::pipeline<S, V, FORCE, K>(smem, src, dst, links, nx, ny, pitch, plane, periodic, prm, reverse, status);
 }
 
-// launch the row sweep with a ring of NSLOT slots (dynamic shared memory beyond 48 KB is opted in
-// on the current device before the launch)
-template <class S, bool FORCE, int NSLOT>
-cudaError_t launch_stage(dim3 grid, cudaStream_t st, const S *src, S *dst, const uint16_t *links, int nx, int ny,
-                         int pitch, int plane, int periodic, const D2Q9Params &prm, int rows, int reverse) {
-    constexpr size_t bytes = d2q9::stage::ring_bytes<NSLOT>();
-    if (bytes > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(stage_kernel<S, FORCE, NSLOT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)bytes);
-        if (e != cudaSuccess) return e;
+// Resident blocks of a kernel per SM times the SMs of `device` (cached per kernel and device).
+int resident_blocks(const void *kernel, int threads, size_t smem, int device) {
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, int> cache;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find({kernel, device});
+    if (it != cache.end()) return it->second;
+    int per_sm = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+        return 0;
+    return cache[{kernel, device}] = std::max(1, per_sm) * sms;
+}
+
+// launch the bulk-copy pipeline (V cells per consumer thread) with a ring of K slots, registers
+// bounded for MINB blocks per SM (the dynamic shared memory is opted in once per kernel and
+// device); one persistent block per resident slot, at most one per task
+template <class S, int V, bool FORCE, int K, int MINB>
+cudaError_t launch_bulk(const lbm_ctx *ctx, const S *src, S *dst, int reverse) {
+    namespace B = d2q9::bulk;
+    constexpr size_t bytes = B::smem_bytes<K>();
+    constexpr int threads = B::threads<V>();
+    auto kern = bulk_kernel<S, V, FORCE, K, MINB>;
+    static std::mutex mu;
+    static unsigned long long opted = 0;  // devices on which the attribute is set
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!(opted >> (ctx->device & 63) & 1ull)) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            if (e != cudaSuccess) return e;
+            opted |= 1ull << (ctx->device & 63);
+        }
     }
-    stage_kernel<S, FORCE, NSLOT><<<grid, d2q9::stage::THREADS, bytes, st>>>(src, dst, links, nx, ny, pitch, plane,
-                                                                               periodic, prm, rows, reverse);
+    const lbm_desc &d = ctx->desc;
+    const int pitch = (int)ctx->pitch, plane = (int)ctx->plane;
+    const int ntasks = ((pitch + B::W - 1) / B::W) * d.ny;
+    const int resident = resident_blocks(reinterpret_cast<const void *>(kern), threads, bytes, ctx->device);
+    if (resident <= 0) return cudaErrorInvalidConfiguration;
+    const int grid = std::min(ntasks, resident);
+    const_cast<lbm_ctx *>(ctx)->pipe_used = true;
+    kern<<<grid, threads, bytes, ctx->stream>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic,
+                                                d2q9_params(d), reverse, ctx->pipe_status_d);
     return cudaGetLastError();
+}
+
+// pipeline variants (4 cells per consumer thread; 2 measured slower on the FP16 channel, 78-88k
+// against 96-104k MLUPS): pol selects the ring depth and the register bound (0: 4 slots, 5 blocks
+// per SM; 1: 4 slots, 4 blocks; 2: 6 slots, 3 blocks)
+template <class S, bool FORCE>
+cudaError_t launch_bulk_variant(const lbm_ctx *ctx, int pol, const S *src, S *dst, int reverse) {
+    if (pol == 0) return launch_bulk<S, 4, FORCE, 4, 5>(ctx, src, dst, reverse);
+    if (pol == 1) return launch_bulk<S, 4, FORCE, 4, 4>(ctx, src, dst, reverse);
+    return launch_bulk<S, 4, FORCE, 6, 3>(ctx, src, dst, reverse);
 }
 
 template <class S>
@@ -326,16 +359,10 @@ cudaError_t launch_one(lbm_ctx *ctx, const Shape &sh, const S *src, S *dst, int 
         return cudaGetLastError();
     }
     const int pitch = (int)ctx->pitch, plane = (int)ctx->plane;
-    if (sh.v == 0) {  // row sweep; pol selects the ring depth: 0 -> 4 slots, 1 -> 8 slots
-        if constexpr (sizeof(S) == 2) {
-            const dim3 sgrid((unsigned)((d.nx + d2q9::stage::W - 1) / d2q9::stage::W), (unsigned)((d.ny + sh.ty - 1) / sh.ty));
-            const uint16_t *L = ctx->links_d;
-            if (sh.pol == 1)
-                return force ? launch_stage<S, true, 8>(sgrid, st, src, dst, L, d.nx, d.ny, pitch, plane, d.periodic, prm, sh.ty, reverse)
-                             : launch_stage<S, false, 8>(sgrid, st, src, dst, L, d.nx, d.ny, pitch, plane, d.periodic, prm, sh.ty, reverse);
-            return force ? launch_stage<S, true, 4>(sgrid, st, src, dst, L, d.nx, d.ny, pitch, plane, d.periodic, prm, sh.ty, reverse)
-                         : launch_stage<S, false, 4>(sgrid, st, src, dst, L, d.nx, d.ny, pitch, plane, d.periodic, prm, sh.ty, reverse);
-        }
+    if (sh.v == 0) {  // bulk-copy pipeline
+        if constexpr (sizeof(S) == 2)
+            return force ? launch_bulk_variant<S, true>(ctx, sh.pol, src, dst, reverse)
+                         : launch_bulk_variant<S, false>(ctx, sh.pol, src, dst, reverse);
         return cudaErrorInvalidValue;
     }
 #define LBM_VEC_LAUNCH(VV, PP)                                                                                  \
@@ -362,8 +389,8 @@ template <class S>
 std::vector<Shape> candidates(const lbm_ctx *ctx) {
     std::vector<Shape> c = {{1, 256, 1, 0}, {1, 128, 2, 0}};
     if (!small_index(ctx)) return c;
-    if (sizeof(S) == 2)  // the shared-memory row sweep, short runs with a ring of 4 (the fastest measured)
-        for (int rows : {4, 8}) c.push_back({0, d2q9::stage::THREADS, rows, 0});
+    if (sizeof(S) == 2)  // the bulk-copy pipeline
+        for (int pol : {0, 1, 2}) c.push_back({0, d2q9::bulk::threads<4>(), 1, pol});
     for (int v : {2, 4, 8}) {
         if (!vec_ok<S>(v) || ctx->pitch % v) continue;
         const int per_row = (int)(ctx->pitch / v);
@@ -474,6 +501,7 @@ cudaError_t tune(lbm_ctx *ctx) {
         if (err != cudaSuccess) break;
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, e0, e1);
+        if (sh.v == 0 && d2q9_take_pipe_status(ctx) != 0) continue;  // a bounded wait gave up: not a candidate
         if (ms < best) {
             best = ms;
             pick = sh;
@@ -555,9 +583,10 @@ cudaError_t d2q9_init_equilibrium(lbm_ctx *ctx, const float *rho_d, const float 
 }
 
 bool d2q9_shape_valid(const lbm_ctx *ctx, int v, int tx, int ty, int pol) {
-    if (v == 0)  // shared-memory row sweep: 16-bit storage, fixed block width, 1 .. 1024 rows per block, ring 0/1
-        return (ctx->desc.dtype == LBM_F16S || ctx->desc.dtype == LBM_BF16S) && tx == d2q9::stage::THREADS && ty >= 1 &&
-               ty <= 1024 && (pol == 0 || pol == 1) && small_index(ctx);
+    if (v == 0)  // bulk-copy pipeline: 16-bit storage, fixed block shape, three ring variants
+        return (ctx->desc.dtype == LBM_F16S || ctx->desc.dtype == LBM_BF16S) &&
+               tx == d2q9::bulk::threads<4>() && ty == 1 &&
+               pol >= 0 && pol <= 2 && small_index(ctx);
     if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256 || pol < 0 || pol > 2) return false;
     if (v == 1) return pol == 0;
     if (!small_index(ctx) || ctx->pitch % v) return false;
@@ -616,6 +645,18 @@ cudaError_t d2q9_autotune(lbm_ctx *ctx, bool force_retune) {
     g_tune_cache[key] = Shape{ctx->cells_per_thread, ctx->block_threads, ctx->rows_per_block, ctx->l2_policy};
     save_tune_file();
     return cudaSuccess;
+}
+
+unsigned d2q9_take_pipe_status(lbm_ctx *ctx) {
+    if (!ctx->pipe_status_d) return 0;
+    unsigned h = 0;
+    if (cudaMemcpyAsync(&h, ctx->pipe_status_d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        return ~0u;
+    if (h && (cudaMemsetAsync(ctx->pipe_status_d, 0, sizeof(unsigned), ctx->stream) != cudaSuccess ||
+              cudaStreamSynchronize(ctx->stream) != cudaSuccess))
+        return ~0u;
+    return h;
 }
 
 cudaError_t d2q9_step(lbm_ctx *ctx, int nsteps) {

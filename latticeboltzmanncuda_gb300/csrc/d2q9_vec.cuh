@@ -36,33 +36,108 @@ __device__ __forceinline__ void scalar_cell(const S *__restrict__ src, S *__rest
     for (int q = 0; q < 9; ++q) sth<S>(dst + q * plane + c, h[q]);
 }
 
-template <class S, int V, bool FORCE, class I, int POL = 0>
-__device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restrict__ dst,
-                                         const uint16_t *__restrict__ links, int x0, int y, int nx, int ny,
-                                         I pitch, I plane, int periodic, const D2Q9Params &prm) {
-    using R = typename Store<S>::R;
-    const uint64_t pol_ld = POL ? policy_evict_first() : 0;
-    const uint64_t pol_st = POL == 1 ? policy_evict_last() : 0;
+// The source values one thread reads for its vector of a row, kept as raw stored words until
+// they are used: a thread can hold the next row's loads in flight while it updates this row
+// (16-bit storage: 9 populations x V cells in 9 V / 2 registers).
+template <class S, int V, class I>
+struct RowLoad {
+    using T = typename RawPack<sizeof(S) * V>::T;
+    using LT = typename RawPack<2 * V < 4 ? 4 : 2 * V>::T;
+    T q0, q2, q4, a1, a5, a8, b3, b6, b7;  // populations at x0 .. x0+V-1 of rows y (0, 1, 3), y-1 (2, 5, 6), y+1 (4, 7, 8)
+    LT links;
+    S e[3];  // lane 0: populations 1, 5, 8 at x0 - 1; lane 31: populations 3, 6, 7 at x0 + V
+    S w[3];  // periodic row, the vector holding the last column: populations 3, 6, 7 at x = 0
+    I r0, rm, rp;
+    int xa;
+};
+
+template <class T, int POL>
+__device__ __forceinline__ T ld_raw(const T *p, uint64_t pol) {
+    if constexpr (POL == 0)
+        return __ldg(p);
+    else
+        return ld_hint<T>(p, pol);
+}
+
+template <class S, int V, class I, int POL>
+__device__ __forceinline__ void load_row(RowLoad<S, V, I> &ld, const S *__restrict__ src,
+                                         const uint16_t *__restrict__ links, int x0, int y, int nx, int ny, I pitch,
+                                         I plane, int periodic, uint64_t pol_ld) {
+    using T = typename RowLoad<S, V, I>::T;
+    using LT = typename RowLoad<S, V, I>::LT;
     const int lane = threadIdx.x & 31;
     const int xa = min(x0, (int)pitch - V);  // threads beyond the row load a valid vector
     int ym = y - 1, yp = y + 1;
     if (ym < 0) ym = (periodic & 2) ? ny - 1 : 0;
     if (yp >= ny) yp = (periodic & 2) ? 0 : ny - 1;
     const I r0 = (I)y * pitch, rm = (I)ym * pitch, rp = (I)yp * pitch;
+    ld.r0 = r0;
+    ld.rm = rm;
+    ld.rp = rp;
+    ld.xa = xa;
+    auto at = [&](int q, I r) { return reinterpret_cast<const T *>(src + q * plane + r + xa); };
+    ld.q0 = ld_raw<T, POL>(at(0, r0), pol_ld);
+    ld.q2 = ld_raw<T, POL>(at(2, rm), pol_ld);
+    ld.q4 = ld_raw<T, POL>(at(4, rp), pol_ld);
+    ld.a1 = ld_raw<T, POL>(at(1, r0), pol_ld);
+    ld.a5 = ld_raw<T, POL>(at(5, rm), pol_ld);
+    ld.a8 = ld_raw<T, POL>(at(8, rp), pol_ld);
+    ld.b3 = ld_raw<T, POL>(at(3, r0), pol_ld);
+    ld.b6 = ld_raw<T, POL>(at(6, rm), pol_ld);
+    ld.b7 = ld_raw<T, POL>(at(7, rp), pol_ld);
+    if constexpr (V == 1)
+        ld.links = __ldg(links + r0 + xa);
+    else
+        ld.links = __ldg(reinterpret_cast<const LT *>(links + r0 + xa));
+    if (lane == 0) {
+        // from the clamped xa: a warp lying wholly beyond the row must not address past it
+        int xm = xa - 1;
+        if (xm < 0) xm = (periodic & 1) ? nx - 1 : 0;  // unused (bounce-back) when not periodic
+        ld.e[0] = __ldg(src + 1 * plane + r0 + xm);
+        ld.e[1] = __ldg(src + 5 * plane + rm + xm);
+        ld.e[2] = __ldg(src + 8 * plane + rp + xm);
+    } else if (lane == 31) {
+        const int xq = min(x0 + V, (int)pitch - 1);
+        ld.e[0] = __ldg(src + 3 * plane + r0 + xq);
+        ld.e[1] = __ldg(src + 6 * plane + rm + xq);
+        ld.e[2] = __ldg(src + 7 * plane + rp + xq);
+    }
+    const int kl = nx - 1 - x0;
+    if ((periodic & 1) && kl >= 0 && kl < V) {
+        ld.w[0] = __ldg(src + 3 * plane + r0);
+        ld.w[1] = __ldg(src + 6 * plane + rm);
+        ld.w[2] = __ldg(src + 7 * plane + rp);
+    }
+}
 
+// Update the vector of ld and store it to dst.  own(q, out) yields the vector's own population q
+// (bounce-back takes the opposite population of the cell itself; solid cells keep their own).
+template <class S, int V, bool FORCE, class I, int POL, class Own>
+__device__ __forceinline__ void finish_row(const RowLoad<S, V, I> &ld, Own own, S *__restrict__ dst, int x0, int nx,
+                                           I plane, int periodic, const D2Q9Params &prm, uint64_t pol_st) {
+    using R = typename Store<S>::R;
+    const int lane = threadIdx.x & 31;
+    const I r0 = ld.r0;
     R f[9][V];
     R a1[V], a5[V], a8[V], b3[V], b6[V], b7[V];
-    ld_pack_pol<S, V, POL>(src + 0 * plane + r0 + xa, f[0], pol_ld);
-    ld_pack_pol<S, V, POL>(src + 2 * plane + rm + xa, f[2], pol_ld);
-    ld_pack_pol<S, V, POL>(src + 4 * plane + rp + xa, f[4], pol_ld);
-    ld_pack_pol<S, V, POL>(src + 1 * plane + r0 + xa, a1, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 5 * plane + rm + xa, a5, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 8 * plane + rp + xa, a8, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 3 * plane + r0 + xa, b3, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 6 * plane + rm + xa, b6, pol_ld);
-    ld_pack_pol<S, V, POL>(src + 7 * plane + rp + xa, b7, pol_ld);
+    unpack<S, V>(ld.q0, f[0]);
+    unpack<S, V>(ld.q2, f[2]);
+    unpack<S, V>(ld.q4, f[4]);
+    unpack<S, V>(ld.a1, a1);
+    unpack<S, V>(ld.a5, a5);
+    unpack<S, V>(ld.a8, a8);
+    unpack<S, V>(ld.b3, b3);
+    unpack<S, V>(ld.b6, b6);
+    unpack<S, V>(ld.b7, b7);
     uint32_t L[V];
-    ld_links<V>(links + r0 + xa, L);
+    if constexpr (V == 1) {
+        L[0] = ld.links;
+    } else {
+        uint16_t e[V];
+        memcpy(e, &ld.links, sizeof(e));
+#pragma unroll
+        for (int k = 0; k < V; ++k) L[k] = e[k];
+    }
 
     // populations moving +x come from x-1: the previous lane's last element
     R p1 = __shfl_up_sync(0xffffffffu, a1[V - 1], 1);
@@ -73,18 +148,14 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
     R n6 = __shfl_down_sync(0xffffffffu, b6[0], 1);
     R n7 = __shfl_down_sync(0xffffffffu, b7[0], 1);
     if (lane == 0) {
-        // from the clamped xa: a warp lying wholly beyond the row must not address past it
-        int xm = xa - 1;
-        if (xm < 0) xm = (periodic & 1) ? nx - 1 : 0;  // unused (bounce-back) when not periodic
-        p1 = ldh<S>(src + 1 * plane + r0 + xm);
-        p5 = ldh<S>(src + 5 * plane + rm + xm);
-        p8 = ldh<S>(src + 8 * plane + rp + xm);
+        p1 = Store<S>::to(ld.e[0]);
+        p5 = Store<S>::to(ld.e[1]);
+        p8 = Store<S>::to(ld.e[2]);
     }
     if (lane == 31) {
-        const int xq = min(x0 + V, (int)pitch - 1);
-        n3 = ldh<S>(src + 3 * plane + r0 + xq);
-        n6 = ldh<S>(src + 6 * plane + rm + xq);
-        n7 = ldh<S>(src + 7 * plane + rp + xq);
+        n3 = Store<S>::to(ld.e[0]);
+        n6 = Store<S>::to(ld.e[1]);
+        n7 = Store<S>::to(ld.e[2]);
     }
 #pragma unroll
     for (int k = 0; k < V; ++k) {
@@ -98,7 +169,7 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
     // periodic row: the last column pulls q = 3, 6, 7 from x = 0
     const int kl = nx - 1 - x0;
     if ((periodic & 1) && kl >= 0 && kl < V) {
-        const R w3 = ldh<S>(src + 3 * plane + r0), w6 = ldh<S>(src + 6 * plane + rm), w7 = ldh<S>(src + 7 * plane + rp);
+        const R w3 = Store<S>::to(ld.w[0]), w6 = Store<S>::to(ld.w[1]), w7 = Store<S>::to(ld.w[2]);
 #pragma unroll
         for (int k = 0; k < V; ++k)
             if (k == kl) {
@@ -120,12 +191,12 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
 #pragma unroll
             for (int k = 0; k < V; ++k) hit |= L[k] != LINK_SOLID ? (L[k] >> (q - 1)) & 1u : 0u;
             if (hit) {
-                R own[V];
-                ld_pack<S, V>(src + opp(q) * plane + r0 + xa, own);
+                R mine[V];
+                own(opp(q), mine);
 #pragma unroll
                 for (int k = 0; k < V; ++k) {
                     if (L[k] != LINK_SOLID && ((L[k] >> (q - 1)) & 1u)) {
-                        R v = own[k];
+                        R v = mine[k];
                         if ((L[k] >> (q + 7)) & 1u) v = add_(v, wall_term<S, R>(q, uw));
                         f[q][k] = v;
                     }
@@ -166,14 +237,28 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         if (solid_any) {
-            R own[V];
-            ld_pack<S, V>(src + q * plane + r0 + x0, own);
+            R mine[V];
+            own(q, mine);
 #pragma unroll
             for (int k = 0; k < V; ++k)
-                if (L[k] == LINK_SOLID) f[q][k] = own[k];
+                if (L[k] == LINK_SOLID) f[q][k] = mine[k];
         }
         st_pack_pol<S, V, POL>(dst + q * plane + r0 + x0, f[q], pol_st);
     }
+}
+
+template <class S, int V, bool FORCE, class I, int POL = 0>
+__device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restrict__ dst,
+                                         const uint16_t *__restrict__ links, int x0, int y, int nx, int ny,
+                                         I pitch, I plane, int periodic, const D2Q9Params &prm) {
+    const uint64_t pol_ld = POL ? policy_evict_first() : 0;
+    const uint64_t pol_st = POL == 1 ? policy_evict_last() : 0;
+    RowLoad<S, V, I> ld;
+    load_row<S, V, I, POL>(ld, src, links, x0, y, nx, ny, pitch, plane, periodic, pol_ld);
+    // own populations at the clamped xa (equal to x0 for every vector that is stored)
+    const S *mine = src + ld.r0 + ld.xa;
+    auto own = [&](int q, typename Store<S>::R (&out)[V]) { ld_pack<S, V>(mine + q * plane, out); };
+    finish_row<S, V, FORCE, I, POL>(ld, own, dst, x0, nx, plane, periodic, prm, pol_st);
 }
 
 }  // namespace d2q9

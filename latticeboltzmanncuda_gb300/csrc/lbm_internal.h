@@ -117,6 +117,8 @@ struct lbm_ctx {
     int cells_per_thread = 1;
     int rows_per_block = 1;
     int l2_policy = 0;             // vector path: L2 eviction hints (0 none, 1 ld first/st last, 2 ld first)
+    unsigned *pipe_status_d = nullptr;  // D2Q9 bulk-copy pipeline: status bits set by a block whose wait gave up
+    bool pipe_used = false;             // the pipeline ran since the status was last read
     bool tuned = false;
     bool alternate_sweeps = true;  // visit rows in alternating order on successive steps
     unsigned sweep = 0;
@@ -142,6 +144,8 @@ cudaError_t d2q9_build_links(lbm_ctx *ctx);
 cudaError_t d2q9_init_equilibrium(lbm_ctx *ctx, const float *rho_d, const float *ux_d, const float *uy_d);
 cudaError_t d2q9_step(lbm_ctx *ctx, int nsteps);
 cudaError_t d2q9_autotune(lbm_ctx *ctx, bool force_retune);
+// read and clear the bulk-copy pipeline's status bits (synchronises the context's stream)
+unsigned d2q9_take_pipe_status(lbm_ctx *ctx);
 bool d2q9_shape_valid(const lbm_ctx *ctx, int v, int tx, int ty, int pol);
 cudaError_t d2q9_moments(lbm_ctx *ctx, float *rho_d, float *ux_d, float *uy_d);
 cudaError_t d2q9_conservation(lbm_ctx *ctx, double *out_d);

@@ -197,10 +197,11 @@ def test_steps_are_deterministic():
 
 
 # (cells per thread, block width, rows per block, L2 policy)
-# (cells per thread, block width, rows per block, L2 policy); cells per thread 0 is the
-# shared-memory row sweep of 16-bit storage (128 threads, rows per block = the run of rows it sweeps)
+# (cells per thread, block width, rows per block, L2 policy); cells per thread 0 is the bulk-copy
+# pipeline of 16-bit storage (160 threads, 4 cells per consumer thread, one row per task; the last
+# field the ring variant)
 SHAPES = [(1, 256, 1, 0), (1, 128, 2, 0), (2, 64, 1, 0), (2, 32, 4, 1), (4, 32, 1, 2), (4, 64, 2, 0),
-          (4, 128, 1, 1), (8, 32, 1, 1), (8, 64, 2, 2), (0, 128, 1, 0), (0, 128, 8, 1), (0, 128, 64, 0)]
+          (4, 128, 1, 1), (8, 32, 1, 1), (8, 64, 2, 2), (0, 160, 1, 0), (0, 160, 1, 1), (0, 160, 1, 2)]
 
 
 def shape_ok(dtype, v):
@@ -261,19 +262,19 @@ def test_shapes_and_sweep_orders_agree_bitwise(dtype):
 
 @pytest.mark.parametrize("dtype", ["f16s", "bf16s"])
 @pytest.mark.parametrize("periodic", [0, 1, 2, 3])
-def test_row_sweep_matches_vector_kernel_across_strips(dtype, periodic):
-    """The shared-memory row sweep over several strips and row runs (strip edges, run edges, wrap
+def test_bulk_pipeline_matches_vector_kernel_across_strips(dtype, periodic):
+    """The bulk-copy pipeline over several strips and row runs (strip edges, run edges, wrap
     in x and y, walls, moving walls, solid cells on strip edges) is bit-identical to the vector
     kernel."""
     nx, ny = 777, 70
     flags, _ = lbm.gen_channel(nx, ny, 9, 3.0, 9.0, 11)
     if periodic & 2:
         flags[0, :] = flags[-1, :] = 0
-    flags[:, 255:258] = np.where(np.arange(ny)[:, None] % 5 == 0, 1, flags[:, 255:258])  # solid on a strip edge
+    flags[:, 510:514] = np.where(np.arange(ny)[:, None] % 5 == 0, 1, flags[:, 510:514])  # solid on a strip edge
     flags[ny // 3, ::7] = lbm.MOVING_WALL
     f0 = random_state(nx, ny, 5 + periodic)
     outs = []
-    for shape in ((8, 64, 2, 0), (0, 128, 16, 0), (0, 128, 7, 1)):
+    for shape in ((8, 64, 2, 0), (0, 160, 1, 0), (0, 160, 1, 1), (0, 160, 1, 2)):
         with lbm.Lattice(nx, ny, dtype=dtype, tau=0.61, periodic=periodic, body_force=(1e-5, -2e-6, 0),
                          wall_velocity=(0.03, 0.01, 0)) as L:
             L.set_flags(flags)
@@ -281,7 +282,8 @@ def test_row_sweep_matches_vector_kernel_across_strips(dtype, periodic):
             L.set_launch(*shape)
             L.step(23)
             outs.append(L.retrieve_populations())
-    assert np.array_equal(outs[1], outs[0]) and np.array_equal(outs[2], outs[0])
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
 
 
 def test_autotune_picks_a_valid_shape_and_keeps_state():
@@ -308,7 +310,11 @@ def test_bad_launch_shape_rejected():
         with pytest.raises(lbm.LBMError):
             L.set_launch(2, 256, 2)  # more than 256 threads
         with pytest.raises(lbm.LBMError):
-            L.set_launch(0, 128, 8)  # the row sweep is for 16-bit storage
+            L.set_launch(0, 160, 8)  # the bulk-copy pipeline is for 16-bit storage
     with lbm.Lattice(64, 8, dtype="f16s") as L:
         with pytest.raises(lbm.LBMError):
-            L.set_launch(0, 64, 8)  # the row sweep has 128 threads per block
+            L.set_launch(0, 64, 1)  # the bulk-copy pipeline has 160 threads per block
+        with pytest.raises(lbm.LBMError):
+            L.set_launch(0, 160, 1, 3)  # three pipeline variants
+        with pytest.raises(lbm.LBMError):
+            L.set_launch(0, 160, 2, 0)  # one row per task

@@ -1,8 +1,10 @@
-"""CPU replay of the vectorised D2Q9 step's address arithmetic (csrc/d2q9_vec.cuh, step_vec) for
-every thread of every launch shape the library can use, single-domain grids and batch tiles,
-over many domain sizes: every population offset must lie in [0, 9 * plane) and every link-word
-offset in [0, plane).  The kernel has no device-side bounds checks, so this replay is where its
-indexing is checked; keep it in step with step_vec."""
+"""CPU replay of the D2Q9 kernels' address arithmetic for every thread of every launch shape the
+library can use, over many domain sizes: the vectorised step (csrc/d2q9_vec.cuh, single-domain
+grids and batch tiles) and the bulk-copy pipeline (csrc/d2q9_bulk.cuh: copy ranges, alignment,
+shared-memory indexes, and its slot protocol under random interleavings).  Every population offset
+must lie in [0, 9 * plane) and every link-word offset in [0, plane).  The kernels have no
+device-side bounds checks, so this replay is where their indexing is checked; keep it in step
+with the kernels."""
 import itertools
 
 import numpy as np
@@ -95,90 +97,189 @@ def test_replay_catches_an_unclamped_left_neighbour():
     assert bad.max() >= 9 * plane
 
 
-# ------------------------------------------------------------------ shared-memory row sweep
-# csrc/d2q9_stage.cuh: 128 threads x 4 cells = strips of W = 512, plane rows of SEG = W + 16
-# elements staged as 16-byte (8-element) chunks, link words after the nine planes of a slot.
-THREADS, CPT = 128, 4
-W = THREADS * CPT
-SEG = W + 16
-CHUNKS, LCHUNKS = SEG // 8, W // 8
-LINKS, SLOT = 9 * SEG, 9 * SEG + W
+# ------------------------------------------------------------------ bulk-copy pipeline
+# csrc/d2q9_bulk.cuh: strips of BW = 512 cells, BV = 4 or 2 cells per consumer lane (NC = 4 or 8
+# consumer warps); a slot holds the nine plane segments one output row pulls (BSEG = BW + 16
+# elements each, x0 - 8 .. x0 + BW + 8), BW link words and 8 elements of wrapped columns.
+BW = 512
+NC = BW // (32 * 4)
+BSEG = BW + 16
+BLINKS, BWRAP, BSLOT = 9 * BSEG, 9 * BSEG + BW, 9 * BSEG + BW + 8
+CY = [0, 0, 1, 0, -1, 1, 1, -1, -1]  # c_y of the populations: plane q is pulled from row y - c_y(q)
 
 
-def stage_offsets(nx, ny, rows, periodic, nslot):
-    """Every global element offset and shared-memory index the row sweep touches, over all blocks."""
+def bulk_tasks(nx, ny, reverse):
+    """(x0, y) of every task in the order blocks take them (task_of)."""
+    pitch = (nx + 31) // 32 * 32
+    nstrips = (pitch + BW - 1) // BW
+    ntasks = nstrips * ny
+    for i in range(ntasks):
+        j = ntasks - 1 - i if reverse else i
+        y, strip = divmod(j, nstrips)
+        yield strip * BW, y
+
+
+def bulk_check(nx, ny, periodic, reverse, BV):
     pitch = (nx + 31) // 32 * 32
     plane = pitch * ny
-    gread, lread, gwrite, smem = [], [], [], []
-    nbx, nby = (nx + W - 1) // W, (ny + rows - 1) // rows
-    t = np.arange(THREADS)
-    for bx in range(nbx):
-        x0 = bx * W
-        for by in range(nby):
-            ya = by * rows
-            yb = min(ya + rows, ny)
-            for p in range(yb - ya + 2):  # copies of rows ya-1 .. yb
-                row = ya - 1 + p
-                if row < 0 or row >= ny:
-                    if not periodic & 2:
-                        continue
-                    row = row + ny if row < 0 else row - ny
-                base = (p % nslot) * SLOT
-                tp = t[t < CHUNKS]
-                gx = x0 - 8 + 8 * tp
-                ok = (gx >= 0) & (gx + 8 <= pitch)
-                for q in range(9):
-                    g = q * plane + row * pitch + gx[ok]
-                    gread += [g, g + 7]
-                    smem += [base + q * SEG + 8 * tp[ok], base + q * SEG + 8 * tp[ok] + 7]
-                lt = t - (THREADS - LCHUNKS)
-                lt = lt[lt >= 0]
-                gl = x0 + 8 * lt
-                okl = gl + 8 <= pitch
-                lread += [row * pitch + gl[okl], row * pitch + gl[okl] + 7]
-                smem += [base + LINKS + 8 * lt[okl], base + LINKS + 8 * lt[okl] + 7]
-            xa = x0 + CPT * t
-            act = xa < nx
-            lx = 8 + CPT * t[act]
-            for k, y in enumerate(range(ya, yb)):
-                c = y * pitch + xa[act]
-                for q in range(9):
-                    gwrite += [q * plane + c, q * plane + c + CPT - 1]  # one 8-byte store
-                for d in range(3):
-                    base = ((k + d) % nslot) * SLOT
-                    smem += [base + 8 * SEG + lx - 1, base + 8 * SEG + lx + CPT]  # reads lx-1 .. lx+4 of a plane
-                    smem += [base + LINKS + CPT * t[act], base + LINKS + CPT * t[act] + CPT - 1]
-                if periodic & 1:
-                    ym = y - 1 if y > 0 else (ny - 1 if periodic & 2 else 0)
-                    yp = y + 1 if y < ny - 1 else (0 if periodic & 2 else ny - 1)
-                    cells = np.concatenate([xa[act] + cc for cc in range(CPT)])
-                    for q, r in ((1, y), (5, ym), (8, yp)):
-                        gread.append(q * plane + r * pitch + np.full(int((cells == 0).sum()), nx - 1))
-                    for q, r in ((3, y), (6, ym), (7, yp)):
-                        gread.append(q * plane + r * pitch + np.zeros(int((cells == nx - 1).sum()), int))
-    cat = lambda a: np.concatenate(a) if a else np.zeros(0, int)
-    return cat(gread), cat(lread), cat(gwrite), cat(smem), plane
+    for K in (4, 6):  # slot bases and the barriers after the ring keep 16- and 8-byte alignment
+        assert all((s * BSLOT * 2) % 16 == 0 for s in range(K + 1))
+    assert (BSEG * 2) % 16 == 0 and (BLINKS * 2) % 16 == 0 and BWRAP + 6 <= BSLOT
+    t = np.arange(BW // BV)
+    lx = 8 + BV * t
+    # consumer reads inside one plane row of a slot: lx .. lx+3, lane 0 lx-1, lane 31 lx+4
+    assert lx.min() - 1 >= 0 and lx.max() + BV < BSEG and (BV * t + BV - 1).max() < BW
+    for x0, y in bulk_tasks(nx, ny, reverse):
+        assert x0 < pitch and x0 % 8 == 0
+        gx0, gx1, lx1 = max(x0 - 8, 0), min(x0 + BW + 8, pitch), min(x0 + BW, pitch)
+        n, nl = gx1 - gx0, lx1 - x0
+        assert n > 0 and nl > 0 and (2 * n) % 16 == 0 and (2 * nl) % 16 == 0
+        dst = gx0 - (x0 - 8)
+        assert dst >= 0 and dst + n <= BSEG and (2 * dst) % 16 == 0
+        for q in range(9):
+            row = y - CY[q]
+            if row < 0 or row >= ny:
+                if not periodic & 2:
+                    continue  # not copied
+                row %= ny
+            g = q * plane + row * pitch + gx0
+            assert (2 * g) % 16 == 0 and g >= 0 and g + n <= 9 * plane
+        gl = y * pitch + x0
+        assert (2 * gl) % 16 == 0 and gl + nl <= plane
+        ym = y - 1 if y > 0 else (ny - 1 if periodic & 2 else 0)
+        yp = y + 1 if y < ny - 1 else (0 if periodic & 2 else ny - 1)
+        if periodic & 1:  # lane 1: wrapped columns
+            for r in (y, ym, yp):
+                if x0 == 0:
+                    assert 0 <= 8 * plane + r * pitch + nx - 1 < 9 * plane
+                if x0 <= nx - 1 < x0 + BW:
+                    assert 0 <= 7 * plane + r * pitch < 9 * plane
+        xc = x0 + BV * t
+        # own populations from global memory at the clamped vector
+        xa = np.minimum(xc, pitch - BV)
+        own = np.arange(9)[:, None] * plane + y * pitch + xa[None, :]
+        assert own.min() >= 0 and (own + BV - 1).max() < 9 * plane
+        act = xc < nx
+        stores = np.arange(9)[:, None] * plane + y * pitch + xc[act][None, :]
+        if stores.size:
+            assert stores.min() >= 0 and (stores + BV - 1).max() < 9 * plane and (xc[act] + BV - 1).max() < pitch
 
 
-@pytest.mark.parametrize("nx,ny", SIZES + [(512, 5), (513, 40), (1023, 33)])
-def test_row_sweep_addresses_stay_in_buffers(nx, ny):
-    for rows, periodic, nslot in itertools.product((1, 8, 64), range(4), (4, 8)):
-        gread, lread, gwrite, smem, plane = stage_offsets(nx, ny, rows, periodic, nslot)
-        for a, hi in ((gread, 9 * plane), (lread, plane), (gwrite, 9 * plane), (smem, nslot * SLOT)):
-            if a.size:
-                assert a.min() >= 0 and a.max() < hi, (nx, ny, rows, periodic, nslot, a.min(), a.max(), hi)
+@pytest.mark.parametrize("nx,ny", SIZES + [(512, 5), (513, 40), (1023, 33), (4096, 17)])
+def test_bulk_pipeline_addresses_stay_in_buffers(nx, ny):
+    for periodic, reverse, BV in itertools.product(range(4), (0, 1), (2, 4)):
+        bulk_check(nx, ny, periodic, reverse, BV)
 
 
-@pytest.mark.parametrize("nslot", [4, 8])
-def test_row_sweep_slot_reuse_never_overwrites_a_live_row(nslot):
-    """Iteration k reads positions k, k+1, k+2 and refills the slot of position k + nslot - 1,
-    which is the slot of position k - 1: no slot is refilled while a live row sits in it; and
-    waiting until at most nslot - 4 copy groups are pending leaves positions <= k + 2 landed."""
-    for k in range(200):
-        live = {(k + d) % nslot for d in range(3)}
-        assert (k + nslot - 1) % nslot not in live
-        committed = (nslot - 1) + k  # prologue groups + one per earlier iteration
-        assert committed - (nslot - 4) >= k + 3
+def test_bulk_tasks_cover_every_cell_once():
+    for nx, ny in itertools.product((1, 100, 512, 1000, 4096), (1, 7, 64, 65)):
+        pitch = (nx + 31) // 32 * 32
+        for reverse in (0, 1):
+            seen = np.zeros((ny, pitch), int)
+            for x0, y in bulk_tasks(nx, ny, reverse):
+                seen[y, x0:min(x0 + BW, pitch)] += 1
+            assert (seen == 1).all()
+
+
+class Barrier:
+    """mbarrier phase semantics: a phase completes when its pending arrivals (and bytes) reach 0;
+    try_wait.parity(P) succeeds when the current phase's parity differs from P.  Waiting for phase
+    m is only unambiguous while at most m + 1 phases have completed."""
+
+    def __init__(self, count):
+        self.count, self.pending, self.tx, self.done = count, count, 0, 0
+
+    def arrive(self, tx=0):
+        self.pending -= 1
+        self.tx += tx
+        self._maybe_complete()
+
+    def land(self, nbytes):
+        self.tx -= nbytes
+        self._maybe_complete()
+
+    def _maybe_complete(self):
+        if self.pending == 0 and self.tx == 0:
+            self.done += 1
+            self.pending = self.count
+
+    def waited(self, m):
+        assert self.done <= m + 1, "parity wait would be ambiguous"
+        return self.done > m
+
+
+def simulate_bulk_protocol(ntasks, K, wrap_lane, seed, consumers=NC, arrivals=NC):
+    """pipeline(): producer lane 0 (copies, landing at random later times), optionally lane 1 (the
+    wrapped columns) and `consumers` consumer warps, each empty barrier expecting `arrivals` (both
+    the number of consumer warps in the kernel), under a random interleaving."""
+    rng = np.random.default_rng(seed)
+    full = [Barrier(2 if wrap_lane else 1) for _ in range(K)]
+    empty = [Barrier(arrivals) for _ in range(K)]
+    released = [set() for _ in range(consumers)]
+    written = {}  # (slot, lane) -> position last written by that producer lane
+    ppos = [0, 0 if wrap_lane else ntasks]
+    in_flight = []
+    cpos = [0] * consumers
+
+    def producer_step(ln):
+        p = ppos[ln]
+        if p >= ntasks:
+            return False
+        s = p % K
+        if p >= K and not empty[s].waited(p // K - 1):
+            return False
+        if (s, ln) in written:  # every consumer has released what this lane wrote there before
+            assert all(written[(s, ln)] in r for r in released), "slot refilled while live"
+        written[(s, ln)] = p
+        if ln == 0:
+            full[s].arrive(tx=1)
+            in_flight.append(s)
+        else:
+            full[s].arrive()
+        ppos[ln] += 1
+        return True
+
+    def land_step():
+        if not in_flight:
+            return False
+        full[in_flight.pop(int(rng.integers(len(in_flight))))].land(1)
+        return True
+
+    def consumer_step(c):
+        p = cpos[c]
+        if p >= ntasks:
+            return False
+        s = p % K
+        if not full[s].waited(p // K):
+            return False
+        assert written.get((s, 0)) == p and (not wrap_lane or written.get((s, 1)) == p), "read a stale slot"
+        released[c].add(p)
+        empty[s].arrive()
+        cpos[c] += 1
+        return True
+
+    actors = [lambda: producer_step(0), lambda: producer_step(1), land_step]
+    actors += [lambda c=c: consumer_step(c) for c in range(consumers)]
+    while True:
+        if not any(actors[a]() for a in rng.permutation(len(actors))):
+            break
+    assert ppos[0] == ntasks and not in_flight, "producer stalled"
+    assert all(p == ntasks for p in cpos), "a consumer stalled"
+
+
+@pytest.mark.parametrize("K", [2, 4, 6])
+@pytest.mark.parametrize("consumers", [4, 8])
+def test_bulk_slot_protocol_never_deadlocks_or_overwrites(K, consumers):
+    for seed in range(30):
+        simulate_bulk_protocol(int(np.random.default_rng(seed).integers(1, 40)), K, seed % 2 == 1, seed,
+                               consumers=consumers, arrivals=consumers)
+
+
+def test_bulk_protocol_simulation_catches_a_missing_release():
+    """A consumer warp that never released its slots would stall the producer: the simulation
+    reports it."""
+    with pytest.raises(AssertionError):
+        simulate_bulk_protocol(20, 4, False, 0, consumers=NC - 1)
 
 
 def test_invariant_division_formula():
