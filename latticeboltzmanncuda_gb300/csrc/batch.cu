@@ -304,8 +304,9 @@ cudaError_t launch_any(lbm_batch *b, int step, int reverse) {
     return cudaErrorInvalidValue;
 }
 
-// Time every candidate tile shape on the live batch (two launches per candidate with the step
-// parity kept even, so src -> dst is recomputed without changing the state).
+// Time every candidate tile shape on the live batch (launches with the step parity kept even, so
+// src -> dst is recomputed without changing the state), then the three fastest again with three
+// times the launches, in forward and reverse order, and keep the fastest of those.
 lbm_status tune(lbm_batch *b) {
     struct Cand {
         int v, tx, ty;
@@ -319,9 +320,10 @@ lbm_status tune(lbm_batch *b) {
     cudaEvent_t e0, e1;
     BCUDA(b, cudaEventCreate(&e0), "batch tune: event");
     BCUDA(b, cudaEventCreate(&e1), "batch tune: event");
-    float best = 1e30f;
-    Cand pick = cands[0];
-    for (const Cand &c : cands) {
+    bool empty = false;
+    // ms of n launches with tile shape c (after one warm-up launch); -1 when the batch is empty
+    auto time_cand = [&](const Cand &c, int n, float &ms) -> lbm_status {
+        ms = -1.0f;
         b->v = c.v;
         b->tx = c.tx;
         b->ty = c.ty;
@@ -329,22 +331,49 @@ lbm_status tune(lbm_batch *b) {
         b->tiles_dirty = true;
         lbm_status st = rebuild(b, 1);
         if (st != LBM_OK) return st;
-        if (b->ntiles == 0) break;
+        if (b->ntiles == 0) {
+            empty = true;
+            return LBM_OK;
+        }
         cudaError_t e = launch_any(b, 0, 0);
         if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
-        for (int r = 0; r < 4 && e == cudaSuccess; ++r) e = launch_any(b, 0, r & 1);
+        for (int r = 0; r < n && e == cudaSuccess; ++r) e = launch_any(b, 0, r & 1);
         if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
         if (e == cudaSuccess) e = cudaEventSynchronize(e1);
         BCUDA(b, e, "batch tune: launch");
-        float ms = 0.0f;
         cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best) {
-            best = ms;
-            pick = c;
-        }
+        return LBM_OK;
+    };
+    std::vector<std::pair<float, Cand>> timed;
+    lbm_status st = LBM_OK;
+    for (const Cand &c : cands) {
+        float ms;
+        if ((st = time_cand(c, 4, ms)) != LBM_OK || empty) break;
+        timed.push_back({ms, c});
+    }
+    Cand pick = cands[0];
+    if (st == LBM_OK && !empty && !timed.empty()) {
+        std::stable_sort(timed.begin(), timed.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
+        const size_t top = std::min<size_t>(3, timed.size());
+        std::vector<float> total(top, 0.0f);
+        for (int pass = 0; pass < 2 && st == LBM_OK; ++pass)
+            for (size_t k = 0; k < top && st == LBM_OK; ++k) {
+                const size_t c = pass ? top - 1 - k : k;
+                float ms;
+                st = time_cand(timed[c].second, 12, ms);
+                total[c] += ms;
+            }
+        pick = timed[0].second;
+        float best = 1e30f;
+        for (size_t k = 0; k < top; ++k)
+            if (total[k] < best) {
+                best = total[k];
+                pick = timed[k].second;
+            }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (st != LBM_OK) return st;
     b->v = pick.v;
     b->tx = pick.tx;
     b->ty = pick.ty;

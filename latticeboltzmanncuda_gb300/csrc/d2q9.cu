@@ -473,7 +473,9 @@ void save_tune_file() {
 }
 
 // Time every candidate shape on the context's own domain (f[cur] -> f[cur^1] repeatedly, without
-// swapping, so the state is unchanged) and keep the fastest.
+// swapping, so the state is unchanged), then time the four fastest again with four times the
+// launches, in forward and reverse order, and keep the fastest of those (shapes within a few per
+// cent of each other are otherwise picked by timing noise).
 template <class S>
 cudaError_t tune(lbm_ctx *ctx) {
     const S *src = static_cast<const S *>(ctx->f[ctx->cur]);
@@ -488,24 +490,48 @@ cudaError_t tune(lbm_ctx *ctx) {
     }
     const int64_t cells = (int64_t)ctx->desc.nx * ctx->desc.ny;
     const int reps = cells > (1 << 22) ? 6 : (cells > (1 << 18) ? 12 : 30);
-    float best = 1e30f;
-    Shape pick = {1, 256, 1, 0};
-    for (const Shape &sh : candidates<S>(ctx)) {
-        for (int w = 0; w < 2 && err == cudaSuccess; ++w) err = launch_one<S>(ctx, sh, src, dst, w & 1);
-        if (err != cudaSuccess) break;
+    // ms of `n` launches of shape sh after two warm-up launches; < 0 when the shape is not usable
+    auto time_shape = [&](const Shape &sh, int n, float &ms) -> cudaError_t {
+        ms = -1.0f;
+        cudaError_t e = cudaSuccess;
+        for (int w = 0; w < 2 && e == cudaSuccess; ++w) e = launch_one<S>(ctx, sh, src, dst, w & 1);
+        if (e != cudaSuccess) return e;
         cudaEventRecord(e0, ctx->stream);
-        for (int r = 0; r < reps && err == cudaSuccess; ++r) err = launch_one<S>(ctx, sh, src, dst, r & 1);
+        for (int r = 0; r < n && e == cudaSuccess; ++r) e = launch_one<S>(ctx, sh, src, dst, r & 1);
         cudaEventRecord(e1, ctx->stream);
-        if (err != cudaSuccess) break;
-        err = cudaEventSynchronize(e1);
-        if (err != cudaSuccess) break;
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (sh.v == 0 && d2q9_take_pipe_status(ctx) != 0) continue;  // a bounded wait gave up: not a candidate
-        if (ms < best) {
-            best = ms;
-            pick = sh;
-        }
+        if (e != cudaSuccess) return e;
+        if ((e = cudaEventSynchronize(e1)) != cudaSuccess) return e;
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (sh.v == 0 && d2q9_take_pipe_status(ctx) != 0) return cudaSuccess;  // a bounded wait gave up
+        ms = t;
+        return cudaSuccess;
+    };
+    std::vector<std::pair<float, Shape>> timed;
+    for (const Shape &sh : candidates<S>(ctx)) {
+        float ms;
+        if ((err = time_shape(sh, reps, ms)) != cudaSuccess) break;
+        if (ms >= 0.0f) timed.push_back({ms, sh});
+    }
+    Shape pick = {1, 256, 1, 0};
+    if (err == cudaSuccess && !timed.empty()) {
+        std::stable_sort(timed.begin(), timed.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+        const size_t top = std::min<size_t>(4, timed.size());
+        std::vector<float> total(top, 0.0f);
+        for (int pass = 0; pass < 2 && err == cudaSuccess; ++pass)
+            for (size_t k = 0; k < top && err == cudaSuccess; ++k) {
+                const size_t c = pass ? top - 1 - k : k;
+                float ms;
+                err = time_shape(timed[c].second, 4 * reps, ms);
+                total[c] = (ms < 0.0f || total[c] < 0.0f) ? -1.0f : total[c] + ms;
+            }
+        float best = 1e30f;
+        pick = timed[0].second;
+        for (size_t k = 0; k < top; ++k)
+            if (total[k] >= 0.0f && total[k] < best) {
+                best = total[k];
+                pick = timed[k].second;
+            }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
