@@ -504,7 +504,9 @@ def run_serve(args):
             row[f"served_{dtype}"] = {"status": status, "ok": len(lat), "p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99),
                                       "aggregate_mlups": st["cell_updates"] / st["makespan"] / 1e6,
                                       "makespan_s": st["makespan"], "peak_slots": st["peak_slots"],
-                                      "peak_gb": st["peak_bytes"] / 1e9, "rounds": st["rounds"]}
+                                      "peak_gb": st["peak_bytes"] / 1e9, "rounds": st["rounds"],
+                                      "round_device_s": round(st["round_seconds"], 3),
+                                      "tile_shape": st["tile_shape"], "tunings": st["tunings"]}
         lat, work, makespan = _serial_plain(reqs)
         row["plain_f32"] = {"p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99),
                             "aggregate_mlups": work / makespan / 1e6, "makespan_s": makespan}

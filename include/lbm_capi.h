@@ -246,12 +246,19 @@ LBM_API lbm_status lbm_conservation(lbm_ctx *ctx, double host_out[4]);
  * single-domain context with the same descriptor computes (bit-identical populations).  Slots
  * are added (allocated, flags set, equilibrium rho = 1, u = 0) and removed between steps;
  * lbm_batch_step advances every live slot.  The tile shape (cells per thread, block width, rows
- * per block) is tuned on the batch at the first step, or fixed with lbm_batch_set_launch. */
+ * per block) is tuned on the batch itself by the first lbm_batch_step that finds 2^24 or more live
+ * cells (until then a default shape runs), and once more when the live cells have grown to four
+ * times those it was tuned on; lbm_batch_autotune tunes now, lbm_batch_set_launch fixes a shape.
+ * Adding, removing and stepping only queue work on the batch stream (host data is staged through
+ * pinned memory), so a request loop can prepare its next round while the device runs the current
+ * one; device errors of queued work surface at the next call that waits (lbm_batch_synchronize,
+ * lbm_batch_collect with wait, lbm_batch_moments, lbm_batch_info). */
 typedef struct lbm_batch lbm_batch;
 LBM_API lbm_status lbm_batch_create(int32_t dtype, int32_t device, void *stream, lbm_batch **out);
 LBM_API lbm_status lbm_batch_destroy(lbm_batch *b);
 LBM_API const char *lbm_batch_last_error(const lbm_batch *b);
-/* device bytes a slot of this size takes (two population buffers, link words, flags) */
+/* device bytes a slot of this size takes (two population buffers, link words, flags and the
+ * fluid-cell count) */
 LBM_API int64_t lbm_batch_slot_bytes(int32_t dtype, int32_t nx, int32_t ny);
 /* desc: mode LBM_D2Q9, nx, ny, tau, periodic, body_force, wall_velocity (dtype, device and stream
  * come from the batch); host_flags[ny][nx] may be NULL (all fluid) */
@@ -260,6 +267,8 @@ LBM_API lbm_status lbm_batch_add(lbm_batch *b, const lbm_desc *desc, const uint8
 LBM_API lbm_status lbm_batch_remove(lbm_batch *b, int32_t slot);
 LBM_API lbm_status lbm_batch_step(lbm_batch *b, int32_t nsteps);
 LBM_API lbm_status lbm_batch_autotune(lbm_batch *b);
+/* how many times the batch has tuned its tile shape */
+LBM_API lbm_status lbm_batch_tunings(lbm_batch *b, int32_t *count);
 LBM_API lbm_status lbm_batch_set_launch(lbm_batch *b, int32_t cells_per_thread, int32_t block_threads,
                                         int32_t rows_per_block);
 LBM_API lbm_status lbm_batch_synchronize(lbm_batch *b);
@@ -273,6 +282,13 @@ LBM_API lbm_status lbm_batch_slot_steps(lbm_batch *b, int32_t slot, int64_t *ste
 LBM_API lbm_status lbm_batch_set_slot_steps(lbm_batch *b, int32_t slot, int64_t steps);
 LBM_API lbm_status lbm_batch_moments(lbm_batch *b, int32_t slot, float *host_rho, float *host_ux,
                                      float *host_uy);
+/* The same read-back queued without waiting: *ticket names it.  The slot may be removed right
+ * after.  lbm_batch_collect copies a ticket's density and velocity into the host arrays (any may
+ * be NULL) and releases it; with wait == 0 it returns at once with *ready = 0 while the copy is
+ * still running. */
+LBM_API lbm_status lbm_batch_moments_async(lbm_batch *b, int32_t slot, int64_t *ticket);
+LBM_API lbm_status lbm_batch_collect(lbm_batch *b, int64_t ticket, int32_t wait, float *host_rho,
+                                     float *host_ux, float *host_uy, int32_t *ready);
 LBM_API lbm_status lbm_batch_load_populations(lbm_batch *b, int32_t slot, const void *host,
                                               int32_t host_dtype);
 LBM_API lbm_status lbm_batch_retrieve_populations(lbm_batch *b, int32_t slot, void *host,
@@ -322,6 +338,9 @@ typedef struct lbm_server_stats {
     int64_t peak_bytes;
     int32_t peak_slots;
     int32_t rejected;
+    double round_seconds;   /* device time of the rounds' launch sequences (CUDA events) */
+    int32_t tile_shape[3];  /* the batch's final tile shape: cells per thread, block width, rows */
+    int32_t tunings;        /* times the batch tuned its tile shape during the run */
 } lbm_server_stats;
 LBM_API void lbm_server_config_init(lbm_server_config *cfg);
 LBM_API lbm_status lbm_server_create(const lbm_server_config *cfg, lbm_server **out);

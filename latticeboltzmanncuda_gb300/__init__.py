@@ -442,6 +442,22 @@ class Batch:
         self._chk(capi.lib().lbm_batch_moments(self._b, int(slot), *[ptr(o) for o in out]))
         return tuple(out)
 
+    def moments_async(self, slot):
+        """Queue the read-back of a slot's density and velocity; returns a ticket for collect()."""
+        t = ctypes.c_int64(0)
+        self._chk(capi.lib().lbm_batch_moments_async(self._b, int(slot), ctypes.byref(t)))
+        return t.value, self.shapes[slot]
+
+    def collect(self, ticket, wait=True):
+        """(rho, ux, uy) of a ticket from moments_async(), or None while its copy is still running
+        (wait=False)."""
+        tid, (nx, ny) = ticket
+        out = [np.empty((ny, nx), np.float32) for _ in range(3)]
+        ready = ctypes.c_int32(0)
+        self._chk(capi.lib().lbm_batch_collect(self._b, int(tid), int(bool(wait)), *[ptr(o) for o in out],
+                                               ctypes.byref(ready)))
+        return tuple(out) if ready.value else None
+
     def load_populations(self, slot, f):
         f = np.asarray(f)
         dt = F64 if f.dtype == np.float64 else F32
@@ -503,4 +519,5 @@ def serve(requests, dtype="f32", budget_bytes=150e9, max_slots=0, round_steps=20
             d["moments"] = tuple(outs[i])
         results.append(d)
     stats = {k: getattr(st, k) for k, _ in capi.ServerStats._fields_}
+    stats["tile_shape"] = list(stats["tile_shape"])
     return results, stats, status

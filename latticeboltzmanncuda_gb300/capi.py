@@ -82,7 +82,8 @@ class RequestResult(ctypes.Structure):
 
 class ServerStats(ctypes.Structure):
     _fields_ = [("makespan", ctypes.c_double), ("cell_updates", ctypes.c_double), ("rounds", ctypes.c_int64),
-                ("peak_bytes", ctypes.c_int64), ("peak_slots", ctypes.c_int32), ("rejected", ctypes.c_int32)]
+                ("peak_bytes", ctypes.c_int64), ("peak_slots", ctypes.c_int32), ("rejected", ctypes.c_int32),
+                ("round_seconds", ctypes.c_double), ("tile_shape", ctypes.c_int32 * 3), ("tunings", ctypes.c_int32)]
 
 
 class MeshInfo(ctypes.Structure):
@@ -137,6 +138,7 @@ SIGNATURES = [
     ("lbm_batch_remove", _S, [_P, _I32]),
     ("lbm_batch_step", _S, [_P, _I32]),
     ("lbm_batch_autotune", _S, [_P]),
+    ("lbm_batch_tunings", _S, [_P, _P]),
     ("lbm_batch_set_launch", _S, [_P, _I32, _I32, _I32]),
     ("lbm_batch_synchronize", _S, [_P]),
     ("lbm_batch_get_stream", _S, [_P, _P]),
@@ -144,6 +146,8 @@ SIGNATURES = [
     ("lbm_batch_slot_steps", _S, [_P, _I32, _P]),
     ("lbm_batch_set_slot_steps", _S, [_P, _I32, _I64]),
     ("lbm_batch_moments", _S, [_P, _I32, _P, _P, _P]),
+    ("lbm_batch_moments_async", _S, [_P, _I32, _P]),
+    ("lbm_batch_collect", _S, [_P, _I64, _I32, _P, _P, _P, _P]),
     ("lbm_batch_load_populations", _S, [_P, _I32, _P, _I32]),
     ("lbm_batch_retrieve_populations", _S, [_P, _I32, _P, _I32]),
     ("lbm_server_config_init", None, [_P]),

@@ -11,11 +11,19 @@
 // slot, rows ascending; odd steps walk the list backwards (each step starts where the previous
 // one ended, on data still in L2).  The tile shape (V, TX, TY) is picked by the autotuner from
 // timings on the batch itself.
+//
+// Nothing on the serving path waits for the device: adding a slot (flags upload, link words,
+// fluid-cell count, equilibrium), the table uploads before a launch sequence, freeing a slot and
+// reading a slot's moments back through a ticket (lbm_batch_moments_async) are all queued on the
+// batch stream, with host data staged through pinned blocks that are reused once the copy that
+// last used them has completed.  The host can thus prepare the next round of a request loop
+// while the device runs the current one.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -44,6 +52,21 @@ struct Tile {
     int slot, xchunk, y0, pad;
 };
 
+// A pinned host block for asynchronous copies; reusable once `done` (recorded after the last copy
+// that used it) has completed.
+struct PinnedBlock {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaEvent_t done = nullptr;
+};
+
+// An asynchronous read-back of a slot's moments: 3 n floats in a pinned block, ready at `done`.
+struct Pending {
+    size_t block;
+    size_t n;
+    cudaEvent_t done;
+};
+
 struct Slot {
     bool live = false;
     lbm_desc desc{};
@@ -52,12 +75,16 @@ struct Slot {
     void *f[2] = {nullptr, nullptr};
     uint16_t *links = nullptr;
     uint8_t *flags = nullptr;
+    unsigned long long *count_d = nullptr;  // fluid-cell count, behind the flags in their allocation
     int cur = 0;
     int64_t steps_done = 0;
     int64_t limit = -1;  // steps the slot may still take (-1: no limit)
-    int64_t fluid = 0;
+    int64_t fluid = -1;  // -1 until the device count has been read
     size_t bytes = 0;
 };
+
+// bytes of a slot's flag allocation: the flags, padded to 8 bytes, then the fluid-cell count
+size_t flags_bytes(int nx, int ny) { return ((size_t)nx * ny + 7) / 8 * 8 + 8; }
 
 // One block per tile.  The tile's slot descriptor is copied into registers, so no field is re-read
 // from global memory after the population stores.  (A persistent grid-stride loop over the tiles
@@ -126,12 +153,19 @@ struct lbm_batch {
     // tile shape
     int v = 4, tx = 32, ty = 4;
     bool tuned = false;
+    bool fixed = false;      // shape set by lbm_batch_set_launch: never tuned
+    int64_t live_cells = 0;  // cells of the live slots
+    int64_t tuned_cells = 0; // live cells when the shape was last tuned
+    int32_t tunings = 0;
     unsigned sweep = 0;
     int64_t device_bytes = 0;
     // persistent staging for slot I/O and a small result buffer (no allocation per call)
     void *staging = nullptr;
     size_t staging_bytes = 0;
     double *result_d = nullptr;
+    std::vector<PinnedBlock> pinned;
+    std::map<int64_t, Pending> pending;  // read-backs by ticket
+    int64_t next_ticket = 1;
 };
 
 namespace {
@@ -148,6 +182,17 @@ lbm_status bfail(lbm_batch *b, lbm_status s, const std::string &m) {
             return bfail(b, e_ == cudaErrorMemoryAllocation ? LBM_ERR_OOM : LBM_ERR_CUDA,                     \
                          std::string(what) + ": " + cudaGetErrorString(e_));                                  \
     } while (0)
+
+// below this many live cells the batch runs the default shape and does not tune
+constexpr int64_t TUNE_CELLS = (int64_t)1 << 24;
+
+// default tile shape (the autotuner's choice on the mixed serve domains: 16-bit 4 x 32 x 4,
+// FP32 4 x 32 x 2)
+void default_shape(int dtype, int &v, int &tx, int &ty) {
+    v = dtype == LBM_F64 ? 2 : 4;
+    tx = 32;
+    ty = dtype == LBM_F32 ? 2 : 4;
+}
 
 bool shape_ok(int dtype, int v, int tx, int ty) {
     if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256) return false;
@@ -204,6 +249,63 @@ void free_slot(lbm_batch *b, Slot &s) {
     s.flags = nullptr;
 }
 
+bool block_in_use(const lbm_batch *b, size_t k) {
+    for (const auto &kv : b->pending)
+        if (kv.second.block == k) return true;
+    return false;
+}
+
+// A free pinned block of at least n bytes (the smallest that fits; a new one when none is free).
+// Sets *index; the caller records the block's event after queuing the copy that uses it.
+lbm_status pinned_get(lbm_batch *b, size_t n, size_t *index) {
+    size_t best = SIZE_MAX;
+    for (size_t k = 0; k < b->pinned.size(); ++k) {
+        const PinnedBlock &pb = b->pinned[k];
+        if (pb.bytes < n || (best != SIZE_MAX && pb.bytes >= b->pinned[best].bytes)) continue;
+        if (cudaEventQuery(pb.done) != cudaSuccess || block_in_use(b, k)) continue;
+        best = k;
+    }
+    cudaGetLastError();  // cudaEventQuery reports cudaErrorNotReady for blocks still in use
+    if (best == SIZE_MAX) {
+        PinnedBlock pb;
+        pb.bytes = std::max<size_t>(n, (size_t)1 << 20);
+        BCUDA(b, cudaHostAlloc(&pb.p, pb.bytes, cudaHostAllocDefault), "batch: pinned staging");
+        if (cudaEventCreateWithFlags(&pb.done, cudaEventDisableTiming) != cudaSuccess) {
+            cudaFreeHost(pb.p);
+            return bfail(b, LBM_ERR_CUDA, "batch: pinned staging event");
+        }
+        b->pinned.push_back(pb);
+        best = b->pinned.size() - 1;
+    }
+    *index = best;
+    return LBM_OK;
+}
+
+// Copy n host bytes to device memory without waiting: through a pinned block, on the batch stream.
+lbm_status upload_async(lbm_batch *b, void *dst_d, const void *src_h, size_t n, const char *what) {
+    if (n == 0) return LBM_OK;
+    size_t k;
+    lbm_status st = pinned_get(b, n, &k);
+    if (st != LBM_OK) return st;
+    std::memcpy(b->pinned[k].p, src_h, n);
+    BCUDA(b, cudaMemcpyAsync(dst_d, b->pinned[k].p, n, cudaMemcpyHostToDevice, b->stream), what);
+    BCUDA(b, cudaEventRecord(b->pinned[k].done, b->stream), what);
+    return LBM_OK;
+}
+
+// Grow a device table to hold n elements of `size` bytes, stream-ordered (launches queued before
+// keep the old table until they have run).
+lbm_status grow_table(lbm_batch *b, void **table, size_t *cap, size_t n, size_t size, size_t min_cap, const char *what) {
+    if (n <= *cap) return LBM_OK;
+    if (*table) cudaFreeAsync(*table, b->stream);
+    *table = nullptr;
+    *cap = 0;
+    const size_t want = std::max(n + n / 4, min_cap);
+    BCUDA(b, cudaMallocAsync(table, want * size, b->stream), what);
+    *cap = want;
+    return LBM_OK;
+}
+
 // steps slot s takes in a launch sequence of nsteps
 int64_t advance_of(const Slot &s, int64_t nsteps) { return s.limit < 0 ? nsteps : std::min(nsteps, s.limit); }
 
@@ -242,26 +344,16 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
         for (int y0 = 0; y0 < s.desc.ny; y0 += b->ty)
             for (int xc = 0; xc < chunks; ++xc) tiles.push_back(Tile{(int)i, xc, y0, 0});
     }
-    BCUDA(b, cudaStreamSynchronize(b->stream), "batch: synchronize before table upload");
-    if (descs.size() > b->desc_cap) {
-        if (b->desc_d) cudaFree(b->desc_d);
-        b->desc_d = nullptr;
-        b->desc_cap = std::max<size_t>(descs.size(), 64);
-        BCUDA(b, cudaMalloc(&b->desc_d, b->desc_cap * sizeof(SlotDesc)), "batch: descriptor table");
-    }
-    if (retile && tiles.size() > b->tiles_cap) {
-        if (b->tiles_d) cudaFree(b->tiles_d);
-        b->tiles_d = nullptr;
-        b->tiles_cap = std::max<size_t>(tiles.size() + tiles.size() / 4, 1024);
-        BCUDA(b, cudaMalloc(&b->tiles_d, b->tiles_cap * sizeof(Tile)), "batch: tile table");
-    }
-    if (!descs.empty())
-        BCUDA(b, cudaMemcpy(b->desc_d, descs.data(), descs.size() * sizeof(SlotDesc), cudaMemcpyHostToDevice),
-              "batch: upload descriptors");
+    // uploads queued behind the launches that still read the old tables
+    lbm_status st = grow_table(b, (void **)&b->desc_d, &b->desc_cap, descs.size(), sizeof(SlotDesc), 64,
+                               "batch: descriptor table");
+    if (st == LBM_OK)
+        st = upload_async(b, b->desc_d, descs.data(), descs.size() * sizeof(SlotDesc), "batch: upload descriptors");
+    if (st != LBM_OK) return st;
     if (retile) {
-        if (!tiles.empty())
-            BCUDA(b, cudaMemcpy(b->tiles_d, tiles.data(), tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice),
-                  "batch: upload tiles");
+        st = grow_table(b, (void **)&b->tiles_d, &b->tiles_cap, tiles.size(), sizeof(Tile), 1024, "batch: tile table");
+        if (st == LBM_OK) st = upload_async(b, b->tiles_d, tiles.data(), tiles.size() * sizeof(Tile), "batch: upload tiles");
+        if (st != LBM_OK) return st;
         b->ntiles = (int)tiles.size();
     }
     b->dirty = false;
@@ -383,14 +475,14 @@ lbm_status tune(lbm_batch *b) {
     return LBM_OK;
 }
 
+// device staging for slot I/O, grown stream-ordered (work queued before keeps the old buffer)
 lbm_status ensure_staging(lbm_batch *b, size_t bytes) {
-    if (!b->result_d) BCUDA(b, cudaMalloc(&b->result_d, 16 * sizeof(double)), "batch: result buffer");
+    if (!b->result_d) BCUDA(b, cudaMallocAsync((void **)&b->result_d, 16 * sizeof(double), b->stream), "batch: result buffer");
     if (b->staging_bytes >= bytes) return LBM_OK;
-    BCUDA(b, cudaStreamSynchronize(b->stream), "batch: synchronize before staging resize");
-    if (b->staging) cudaFree(b->staging);
+    if (b->staging) cudaFreeAsync(b->staging, b->stream);
     b->staging = nullptr;
     b->staging_bytes = 0;
-    BCUDA(b, cudaMalloc(&b->staging, bytes), "batch: staging");
+    BCUDA(b, cudaMallocAsync(&b->staging, bytes, b->stream), "batch: staging");
     b->staging_bytes = bytes;
     return LBM_OK;
 }
@@ -399,6 +491,8 @@ Slot *get_slot(lbm_batch *b, int32_t slot) {
     if (!b || slot < 0 || (size_t)slot >= b->slots.size() || !b->slots[slot].live) return nullptr;
     return &b->slots[slot];
 }
+
+
 
 }  // namespace
 
@@ -432,7 +526,7 @@ LBM_API lbm_status lbm_batch_create(int32_t dtype, int32_t device, void *stream,
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
     cudaGetLastError();
-    b->v = dtype == LBM_F64 ? 2 : 4;
+    default_shape(dtype, b->v, b->tx, b->ty);
     *out = b;
     return LBM_OK;
 }
@@ -447,6 +541,10 @@ LBM_API lbm_status lbm_batch_destroy(lbm_batch *b) {
     cudaFree(b->tiles_d);
     cudaFree(b->staging);
     cudaFree(b->result_d);
+    for (PinnedBlock &pb : b->pinned) {
+        cudaFreeHost(pb.p);
+        cudaEventDestroy(pb.done);
+    }
     if (b->own_stream) cudaStreamDestroy(b->stream);
     delete b;
     return LBM_OK;
@@ -457,7 +555,7 @@ LBM_API const char *lbm_batch_last_error(const lbm_batch *b) { return b ? b->err
 LBM_API int64_t lbm_batch_slot_bytes(int32_t dtype, int32_t nx, int32_t ny) {
     if (nx < 1 || ny < 1 || dsize(dtype) == 0) return -1;
     const int64_t pitch = ((int64_t)nx + 31) / 32 * 32;
-    return 2 * 9 * pitch * ny * (int64_t)dsize(dtype) + pitch * ny * 2 + (int64_t)nx * ny;
+    return 2 * 9 * pitch * ny * (int64_t)dsize(dtype) + pitch * ny * 2 + (int64_t)flags_bytes(nx, ny);
 }
 
 LBM_API lbm_status lbm_batch_add(lbm_batch *b, const lbm_desc *desc, const uint8_t *host_flags, int32_t *slot_out) {
@@ -480,10 +578,11 @@ LBM_API lbm_status lbm_batch_add(lbm_batch *b, const lbm_desc *desc, const uint8
         free_slot(b, s);
         cudaStreamSynchronize(b->stream);
     };
+    const size_t ncell = (size_t)desc->nx * desc->ny;
     cudaError_t e = cudaMallocAsync(&s.f[0], pop, b->stream);
     if (e == cudaSuccess) e = cudaMallocAsync(&s.f[1], pop, b->stream);
     if (e == cudaSuccess) e = cudaMallocAsync(&s.links, (size_t)s.plane * sizeof(uint16_t), b->stream);
-    if (e == cudaSuccess) e = cudaMallocAsync(&s.flags, (size_t)desc->nx * desc->ny, b->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(&s.flags, flags_bytes(desc->nx, desc->ny), b->stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
         cleanup();
@@ -491,27 +590,29 @@ LBM_API lbm_status lbm_batch_add(lbm_batch *b, const lbm_desc *desc, const uint8
                      std::string("lbm_batch_add: ") + cudaGetErrorString(e));
     }
     s.live = true;
-    // flags, link words, equilibrium at rho = 1, u = 0 through the single-domain kernels
+    s.count_d = reinterpret_cast<unsigned long long *>(s.flags + flags_bytes(desc->nx, desc->ny) - 8);
+    // flags, link words, fluid count, equilibrium at rho = 1, u = 0 through the single-domain
+    // kernels, all queued without waiting
     if (host_flags) {
-        for (int64_t i = 0; i < (int64_t)desc->nx * desc->ny; ++i)
+        for (size_t i = 0; i < ncell; ++i)
             if (host_flags[i] > LBM_MOVING_WALL) {
                 cleanup();
                 return bfail(b, LBM_ERR_INVALID, "lbm_batch_add: flag values must be 0, 1 or 2");
             }
-        e = cudaMemcpyAsync(s.flags, host_flags, (size_t)desc->nx * desc->ny, cudaMemcpyHostToDevice, b->stream);
+        if (upload_async(b, s.flags, host_flags, ncell, "lbm_batch_add: upload flags") != LBM_OK) {
+            const std::string m = b->err;
+            cleanup();
+            return bfail(b, LBM_ERR_CUDA, m);
+        }
     } else {
-        e = cudaMemsetAsync(s.flags, 0, (size_t)desc->nx * desc->ny, b->stream);
+        e = cudaMemsetAsync(s.flags, 0, ncell, b->stream);
     }
     // link words of the row padding stay 0 (the vectorised step reads them)
     if (e == cudaSuccess) e = cudaMemsetAsync(s.links, 0, (size_t)s.plane * sizeof(uint16_t), b->stream);
-    if (e == cudaSuccess && ensure_staging(b, 0) != LBM_OK) e = cudaErrorMemoryAllocation;
     if (e == cudaSuccess) {
         CtxView v(b, s);
-        v.c.result_d = b->result_d;
-        e = d2q9_build_links(&v.c);
+        e = d2q9_build_links_async(&v.c, s.count_d);
         if (e == cudaSuccess) e = d2q9_init_equilibrium(&v.c, nullptr, nullptr, nullptr);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
-        s.fluid = v.c.fluid_cells;
     }
     if (e != cudaSuccess) {
         cleanup();
@@ -529,6 +630,7 @@ LBM_API lbm_status lbm_batch_add(lbm_batch *b, const lbm_desc *desc, const uint8
     }
     b->slots[id] = s;
     b->device_bytes += (int64_t)s.bytes;
+    b->live_cells += (int64_t)desc->nx * desc->ny;
     b->dirty = true;
     b->tiles_dirty = true;
     *slot_out = id;
@@ -540,6 +642,7 @@ LBM_API lbm_status lbm_batch_remove(lbm_batch *b, int32_t slot) {
     if (!s) return bfail(b, LBM_ERR_INVALID, "lbm_batch_remove: no such slot");
     free_slot(b, *s);  // ordered after the queued steps that may still read the slot
     b->device_bytes -= (int64_t)s->bytes;
+    b->live_cells -= (int64_t)s->desc.nx * s->desc.ny;
     *s = Slot();
     b->dirty = true;
     b->tiles_dirty = true;
@@ -555,6 +658,7 @@ LBM_API lbm_status lbm_batch_set_launch(lbm_batch *b, int32_t cells_per_thread, 
     b->tx = block_threads;
     b->ty = rows_per_block;
     b->tuned = true;
+    b->fixed = true;
     b->dirty = true;
     b->tiles_dirty = true;
     return LBM_OK;
@@ -563,7 +667,19 @@ LBM_API lbm_status lbm_batch_set_launch(lbm_batch *b, int32_t cells_per_thread, 
 LBM_API lbm_status lbm_batch_autotune(lbm_batch *b) {
     if (!b) return lbm::set_thread_error(LBM_ERR_INVALID, "null batch");
     BCUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
-    return tune(b);
+    b->fixed = false;
+    lbm_status st = tune(b);
+    if (st == LBM_OK) {
+        b->tuned_cells = b->live_cells;
+        ++b->tunings;
+    }
+    return st;
+}
+
+LBM_API lbm_status lbm_batch_tunings(lbm_batch *b, int32_t *count) {
+    if (!b || !count) return lbm::set_thread_error(LBM_ERR_INVALID, "null argument");
+    *count = b->tunings;
+    return LBM_OK;
 }
 
 LBM_API lbm_status lbm_batch_step(lbm_batch *b, int32_t nsteps) {
@@ -571,9 +687,15 @@ LBM_API lbm_status lbm_batch_step(lbm_batch *b, int32_t nsteps) {
     if (nsteps < 0) return bfail(b, LBM_ERR_INVALID, "nsteps must be >= 0");
     if (nsteps == 0) return LBM_OK;
     BCUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
-    if (!b->tuned) {
+    // Tuning on a handful of small slots would fix the shape for the mix that follows: the batch
+    // keeps the default shape until it holds TUNE_CELLS cells, tunes then, and once more if it
+    // grows to four times the cells it was tuned on.
+    if (!b->fixed && b->live_cells >= TUNE_CELLS &&
+        (!b->tuned || (b->tunings < 2 && b->live_cells >= 4 * b->tuned_cells))) {
         lbm_status st = tune(b);
         if (st != LBM_OK) return st;
+        b->tuned_cells = b->live_cells;
+        ++b->tunings;
     }
     lbm_status st = rebuild(b, nsteps);
     if (st != LBM_OK) return st;
@@ -618,6 +740,13 @@ LBM_API lbm_status lbm_batch_get_stream(lbm_batch *b, void **stream) {
 LBM_API lbm_status lbm_batch_info(lbm_batch *b, int64_t out[8]) {
     if (!b || !out) return lbm::set_thread_error(LBM_ERR_INVALID, "null argument");
     int64_t live = 0, cells = 0, fluid = 0;
+    for (Slot &s : b->slots)
+        if (s.live && s.fluid < 0) {  // read the counts queued by lbm_batch_add
+            unsigned long long h = 0;
+            BCUDA(b, cudaMemcpyAsync(&h, s.count_d, sizeof(h), cudaMemcpyDeviceToHost, b->stream), "batch info");
+            BCUDA(b, cudaStreamSynchronize(b->stream), "batch info");
+            s.fluid = (int64_t)h;
+        }
     for (const Slot &s : b->slots)
         if (s.live) {
             ++live;
@@ -635,23 +764,62 @@ LBM_API lbm_status lbm_batch_info(lbm_batch *b, int64_t out[8]) {
     return LBM_OK;
 }
 
-// Per-slot host I/O through the single-domain conversion kernels on a view of the slot
-LBM_API lbm_status lbm_batch_moments(lbm_batch *b, int32_t slot, float *rho, float *ux, float *uy) {
+// Per-slot host I/O through the single-domain conversion kernels on a view of the slot.
+// Moments: density and velocity into device staging, then into a pinned block, queued; the ticket
+// is collected (copied into the caller's arrays) once the copy has completed.
+LBM_API lbm_status lbm_batch_moments_async(lbm_batch *b, int32_t slot, int64_t *ticket) {
     Slot *s = get_slot(b, slot);
-    if (!s) return bfail(b, LBM_ERR_INVALID, "lbm_batch_moments: no such slot");
+    if (!s || !ticket) return bfail(b, LBM_ERR_INVALID, "lbm_batch_moments_async: no such slot or null ticket");
     BCUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
     const size_t n = (size_t)s->desc.nx * s->desc.ny;
     lbm_status st = ensure_staging(b, 3 * n * sizeof(float));
     if (st != LBM_OK) return st;
     float *buf = static_cast<float *>(b->staging);
+    size_t k;
+    if ((st = pinned_get(b, 3 * n * sizeof(float), &k)) != LBM_OK) return st;
     CtxView v(b, *s);
     cudaError_t e = d2q9_moments(&v.c, buf, buf + n, buf + 2 * n);
-    float *host[3] = {rho, ux, uy};
-    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
-        if (host[k]) e = cudaMemcpyAsync(host[k], buf + k * n, n * sizeof(float), cudaMemcpyDeviceToHost, b->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
-    BCUDA(b, e, "lbm_batch_moments");
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->pinned[k].p, buf, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b->pinned[k].done, b->stream);
+    BCUDA(b, e, "lbm_batch_moments_async");
+    const int64_t id = b->next_ticket++;
+    b->pending[id] = Pending{k, n, b->pinned[k].done};
+    *ticket = id;
     return LBM_OK;
+}
+
+LBM_API lbm_status lbm_batch_collect(lbm_batch *b, int64_t ticket, int32_t wait, float *rho, float *ux, float *uy,
+                                     int32_t *ready) {
+    if (!b || !ready) return lbm::set_thread_error(LBM_ERR_INVALID, "lbm_batch_collect: null argument");
+    auto it = b->pending.find(ticket);
+    if (it == b->pending.end()) return bfail(b, LBM_ERR_INVALID, "lbm_batch_collect: no such ticket");
+    *ready = 0;
+    const Pending pd = it->second;
+    if (wait) {
+        BCUDA(b, cudaEventSynchronize(pd.done), "lbm_batch_collect");
+    } else {
+        const cudaError_t q = cudaEventQuery(pd.done);
+        if (q == cudaErrorNotReady) {
+            cudaGetLastError();
+            return LBM_OK;
+        }
+        BCUDA(b, q, "lbm_batch_collect");
+    }
+    const float *src = static_cast<const float *>(b->pinned[pd.block].p);
+    float *host[3] = {rho, ux, uy};
+    for (int c = 0; c < 3; ++c)
+        if (host[c]) std::memcpy(host[c], src + c * pd.n, pd.n * sizeof(float));
+    b->pending.erase(it);
+    *ready = 1;
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_batch_moments(lbm_batch *b, int32_t slot, float *rho, float *ux, float *uy) {
+    int64_t ticket = 0;
+    lbm_status st = lbm_batch_moments_async(b, slot, &ticket);
+    if (st != LBM_OK) return st;
+    int32_t ready = 0;
+    return lbm_batch_collect(b, ticket, 1, rho, ux, uy, &ready);
 }
 
 LBM_API lbm_status lbm_batch_retrieve_populations(lbm_batch *b, int32_t slot, void *host, int32_t host_dtype) {

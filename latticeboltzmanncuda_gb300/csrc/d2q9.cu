@@ -580,6 +580,17 @@ inline dim3 row_grid(const lbm_ctx *ctx, int threads) {
 
 }  // namespace
 
+cudaError_t d2q9_build_links_async(lbm_ctx *ctx, unsigned long long *count_d) {
+    const lbm_desc &d = ctx->desc;
+    build_links_kernel<<<row_grid(ctx, 256), 256, 0, ctx->stream>>>(ctx->flags_d, ctx->links_d, d.nx, d.ny,
+                                                                    ctx->pitch, d.periodic);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemsetAsync(count_d, 0, sizeof(unsigned long long), ctx->stream);
+    if (e != cudaSuccess) return e;
+    count_fluid_kernel<<<256, 256, 0, ctx->stream>>>(ctx->flags_d, (int64_t)d.nx * d.ny, count_d);
+    return cudaGetLastError();
+}
+
 cudaError_t d2q9_build_links(lbm_ctx *ctx) {
     const lbm_desc &d = ctx->desc;
     build_links_kernel<<<row_grid(ctx, 256), 256, 0, ctx->stream>>>(ctx->flags_d, ctx->links_d, d.nx, d.ny,

@@ -144,6 +144,8 @@ cudaError_t d2q9_build_links(lbm_ctx *ctx);
 cudaError_t d2q9_init_equilibrium(lbm_ctx *ctx, const float *rho_d, const float *ux_d, const float *uy_d);
 cudaError_t d2q9_step(lbm_ctx *ctx, int nsteps);
 cudaError_t d2q9_autotune(lbm_ctx *ctx, bool force_retune);
+// link words and the fluid-cell count (into count_d) without waiting for them
+cudaError_t d2q9_build_links_async(lbm_ctx *ctx, unsigned long long *count_d);
 // read and clear the bulk-copy pipeline's status bits (synchronises the context's stream)
 unsigned d2q9_take_pipe_status(lbm_ctx *ctx);
 bool d2q9_shape_valid(const lbm_ctx *ctx, int v, int tx, int ty, int pol);

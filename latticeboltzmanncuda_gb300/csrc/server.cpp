@@ -13,8 +13,14 @@
 //             batch slot's step budget, so one that finishes mid-round just stops there (its blocks
 //             exit at once); requests that arrive meanwhile join at the next round boundary, so
 //             their work overlaps on the device with the running ones
-//   retire    a finished solve's density and velocity are read back into the request's host
-//             buffers (if given), its slot is freed and its completion time recorded
+//   retire    the step counts are known on the host, so a solve that finishes in a round is retired
+//             as soon as that round is queued: the read-back of its density and velocity is queued
+//             behind the round (a batch ticket) and its slot freed, stream-ordered; the request
+//             completes when the host has collected the ticket into its buffers
+//   pipeline  batch work is only queued, never waited for, except that the loop keeps at most one
+//             round queued ahead of the one running: after queuing round r it waits for round
+//             r - 1, so admission, table rebuilds and retirement of round r + 1 are prepared on the
+//             host while the device runs round r
 //
 // States stay on the device from admission to completion.  A wall-clock limit (time_limit) bounds
 // the whole run: requests not finished by then end with LBM_ERR_TIMEOUT.
@@ -25,6 +31,8 @@
 #include <string>
 #include <thread>
 #include <vector>
+
+#include <cuda_runtime_api.h>
 
 #include "lbm_capi.h"
 
@@ -114,12 +122,54 @@ LBM_API lbm_status lbm_server_run(lbm_server *s, const lbm_request *reqs, int64_
     lbm_status run_status = LBM_OK;
     const Clock::time_point t0 = Clock::now();
 
+    struct Retiring {
+        int64_t req, ticket;
+    };
+    std::deque<Retiring> retiring;
+    cudaStream_t stream = nullptr;
+    // per round: an event before its launch sequence and one after (timed: device seconds of the
+    // rounds), two rounds in flight
+    cudaEvent_t round_start[2] = {nullptr, nullptr}, round_done[2] = {nullptr, nullptr};
+    bool events_ok = lbm_batch_get_stream(s->batch, reinterpret_cast<void **>(&stream)) == LBM_OK;
+    for (int k = 0; k < 2 && events_ok; ++k)
+        events_ok = cudaEventCreate(&round_start[k]) == cudaSuccess && cudaEventCreate(&round_done[k]) == cudaSuccess;
+    auto destroy_events = [&]() {
+        for (int k = 0; k < 2; ++k) {
+            if (round_start[k]) cudaEventDestroy(round_start[k]);
+            if (round_done[k]) cudaEventDestroy(round_done[k]);
+        }
+    };
+    if (!events_ok) {
+        destroy_events();
+        cudaGetLastError();
+        return lbm::set_thread_error(LBM_ERR_CUDA, "lbm_server_run: round events");
+    }
+
     auto finish = [&](int64_t r, int32_t status) {
         results[r].status = status;
         results[r].finished = seconds_since(t0);
         ++done;
     };
+    // collect the read-backs that have landed (all of them, waiting, with wait_all)
+    auto collect = [&](bool wait_all) -> lbm_status {
+        while (!retiring.empty()) {
+            const Retiring rt = retiring.front();
+            const lbm_request &q = reqs[rt.req];
+            int32_t ready = 0;
+            const lbm_status c = lbm_batch_collect(s->batch, rt.ticket, wait_all ? 1 : 0, q.out_rho, q.out_ux, q.out_uy, &ready);
+            if (c != LBM_OK) {
+                retiring.pop_front();
+                finish(rt.req, c);
+                return c;
+            }
+            if (!ready) break;  // tickets complete in queue order
+            retiring.pop_front();
+            finish(rt.req, LBM_OK);
+        }
+        return LBM_OK;
+    };
 
+    int64_t round = 0;
     while (done < n) {
         double now = seconds_since(t0);
         if (cfg.time_limit > 0 && now > cfg.time_limit) {
@@ -128,7 +178,7 @@ LBM_API lbm_status lbm_server_run(lbm_server *s, const lbm_request *reqs, int64_
         }
         while (next < order.size() && reqs[order[next]].arrival <= now) waiting.push_back(order[next++]);
 
-        // admission, first come first served
+        // admission, first come first served (queued behind the running round)
         while (!waiting.empty()) {
             const int64_t r = waiting.front();
             const lbm_request &q = reqs[r];
@@ -175,11 +225,6 @@ LBM_API lbm_status lbm_server_run(lbm_server *s, const lbm_request *reqs, int64_
             }
             results[r].slot = slot;
             lbm_batch_set_slot_steps(s->batch, slot, q.steps);
-            if (q.steps == 0) {
-                lbm_batch_remove(s->batch, slot);
-                finish(r, LBM_OK);
-                continue;
-            }
             used += bytes;
             live.push_back(Live{r, slot, q.steps, bytes});
             st.peak_bytes = std::max(st.peak_bytes, used);
@@ -187,6 +232,10 @@ LBM_API lbm_status lbm_server_run(lbm_server *s, const lbm_request *reqs, int64_
         }
 
         if (live.empty()) {
+            if (!retiring.empty()) {  // nothing to queue: wait for the read-backs in flight
+                if ((run_status = collect(true)) != LBM_OK) break;
+                continue;
+            }
             if (next < order.size()) {
                 // idle until the next arrival (bounded sleeps; the time limit is checked each pass)
                 const double wait = reqs[order[next]].arrival - seconds_since(t0);
@@ -200,14 +249,16 @@ LBM_API lbm_status lbm_server_run(lbm_server *s, const lbm_request *reqs, int64_
         int64_t longest = 0;
         for (const Live &l : live) longest = std::max(longest, l.remaining);
         const int64_t k = std::min<int64_t>(cfg.round_steps, longest);
-        lbm_status e = lbm_batch_step(s->batch, (int32_t)k);
-        if (e == LBM_OK) e = lbm_batch_synchronize(s->batch);
+        lbm_status e = cudaEventRecord(round_start[round & 1], stream) == cudaSuccess ? LBM_OK : LBM_ERR_CUDA;
+        if (e == LBM_OK && k > 0) e = lbm_batch_step(s->batch, (int32_t)k);
+        if (e == LBM_OK && cudaEventRecord(round_done[round & 1], stream) != cudaSuccess) e = LBM_ERR_CUDA;
         if (e != LBM_OK) {
             s->err = lbm_batch_last_error(s->batch);
             run_status = e;
             break;
         }
         ++st.rounds;
+        // retire the solves this round finishes: read-back and free queued behind it
         std::vector<Live> still;
         still.reserve(live.size());
         for (Live &l : live) {
@@ -218,14 +269,50 @@ LBM_API lbm_status lbm_server_run(lbm_server *s, const lbm_request *reqs, int64_
                 still.push_back(l);
                 continue;
             }
-            const lbm_request &q = reqs[l.req];
-            lbm_status o = LBM_OK;
-            if (q.out_rho || q.out_ux || q.out_uy) o = lbm_batch_moments(s->batch, l.slot, q.out_rho, q.out_ux, q.out_uy);
+            int64_t ticket = 0;
+            const lbm_status o = lbm_batch_moments_async(s->batch, l.slot, &ticket);
             lbm_batch_remove(s->batch, l.slot);
             used -= l.bytes;
-            finish(l.req, o);
+            if (o != LBM_OK)
+                finish(l.req, o);
+            else
+                retiring.push_back(Retiring{l.req, ticket});
         }
         live.swap(still);
+        // at most one round queued ahead of the running one
+        if (round > 0) {
+            const int p = (int)((round - 1) & 1);
+            float ms = 0.0f;
+            if (cudaEventSynchronize(round_done[p]) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, round_start[p], round_done[p]) != cudaSuccess) {
+                cudaGetLastError();
+                s->err = "lbm_server_run: a round failed on the device";
+                run_status = LBM_ERR_CUDA;
+                break;
+            }
+            st.round_seconds += ms * 1e-3;
+        }
+        ++round;
+        if ((run_status = collect(false)) != LBM_OK) break;
+    }
+    if (run_status == LBM_OK && round > 0) {  // the last round's device time
+        const int p = (int)((round - 1) & 1);
+        float ms = 0.0f;
+        if (cudaEventSynchronize(round_done[p]) == cudaSuccess &&
+            cudaEventElapsedTime(&ms, round_start[p], round_done[p]) == cudaSuccess)
+            st.round_seconds += ms * 1e-3;
+        cudaGetLastError();
+    }
+    if (run_status == LBM_OK) run_status = collect(true);
+    else lbm_batch_synchronize(s->batch);
+    {
+        int64_t info[8];
+        if (lbm_batch_info(s->batch, info) == LBM_OK) {
+            st.tile_shape[0] = (int32_t)info[4];
+            st.tile_shape[1] = (int32_t)info[5];
+            st.tile_shape[2] = (int32_t)info[6];
+        }
+        lbm_batch_tunings(s->batch, &st.tunings);
     }
 
     // anything left ends with the run's status (time limit or a device error)
@@ -237,6 +324,9 @@ LBM_API lbm_status lbm_server_run(lbm_server *s, const lbm_request *reqs, int64_
         if (results[r].finished < 0) finish(r, run_status == LBM_OK ? LBM_ERR_STATE : run_status);
     for (; next < order.size(); ++next)
         if (results[order[next]].finished < 0) finish(order[next], run_status == LBM_OK ? LBM_ERR_STATE : run_status);
+    for (const Retiring &rt : retiring)
+        if (results[rt.req].finished < 0) finish(rt.req, run_status == LBM_OK ? LBM_ERR_STATE : run_status);
+    destroy_events();
     st.makespan = seconds_since(t0);
     if (stats) *stats = st;
     if (run_status != LBM_OK) {

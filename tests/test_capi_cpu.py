@@ -148,4 +148,6 @@ def test_server_rejects_bad_configuration():
         setattr(c, field, value)
         assert L.lbm_server_create(ctypes.byref(c), ctypes.byref(srv)) == capi.ERR_INVALID
     assert L.lbm_batch_slot_bytes(capi.F32, 0, 8) == -1
-    assert L.lbm_batch_slot_bytes(capi.F16S, 64, 64) == 2 * 9 * 64 * 64 * 2 + 64 * 64 * 2 + 64 * 64
+    # two population buffers, link words, flags padded to 8 bytes and the 8-byte fluid count
+    assert L.lbm_batch_slot_bytes(capi.F16S, 64, 64) == 2 * 9 * 64 * 64 * 2 + 64 * 64 * 2 + 64 * 64 + 8
+    assert L.lbm_batch_slot_bytes(capi.F32, 33, 3) == 2 * 9 * 64 * 3 * 4 + 64 * 3 * 2 + 104 + 8

@@ -160,6 +160,33 @@ def test_batch_autotune_and_moments():
         assert ux[sp[0][1] - 2, sp[0][0] // 2] > 0  # the lid drags the fluid
 
 
+def test_moments_tickets_equal_moments_and_survive_removal():
+    """lbm_batch_moments_async queues the read-back: its ticket yields the same arrays as the
+    waiting read-back even when the slot is removed and others keep stepping before it is
+    collected, and collecting without waiting eventually returns the result."""
+    sp = specs()
+    with lbm.Batch("f16s") as B:
+        slots = [B.add(*s[:4], s[4], s[5], s[6]) for s in sp]
+        B.set_slot_steps(slots[1], 9)
+        B.step(25)
+        want = [B.moments(sl) for sl in slots[:3]]
+        tickets = [B.moments_async(sl) for sl in slots[:3]]
+        B.remove(slots[0])
+        B.step(40)  # the others advance; slot 1 has used its budget and stays put
+        first = B.collect(tickets[0], wait=False)
+        got = [B.collect(t) for t in tickets[1:]]
+        while first is None:
+            first = B.collect(tickets[0], wait=False)
+        got.insert(0, first)
+        for w, g in zip(want, got):
+            for a, b in zip(w, g):
+                assert np.array_equal(a, b)
+        assert np.array_equal(B.moments(slots[1])[1], want[1][1])  # slot 1 stopped at its budget
+        with pytest.raises(lbm.LBMError):
+            B.collect(tickets[1])  # a ticket is collected once
+        assert B.info()["slots"] == len(sp) - 1
+
+
 def test_batch_rejects_bad_input():
     with lbm.Batch("f32") as B:
         with pytest.raises(lbm.LBMError):

@@ -77,12 +77,21 @@ def test_budget_limits_live_solves():
 
 
 def test_slot_limit_serialises():
+    """With one slot the solves run one after another in arrival order: a request is admitted
+    once the previous one has been retired (its read-back and free queued behind its last round,
+    so the device never holds two), and they complete in the same order, each equal to its solo
+    run."""
     reqs = make_requests(5)
-    results, stats, status = lbm.serve(reqs, max_slots=1, round_steps=1000)
+    results, stats, status = lbm.serve(reqs, max_slots=1, round_steps=1000, outputs=True)
     assert status == capi.OK and stats["peak_slots"] == 1
-    done = sorted((r["admitted"], r["finished"]) for r in results)
-    for (a0, f0), (a1, _) in zip(done, done[1:]):
-        assert a1 >= f0 - 1e-6  # one solve at a time
+    by_arrival = sorted(range(len(reqs)), key=lambda i: reqs[i].arrival)
+    adm = [results[i]["admitted"] for i in by_arrival]
+    fin = [results[i]["finished"] for i in by_arrival]
+    assert adm == sorted(adm) and fin == sorted(fin)
+    assert all(a <= f for a, f in zip(adm, fin))
+    for i in by_arrival:
+        for got, want in zip(results[i]["moments"], solo(reqs[i], "f32")):
+            assert np.array_equal(got, want)
 
 
 def test_over_budget_and_invalid_requests_fail_alone():
