@@ -193,13 +193,56 @@ __host__ __device__ constexpr double kW(int k) {
 __host__ __device__ constexpr float kWhi(int k) { return (float)kW(k); }
 __host__ __device__ constexpr float kWlo(int k) { return (float)(kW(k) - (double)(float)kW(k)); }
 __host__ __device__ constexpr int wclass(int i) { return i == 0 ? 0 : (i < 7 ? 1 : (i < 19 ? 2 : 3)); }
+// the n-th direction i (0 < i < opposite(i)) that stands for a pair of opposite directions (13 pairs)
+__host__ __device__ constexpr int pair_rep(int n) {
+    for (int i = 1; i < 27; ++i)
+        if (i < opp27(i) && n-- == 0) return i;
+    return -1;
+}
+
+// The float-float helpers are written once for T = float and T = float2: a float2 carries two
+// independent evaluations (two pairs of directions) through the paired FP32 instructions of sm_100+
+// (__fadd2_rn, __fmul2_rn, __ffma2_rn), whose every lane rounds as the scalar instruction, so both
+// forms give the same bits.  a - b is a + (-b), the same IEEE value.
+__device__ __forceinline__ float ff_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float ff_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float ff_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float ff_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float ff_neg(float a) { return -a; }
+__device__ __forceinline__ float ff_abs(float a) { return fabsf(a); }
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 ff_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 ff_sub(float2 a, float2 b) { return __fadd2_rn(a, ff_neg(b)); }
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 ff_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 ff_abs(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
+template <class T>
+__device__ __forceinline__ T ff_bc(float c);
+template <>
+__device__ __forceinline__ float ff_bc<float>(float c) { return c; }
+template <>
+__device__ __forceinline__ float2 ff_bc<float2>(float c) { return make_float2(c, c); }
+
+// per-lane flags of T
+struct Ok2 {
+    bool x, y;
+};
+template <class T>
+struct OkOf {
+    using type = bool;
+};
+template <>
+struct OkOf<float2> {
+    using type = Ok2;
+};
 
 // s + e == a + b exactly
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-    s = __fadd_rn(a, b);
-    const float bv = __fsub_rn(s, a);
-    const float av = __fsub_rn(s, bv);
-    e = __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
+template <class T>
+__device__ __forceinline__ void two_sum(T a, T b, T &s, T &e) {
+    s = ff_add(a, b);
+    const T bv = ff_sub(s, a);
+    const T av = ff_sub(s, bv);
+    e = ff_add(ff_sub(a, av), ff_sub(b, bv));
 }
 
 // the reference's expression, FP64 (the fallback and the LBM_EQ_FP64 path)
@@ -210,49 +253,69 @@ __device__ __forceinline__ float eq_fp64(int k, float density, float ct, float u
 // ph + pl: W_k * rho within 2^-47; c1 + c1e == 1.5 usq exactly.  Returns the FP32 rounding of the
 // float-float value; ok says whether it is proven equal to the FP64 evaluation.
 // s + e == a + b exactly when |a| >= |b| (Dekker's fast two-sum)
-__device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &e) {
-    s = __fadd_rn(a, b);
-    e = __fsub_rn(b, __fsub_rn(s, a));
+template <class T>
+__device__ __forceinline__ void fast_two_sum(T a, T b, T &s, T &e) {
+    s = ff_add(a, b);
+    e = ff_sub(b, ff_sub(s, a));
+}
+
+// accept r when |E_ff - E_fp64| <= t (t = |d| + m rounded up by RN's monotonicity) keeps the FP64
+// value strictly inside r's FP32 rounding interval: t below half the smaller gap next to r
+// (2^e * 2^-24, or 2^-25 at a power of two), r normal and far from underflow, finite
+__device__ __forceinline__ bool ff_accept(float r, float t) {
+    const uint32_t rb = __float_as_uint(r) & 0x7fffffffu;
+    const uint32_t ex = rb & 0x7f800000u;
+    const float half_gap = __fmul_rn(__uint_as_float(ex), (rb & 0x7fffffu) ? 0x1p-24f : 0x1p-25f);
+    return ex >= (67u << 23) && ex < 0x7f800000u && t < half_gap;
+}
+__device__ __forceinline__ void ff_accept(float r, float t, bool &ok) { ok = ff_accept(r, t); }
+__device__ __forceinline__ void ff_accept(float2 r, float2 t, Ok2 &ok) {
+    ok.x = ff_accept(r.x, t.x);
+    ok.y = ff_accept(r.y, t.y);
 }
 
 // E = (ph + pl) * (1 + s2 + lo) rounded to FP32, with the acceptance test against the bound m on
 // |E_ff - E_fp64| (see above).
-__device__ __forceinline__ float ff_finish(float ph, float pl, float m, float s2, float lo, bool &ok) {
-    float th, e3;
-    two_sum(1.0f, s2, th, e3);
-    const float tl = __fadd_rn(e3, lo);                                   // T = th + tl
-    const float eh = __fmul_rn(ph, th);
-    const float el = __fmaf_rn(ph, tl, __fmaf_rn(pl, th, __fmaf_rn(ph, th, -eh)));
-    const float r = __fadd_rn(eh, el);
-    const float d = __fadd_rn(__fsub_rn(eh, r), el);                      // (eh + el) - r
-    const uint32_t rb = __float_as_uint(r) & 0x7fffffffu;
-    const uint32_t ex = rb & 0x7f800000u;
-    // half the smaller gap next to r (2^e * 2^-24, or 2^-25 at a power of two)
-    const float half_gap = __fmul_rn(__uint_as_float(ex), (rb & 0x7fffffu) ? 0x1p-24f : 0x1p-25f);
-    ok = ex >= (67u << 23) && ex < 0x7f800000u && __fadd_rn(fabsf(d), m) < half_gap;
+template <class T>
+__device__ __forceinline__ T ff_finish(T ph, T pl, T m, T s2, T lo, typename OkOf<T>::type &ok) {
+    T th, e3;
+    two_sum(ff_bc<T>(1.0f), s2, th, e3);
+    const T tl = ff_add(e3, lo);                                          // T = th + tl
+    const T eh = ff_mul(ph, th);
+    const T el = ff_fma(ph, tl, ff_fma(pl, th, ff_fma(ph, th, ff_neg(eh))));
+    const T r = ff_add(eh, el);
+    const T d = ff_add(ff_sub(eh, r), el);                                // (eh + el) - r
+    ff_accept(r, ff_add(ff_abs(d), m), ok);
     return r;
 }
 
+__device__ __forceinline__ bool ok_and(bool a, bool b) { return a && b; }
+__device__ __forceinline__ Ok2 ok_and(Ok2 a, Ok2 b) { return Ok2{a.x && b.x, a.y && b.y}; }
+__device__ __forceinline__ bool ab_ok(float a, float b) { return fabsf(a) >= b; }
+__device__ __forceinline__ Ok2 ab_ok(float2 a, float2 b) { return Ok2{fabsf(a.x) >= b.x, fabsf(a.y) >= b.y}; }
+
 // The pair of opposite directions (c . u = ct and -ct) shares ct^2, B and the bound: mk = |ph| 2^-42,
 // c1p = 1 + 1.5 usq rounded (M = 1 + |A| + B + C up to rounding, well inside the bound's margin).
-__device__ __forceinline__ void eq_ff_pair(float ph, float pl, float mk, float c1, float c1e, float c1p, float ct,
-                                           float &rp, bool &okp, float &rn, bool &okn) {
-    const float a = __fmul_rn(3.0f, ct), ae = __fmaf_rn(3.0f, ct, -a);      // A = 3 ct (for -ct: -a, -ae)
-    const float p = __fmul_rn(ct, ct), pe = __fmaf_rn(ct, ct, -p);         // ct^2
-    const float b = __fmul_rn(4.5f, p), be = __fmaf_rn(4.5f, p, -b);       // B = 4.5 ct^2 = b + be + 4.5 pe
-    const float bb = __fsub_rn(__fadd_rn(be, __fmul_rn(4.5f, pe)), c1e);   // low parts of B - C
-    const float m = __fmul_rn(mk, __fadd_rn(__fadd_rn(c1p, fabsf(a)), b));
+template <class T>
+__device__ __forceinline__ void eq_ff_pair(T ph, T pl, T mk, T c1, T c1e, T c1p, T ct, T &rp,
+                                           typename OkOf<T>::type &okp, T &rn, typename OkOf<T>::type &okn) {
+    const T three = ff_bc<T>(3.0f), four5 = ff_bc<T>(4.5f);
+    const T a = ff_mul(three, ct), ae = ff_fma(three, ct, ff_neg(a));        // A = 3 ct (for -ct: -a, -ae)
+    const T p = ff_mul(ct, ct), pe = ff_fma(ct, ct, ff_neg(p));             // ct^2
+    const T b = ff_mul(four5, p), be = ff_fma(four5, p, ff_neg(b));         // B = 4.5 ct^2 = b + be + 4.5 pe
+    const T bb = ff_sub(ff_add(be, ff_mul(four5, pe)), c1e);                // low parts of B - C
+    const T m = ff_mul(mk, ff_add(ff_add(c1p, ff_abs(a)), b));
     // A + B by the fast two-sum, exact for |A| >= B (|ct| up to about 2/3); otherwise FP64
-    const bool ab = fabsf(a) >= b;
-    float s1, e1, s2, e2;
+    const auto ab = ab_ok(a, b);
+    T s1, e1, s2, e2;
     fast_two_sum(a, b, s1, e1);
-    two_sum(s1, -c1, s2, e2);
-    rp = ff_finish(ph, pl, m, s2, __fadd_rn(__fadd_rn(__fadd_rn(ae, bb), e1), e2), okp);
-    fast_two_sum(-a, b, s1, e1);
-    two_sum(s1, -c1, s2, e2);
-    rn = ff_finish(ph, pl, m, s2, __fadd_rn(__fadd_rn(__fadd_rn(-ae, bb), e1), e2), okn);
-    okp = okp && ab;
-    okn = okn && ab;
+    two_sum(s1, ff_neg(c1), s2, e2);
+    rp = ff_finish(ph, pl, m, s2, ff_add(ff_add(ff_add(ae, bb), e1), e2), okp);
+    fast_two_sum(ff_neg(a), b, s1, e1);
+    two_sum(s1, ff_neg(c1), s2, e2);
+    rn = ff_finish(ph, pl, m, s2, ff_add(ff_add(ff_add(ff_neg(ae), bb), e1), e2), okn);
+    okp = ok_and(okp, ab);
+    okn = ok_and(okn, ab);
 }
 
 __device__ __forceinline__ float eq_ff(float ph, float pl, float c1, float c1e, float ct, bool &ok) {
@@ -270,11 +333,7 @@ __device__ __forceinline__ float eq_ff(float ph, float pl, float c1, float c1e, 
     const float r = __fadd_rn(eh, el);
     const float d = __fadd_rn(__fsub_rn(eh, r), el);                      // (eh + el) - r
     const float m = __fmul_rn(__fmul_rn(fabsf(ph), __fadd_rn(__fadd_rn(__fadd_rn(1.0f, fabsf(a)), b), c1)), 0x1p-42f);
-    const uint32_t rb = __float_as_uint(r) & 0x7fffffffu;
-    const uint32_t ex = rb & 0x7f800000u;
-    // half the smaller gap next to r (2^e * 2^-24, or 2^-25 at a power of two)
-    const float half_gap = __fmul_rn(__uint_as_float(ex), (rb & 0x7fffffu) ? 0x1p-24f : 0x1p-25f);
-    ok = ex >= (67u << 23) && ex < 0x7f800000u && __fadd_rn(fabsf(d), m) < half_gap;
+    ok = ff_accept(r, __fadd_rn(fabsf(d), m));
     return r;
 }
 
@@ -297,6 +356,19 @@ __device__ __forceinline__ float div_fast(float x, const Tau &t, bool &ok) {
     if (ax == 0.0f) return t.b > 0.0f ? x : -x;  // +-0 / tau
     const float q = __fmul_rn(x, t.y);
     return __fmaf_rn(__fmaf_rn(-q, t.b, x), t.y, q);
+}
+
+// the same for two values at once (paired instructions; per lane as div_fast)
+__device__ __forceinline__ float2 div_fast2(float2 x, const Tau &t, Ok2 &ok) {
+    const float2 y = make_float2(t.y, t.y), b = make_float2(t.b, t.b);
+    const float2 q = __fmul2_rn(x, y);
+    float2 r = __ffma2_rn(__ffma2_rn(ff_neg(q), b, x), y, q);
+    const float ax = fabsf(x.x), ay = fabsf(x.y);
+    ok.x = t.fast && ax <= 0x1p96f && (ax >= 0x1p-96f || ax == 0.0f);
+    ok.y = t.fast && ay <= 0x1p96f && (ay >= 0x1p-96f || ay == 0.0f);
+    if (ax == 0.0f) r.x = t.b > 0.0f ? x.x : -x.x;  // +-0 / tau
+    if (ay == 0.0f) r.y = t.b > 0.0f ? x.y : -x.y;
+    return r;
 }
 
 __device__ __forceinline__ float div_tau(float x, const Tau &t) {
@@ -369,19 +441,38 @@ __device__ __forceinline__ bool collide(float v[27], const Tau &tau) {
         all_ok = ok || still;
         relax(v[0], still ? zero : eq);
     }
-    Unroll<27>::run([&](auto ii) {
-        constexpr int i = decltype(ii)::value;
-        constexpr int j = opp27(i);
-        if constexpr (i > 0 && i < j) {
-            constexpr int k = wclass(i);
-            float rp, rn;
-            bool okp, okn;
-            eq_ff_pair(ph[k], pl[k], mk[k], c1, c1e, c1p, cdot<i>(ux, uy, uz), rp, okp, rn, okn);
-            all_ok = all_ok && ((okp && okn) || still);
-            relax(v[i], still ? zero : rp);
-            relax(v[j], still ? zero : rn);
-        }
+    // the 13 pairs of opposite directions, two pairs per paired instruction, the last one alone
+    auto relax2 = [&](float &f0, float &f1, float2 eq) {
+        Ok2 ok;
+        const float2 q = div_fast2(__fadd2_rn(eq, make_float2(-f0, -f1)), tau, ok);
+        f0 = __fadd_rn(f0, q.x);
+        f1 = __fadd_rn(f1, q.y);
+        all_ok = all_ok && ok.x && ok.y;
+    };
+    const float2 c1_2 = make_float2(c1, c1), c1e_2 = make_float2(c1e, c1e), c1p_2 = make_float2(c1p, c1p);
+    Unroll<6>::run([&](auto nn) {
+        constexpr int n = decltype(nn)::value;
+        constexpr int i0 = pair_rep(2 * n), i1 = pair_rep(2 * n + 1);
+        constexpr int j0 = opp27(i0), j1 = opp27(i1);
+        constexpr int k0 = wclass(i0), k1 = wclass(i1);
+        float2 rp, rn;
+        Ok2 okp, okn;
+        eq_ff_pair(make_float2(ph[k0], ph[k1]), make_float2(pl[k0], pl[k1]), make_float2(mk[k0], mk[k1]), c1_2, c1e_2,
+                   c1p_2, make_float2(cdot<i0>(ux, uy, uz), cdot<i1>(ux, uy, uz)), rp, okp, rn, okn);
+        all_ok = all_ok && ((okp.x && okn.x && okp.y && okn.y) || still);
+        relax2(v[i0], v[i1], still ? make_float2(zero, zero) : rp);
+        relax2(v[j0], v[j1], still ? make_float2(zero, zero) : rn);
     });
+    {
+        constexpr int i = pair_rep(12), j = opp27(i), k = wclass(i);
+        float rp, rn;
+        bool okp, okn;
+        eq_ff_pair(ph[k], pl[k], mk[k], c1, c1e, c1p, cdot<i>(ux, uy, uz), rp, okp, rn, okn);
+        all_ok = all_ok && ((okp && okn) || still);
+        relax(v[i], still ? zero : rp);
+        relax(v[j], still ? zero : rn);
+    }
+    static_assert(pair_rep(12) > 0 && pair_rep(13) < 0, "13 pairs of opposite directions");
     return all_ok;
 }
 
@@ -419,8 +510,12 @@ __device__ __noinline__ void fused_cell_fp64(StepArgs a, int64_t c, int x, int y
     fused_cell<true>(a, c, x, y, z, fl);
 }
 
+// 128-thread blocks, registers bounded for 5 per SM (20 warps): the paired float-float evaluation
+// needs ~100 registers without spilling
+constexpr int FUSED_THREADS = 128;
+
 template <bool EQ64>
-__global__ void __launch_bounds__(256, 3) fused_kernel(StepArgs a) {
+__global__ void __launch_bounds__(FUSED_THREADS, 5) fused_kernel(StepArgs a) {
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= a.d.n) return;
     const uint8_t fl = a.flags[c];
@@ -745,6 +840,25 @@ __global__ void eq_selftest_kernel(int64_t n, uint64_t seed, unsigned long long 
             bad += okp && __float_as_uint(rp) != __float_as_uint(eq_fp64(k, rho, ct, usq));
             bad += okn && __float_as_uint(rn) != __float_as_uint(eq_fp64(k, rho, -ct, usq));
             fell += !okp && (s & 3) >= 2;  // fallbacks counted for |u| <= 0.05 (low-Mach flows)
+            // the paired form, lane x this direction and lane y the next one: the same bits and
+            // flags as the scalar evaluation of each
+            const int i2 = i % 26 + 1, k2 = wclass(i2);
+            const float ph2 = __fmul_rn(kWhi(k2), rho);
+            const float pl2 = __fmaf_rn(kWlo(k2), rho, __fmaf_rn(kWhi(k2), rho, -ph2));
+            const float ct2 = __fadd_rn(__fadd_rn((float)c_dir[i2][0] * ux, (float)c_dir[i2][1] * uy), (float)c_dir[i2][2] * uz);
+            float rp2, rn2;
+            bool okp2, okn2;
+            eq_ff_pair(ph2, pl2, __fmul_rn(fabsf(ph2), 0x1p-42f), c1, c1e, __fadd_rn(1.0f, c1), ct2, rp2, okp2, rn2, okn2);
+            float2 vp, vn;
+            Ok2 op, on;
+            eq_ff_pair(make_float2(ph, ph2), make_float2(pl, pl2),
+                       make_float2(__fmul_rn(fabsf(ph), 0x1p-42f), __fmul_rn(fabsf(ph2), 0x1p-42f)), make_float2(c1, c1),
+                       make_float2(c1e, c1e), make_float2(__fadd_rn(1.0f, c1), __fadd_rn(1.0f, c1)), make_float2(ct, ct2),
+                       vp, op, vn, on);
+            bad += __float_as_uint(vp.x) != __float_as_uint(rp) || __float_as_uint(vn.x) != __float_as_uint(rn) ||
+                   op.x != okp || on.x != okn;
+            bad += __float_as_uint(vp.y) != __float_as_uint(rp2) || __float_as_uint(vn.y) != __float_as_uint(rn2) ||
+                   op.y != okp2 || on.y != okn2;
         }
         for (int i = 0; i < 27; ++i) {
             const int k = wclass(i);
@@ -774,7 +888,7 @@ cudaError_t d3q27_eq_selftest(int64_t n, uint64_t seed, unsigned long long *out_
 }
 
 cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps, double *series_d) {
-    const int threads = 256;
+    const int threads = FUSED_THREADS;
     const Tau tau = tau_of(ctx);
     const Dims dm = dims(ctx);
     for (int s = 0; s < nsteps; ++s) {
