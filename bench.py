@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--tgv-steps", type=int, default=5000)
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=2000)
+    ap.add_argument("--batch-shape", default="", help="v,tx,ty: fixed batch tile shape instead of the tuner "
+                                                       "(reproducible profiling)")
     ap.add_argument("--serve-rates", default="2,6,10,15,25", help="requests per second, comma separated")
     ap.add_argument("--serve-duration", type=float, default=6.0, help="seconds of arrivals per rate")
     ap.add_argument("--round-steps", type=int, default=200)
@@ -402,7 +404,11 @@ def run_batch(args):
         with lbm.Batch(dtype, stream=stream.cuda_stream) as B:
             slots = {i: B.add(doms[i].nx, doms[i].ny, doms[i].tau, doms[i].flags, doms[i].periodic,
                               doms[i].body_force, doms[i].wall_velocity) for i in idx}
-            info = B.autotune()
+            if args.batch_shape and dtype != "f64":
+                B.set_launch(*[int(v) for v in args.batch_shape.split(",")])
+                info = B.info()
+            else:
+                info = B.autotune()
             if dtype != "f64":
                 B.step(args.warmup * 10)
                 B.synchronize()
