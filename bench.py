@@ -513,10 +513,19 @@ def run_serve(args):
                                       "peak_gb": st["peak_bytes"] / 1e9, "rounds": st["rounds"],
                                       "round_device_s": round(st["round_seconds"], 3),
                                       "tile_shape": st["tile_shape"], "tunings": st["tunings"]}
+        # the plain path as a user meets it: every new domain size runs the launch-shape tuner once
+        # (its timing inside the makespan); then again with the tuner's choices cached, which leaves
+        # only the solves themselves -- the stricter baseline
         lat, work, makespan = _serial_plain(reqs)
         row["plain_f32"] = {"p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99),
                             "aggregate_mlups": work / makespan / 1e6, "makespan_s": makespan}
         row["speedup_f16s_vs_plain"] = row["served_f16s"]["aggregate_mlups"] / row["plain_f32"]["aggregate_mlups"]
+        if rate == max(rates):
+            lat, work, makespan = _serial_plain(reqs)
+            row["plain_f32_shapes_cached"] = {"p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99),
+                                              "aggregate_mlups": work / makespan / 1e6, "makespan_s": makespan}
+            row["speedup_f16s_vs_plain_shapes_cached"] = (row["served_f16s"]["aggregate_mlups"] /
+                                                           row["plain_f32_shapes_cached"]["aggregate_mlups"])
         sweep.append(row)
     best = max(sweep, key=lambda r: r["served_f16s"]["aggregate_mlups"])
     line = {"metric": "served aggregate MLUPS and p50/p99 latency vs serial plain solves", "workload": "serve",

@@ -152,7 +152,7 @@ int resident_blocks(const void *kernel, int threads, size_t smem, int device) {
 // bounded for MINB blocks per SM (the dynamic shared memory is opted in once per kernel and
 // device); one persistent block per resident slot, at most one per task
 template <class S, int V, bool FORCE, int K, int MINB>
-cudaError_t launch_bulk(const lbm_ctx *ctx, const S *src, S *dst, int reverse) {
+cudaError_t launch_bulk(lbm_ctx *ctx, const S *src, S *dst, int reverse) {
     namespace B = d2q9::bulk;
     constexpr size_t bytes = B::smem_bytes<K>();
     constexpr int threads = B::threads<V>();
@@ -173,7 +173,7 @@ cudaError_t launch_bulk(const lbm_ctx *ctx, const S *src, S *dst, int reverse) {
     const int resident = resident_blocks(reinterpret_cast<const void *>(kern), threads, bytes, ctx->device);
     if (resident <= 0) return cudaErrorInvalidConfiguration;
     const int grid = std::min(ntasks, resident);
-    const_cast<lbm_ctx *>(ctx)->pipe_used = true;
+    ctx->pipe_used = true;
     kern<<<grid, threads, bytes, ctx->stream>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic,
                                                 d2q9_params(d), reverse, ctx->pipe_status_d);
     return cudaGetLastError();
@@ -183,7 +183,7 @@ cudaError_t launch_bulk(const lbm_ctx *ctx, const S *src, S *dst, int reverse) {
 // against 96-104k MLUPS): pol selects the ring depth and the register bound (0: 4 slots, 5 blocks
 // per SM; 1: 4 slots, 4 blocks; 2: 6 slots, 3 blocks)
 template <class S, bool FORCE>
-cudaError_t launch_bulk_variant(const lbm_ctx *ctx, int pol, const S *src, S *dst, int reverse) {
+cudaError_t launch_bulk_variant(lbm_ctx *ctx, int pol, const S *src, S *dst, int reverse) {
     if (pol == 0) return launch_bulk<S, 4, FORCE, 4, 5>(ctx, src, dst, reverse);
     if (pol == 1) return launch_bulk<S, 4, FORCE, 4, 4>(ctx, src, dst, reverse);
     return launch_bulk<S, 4, FORCE, 6, 3>(ctx, src, dst, reverse);
