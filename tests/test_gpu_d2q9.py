@@ -59,6 +59,8 @@ CASES = {
     "open_edges": (29, 17, lambda nx, ny: np.zeros((ny, nx), np.uint8), 0, (0, 0), (0, 0), 0.8, 40),
     "periodic_y_moving": (24, 30, None, 2, (0, 0), (0.03, 0.01), 0.65, 50),
     "thin_1xN": (1, 40, lambda nx, ny: np.zeros((ny, nx), np.uint8), 3, (0, 1e-5), (0, 0), 0.75, 30),
+    "thin_Nx1": (45, 1, lambda nx, ny: np.zeros((ny, nx), np.uint8), 3, (1e-5, 0), (0, 0), 0.7, 30),
+    "single_cell": (1, 1, lambda nx, ny: np.zeros((ny, nx), np.uint8), 3, (2e-5, -1e-5), (0, 0), 0.8, 20),
 }
 
 
@@ -318,3 +320,39 @@ def test_bad_launch_shape_rejected():
             L.set_launch(0, 160, 1, 3)  # three pipeline variants
         with pytest.raises(lbm.LBMError):
             L.set_launch(0, 160, 2, 0)  # one row per task
+
+
+@pytest.mark.parametrize("dtype", ["f16s", "f32"])
+def test_domain_past_32bit_indexing_reproduces_its_tile(dtype):
+    """A 16384 x 14592 domain (9 planes x 239 M cells: offsets past 2^31, so the step runs with
+    64-bit indexing) periodic in both directions, with flags that repeat a 64 x 64 tile, started at
+    equilibrium: every 64 x 64 tile of its density and velocity equals, bit for bit, the 64 x 64
+    domain run alone (size-independent check of the large-index path), and its conserved sums are
+    58,368 times the tile's."""
+    tile = 64
+    t_flags = np.zeros((tile, tile), np.uint8)
+    yy, xx = np.mgrid[0:tile, 0:tile]
+    t_flags[(xx - 30.5) ** 2 + (yy - 33.5) ** 2 < 10.0 ** 2] = 1
+    t_flags[5, 50:54] = lbm.MOVING_WALL
+    kw = dict(dtype=dtype, tau=0.6, periodic=3, body_force=(1e-5, 2e-6, 0), wall_velocity=(0.02, 0, 0))
+    steps = 7
+    with lbm.Lattice(tile, tile, **kw) as L:
+        L.set_flags(t_flags)
+        L.init_equilibrium()
+        L.step(steps)
+        want = L.moments()
+        want_cons = L.conservation()
+    nx, ny = 16384, 14592
+    assert 9 * nx * ny > 2 ** 31
+    with lbm.Lattice(nx, ny, **kw) as L:
+        L.set_flags(np.tile(t_flags, (ny // tile, nx // tile)))
+        L.init_equilibrium()
+        L.step(steps)
+        cons = L.conservation()
+        got = L.moments()
+    ntiles = (nx // tile) * (ny // tile)
+    for g, w in zip(got, want):
+        g4 = g.reshape(ny // tile, tile, nx // tile, tile)
+        assert np.array_equal(g4, np.broadcast_to(w[None, :, None, :], g4.shape))
+    for c, w in zip(cons[:3], want_cons[:3]):
+        assert abs(c - ntiles * w) <= 1e-9 * max(1.0, abs(ntiles * w))
