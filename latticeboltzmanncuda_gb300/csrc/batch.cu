@@ -125,6 +125,80 @@ __global__ void __launch_bounds__(256, 4) batch_step_kernel_occ(const SlotDesc *
     batch_tile<S, V>(slots, tiles, ntiles, step, reverse);
 }
 
+// Batches of up to PARAM_SLOTS live slots (FP32 and 16-bit storage) pass their descriptors and the
+// first tile of every slot in the kernel's parameter block (constant memory, served to all blocks
+// of an SM by the constant cache): a block finds its slot by a binary search over the tile offsets
+// and derives its row band and column chunk, with no dependent global load before its own
+// population loads.  Larger batches (and FP64) read the descriptor and tile tables from global
+// memory as above.
+constexpr int PARAM_SLOTS = 400;
+
+struct SlotDescP {  // 72 bytes
+    void *f[2];
+    const uint16_t *links;
+    int nx, ny, pitch, plane;
+    int bits;    // periodic (bits 0-1), force (bit 2), current buffer at the sequence start (bit 3)
+    int stop;    // steps this slot takes in the launch sequence
+    int chunks;  // column chunks per row band
+    float omega, fx, fy, uwx, uwy;
+};
+
+struct BatchParams {
+    int n;       // slots in the block
+    int ntiles;  // tiles of the launch
+    int start[PARAM_SLOTS];
+    SlotDescP d[PARAM_SLOTS];
+};
+static_assert(sizeof(BatchParams) <= 32764, "kernel parameter block limit");
+
+template <class S, int V>
+__device__ __forceinline__ void batch_tile_p(const BatchParams &p, int step, int reverse) {
+    const int t = reverse ? p.ntiles - 1 - (int)blockIdx.x : (int)blockIdx.x;
+    int lo = 0, hi = p.n - 1;
+    while (lo < hi) {  // the last slot whose first tile is at or before t (uniform per block)
+        const int mid = (lo + hi + 1) >> 1;
+        if (p.start[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    const SlotDescP &D = p.d[lo];
+    if (step >= D.stop) return;  // the slot has used its step budget
+    const int i = t - p.start[lo];
+    const int band = i / D.chunks, xchunk = i - band * D.chunks;
+    const int y = band * (int)blockDim.y + (int)threadIdx.y;
+    if (y >= D.ny) return;  // uniform per warp
+    const int x0 = (xchunk * (int)blockDim.x + (int)threadIdx.x) * V;
+    const int cur = ((D.bits >> 3) + step) & 1;
+    const S *src = static_cast<const S *>(D.f[cur]);
+    S *dst = static_cast<S *>(D.f[cur ^ 1]);
+    D2Q9Params prm;
+    prm.omega = D.omega;
+    prm.fx = D.fx;
+    prm.fy = D.fy;
+    prm.uwx = D.uwx;
+    prm.uwy = D.uwy;
+    prm.omega_d = prm.fx_d = prm.fy_d = prm.uwx_d = prm.uwy_d = 0.0;  // FP64 storage uses the table path
+    const int periodic = D.bits & 3;
+    if (D.bits & 4)
+        d2q9::step_vec<S, V, true, int>(src, dst, D.links, x0, y, D.nx, D.ny, D.pitch, D.plane, periodic, prm);
+    else
+        d2q9::step_vec<S, V, false, int>(src, dst, D.links, x0, y, D.nx, D.ny, D.pitch, D.plane, periodic, prm);
+}
+
+// registers held to what the table kernel uses (2-wide 64, 4-wide 85, 8-wide 128): the descriptor
+// fields read from the parameter block otherwise stay in registers and cost occupancy
+__host__ __device__ constexpr int batch_min_blocks(int v) { return v == 8 ? 2 : (v == 4 ? 3 : 4); }
+
+template <class S, int V>
+__global__ void __launch_bounds__(256, batch_min_blocks(V)) batch_step_kernel_p(const __grid_constant__ BatchParams p,
+                                                                               int step, int reverse) {
+    batch_tile_p<S, V>(p, step, reverse);
+}
+
+template <class S, int V>
+__global__ void __launch_bounds__(256, 4) batch_step_kernel_p_occ(const __grid_constant__ BatchParams p, int step,
+                                                                  int reverse) {
+    batch_tile_p<S, V>(p, step, reverse);
+}
+
 size_t dsize(int dtype) { return dtype == LBM_F64 ? 8 : (dtype == LBM_F32 ? 4 : 2); }
 
 template <class S>
@@ -165,6 +239,8 @@ struct lbm_batch {
     double *result_d = nullptr;
     std::vector<PinnedBlock> pinned;
     std::map<int64_t, Pending> pending;  // read-backs by ticket
+    bool use_params = false;             // the launch takes the descriptors in its parameter block
+    BatchParams params{};
     int64_t next_ticket = 1;
 };
 
@@ -315,11 +391,52 @@ int64_t advance_of(const Slot &s, int64_t nsteps) { return s.limit < 0 ? nsteps 
 // Tiles of a slot whose budget is used up stay in the list: their blocks return at once.
 lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
     bool limited = false;
-    for (const Slot &s : b->slots) limited |= s.live && s.limit >= 0;
+    int live = 0;
+    for (const Slot &s : b->slots) {
+        limited |= s.live && s.limit >= 0;
+        live += s.live ? 1 : 0;
+    }
     if (!b->dirty && !b->tiles_dirty && !limited) return LBM_OK;
+    if (b->dtype != LBM_F64 && live <= PARAM_SLOTS) {  // descriptors and tile offsets as kernel parameters
+        BatchParams &p = b->params;
+        p.n = 0;
+        int ntiles = 0;
+        for (const Slot &s : b->slots) {
+            if (!s.live) continue;
+            SlotDescP &d = p.d[p.n];
+            const int64_t adv = advance_of(s, nsteps);
+            d.stop = s.limit < 0 ? INT32_MAX : (int)std::min<int64_t>(adv, INT32_MAX);
+            d.f[0] = s.f[0];
+            d.f[1] = s.f[1];
+            d.links = s.links;
+            d.nx = s.desc.nx;
+            d.ny = s.desc.ny;
+            d.pitch = s.pitch;
+            d.plane = (int)s.plane;
+            const bool force = s.desc.body_force[0] != 0.0f || s.desc.body_force[1] != 0.0f;
+            d.bits = (s.desc.periodic & 3) | (force ? 4 : 0) | (s.cur ? 8 : 0);
+            d.chunks = (s.pitch / b->v + b->tx - 1) / b->tx;
+            const D2Q9Params prm = d2q9_params(s.desc);
+            d.omega = prm.omega;
+            d.fx = prm.fx;
+            d.fy = prm.fy;
+            d.uwx = prm.uwx;
+            d.uwy = prm.uwy;
+            p.start[p.n] = ntiles;
+            ntiles += d.chunks * ((s.desc.ny + b->ty - 1) / b->ty);
+            ++p.n;
+        }
+        p.ntiles = ntiles;
+        b->ntiles = ntiles;
+        b->use_params = true;
+        b->dirty = false;
+        b->tiles_dirty = false;
+        return LBM_OK;
+    }
     std::vector<SlotDesc> descs(b->slots.size());
     std::vector<Tile> tiles;
-    const bool retile = b->tiles_dirty;
+    const bool retile = b->tiles_dirty || b->use_params;  // the tile table is stale after parameter launches
+    b->use_params = false;
     for (size_t i = 0; i < b->slots.size(); ++i) {
         const Slot &s = b->slots[i];
         SlotDesc &d = descs[i];
@@ -365,6 +482,13 @@ template <class S, int V>
 cudaError_t launch_v(lbm_batch *b, int step, int reverse) {
     dim3 block(b->tx, b->ty);
     dim3 grid((unsigned)b->ntiles);
+    if (b->use_params) {
+        if constexpr (sizeof(S) == 2 && V == 4)
+            batch_step_kernel_p_occ<S, V><<<grid, block, 0, b->stream>>>(b->params, step, reverse);
+        else if constexpr (sizeof(S) <= 4)
+            batch_step_kernel_p<S, V><<<grid, block, 0, b->stream>>>(b->params, step, reverse);
+        return cudaGetLastError();
+    }
     if constexpr (sizeof(S) == 2 && V == 4)
         batch_step_kernel_occ<S, V><<<grid, block, 0, b->stream>>>(b->desc_d, b->tiles_d, b->ntiles, step, reverse);
     else
