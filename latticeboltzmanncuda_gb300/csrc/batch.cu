@@ -131,12 +131,11 @@ __global__ void __launch_bounds__(256, 4) batch_step_kernel_occ(const SlotDesc *
 // and derives its row band and column chunk, with no dependent global load before its own
 // population loads.  Larger batches (and FP64) read the descriptor and tile tables from global
 // memory as above.
-constexpr int PARAM_SLOTS = 400;
+constexpr int PARAM_SLOTS = 540;
 
-struct SlotDescP {  // 72 bytes
-    void *f[2];
-    const uint16_t *links;
-    int nx, ny, pitch, plane;
+struct SlotDescP {  // 56 bytes; pitch, plane, buffers and link words follow from these
+    void *base;  // the slot's allocation: buffer A, buffer B (9 planes each), link words
+    int nx, ny;
     int bits;    // periodic (bits 0-1), force (bit 2), current buffer at the sequence start (bit 3)
     int stop;    // steps this slot takes in the launch sequence
     int chunks;  // column chunks per row band
@@ -161,14 +160,17 @@ __device__ __forceinline__ void batch_tile_p(const BatchParams &p, int step, int
     }
     const SlotDescP &D = p.d[lo];
     if (step >= D.stop) return;  // the slot has used its step budget
+    const int pitch = (D.nx + 31) & ~31, plane = pitch * D.ny;
     const int i = t - p.start[lo];
     const int band = i / D.chunks, xchunk = i - band * D.chunks;
     const int y = band * (int)blockDim.y + (int)threadIdx.y;
     if (y >= D.ny) return;  // uniform per warp
     const int x0 = (xchunk * (int)blockDim.x + (int)threadIdx.x) * V;
     const int cur = ((D.bits >> 3) + step) & 1;
-    const S *src = static_cast<const S *>(D.f[cur]);
-    S *dst = static_cast<S *>(D.f[cur ^ 1]);
+    S *const a = static_cast<S *>(D.base);
+    const S *src = a + (size_t)cur * 9 * plane;
+    S *dst = a + (size_t)(cur ^ 1) * 9 * plane;
+    const uint16_t *links = reinterpret_cast<const uint16_t *>(a + (size_t)18 * plane);
     D2Q9Params prm;
     prm.omega = D.omega;
     prm.fx = D.fx;
@@ -178,9 +180,9 @@ __device__ __forceinline__ void batch_tile_p(const BatchParams &p, int step, int
     prm.omega_d = prm.fx_d = prm.fy_d = prm.uwx_d = prm.uwy_d = 0.0;  // FP64 storage uses the table path
     const int periodic = D.bits & 3;
     if (D.bits & 4)
-        d2q9::step_vec<S, V, true, int>(src, dst, D.links, x0, y, D.nx, D.ny, D.pitch, D.plane, periodic, prm);
+        d2q9::step_vec<S, V, true, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm);
     else
-        d2q9::step_vec<S, V, false, int>(src, dst, D.links, x0, y, D.nx, D.ny, D.pitch, D.plane, periodic, prm);
+        d2q9::step_vec<S, V, false, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm);
 }
 
 // registers held to what the table kernel uses (2-wide 64, 4-wide 85, 8-wide 128): the descriptor
@@ -318,8 +320,7 @@ struct CtxView {
 // slot does not synchronise the device (its memory returns to the pool once the work queued before
 // the free has run), and a later slot reuses the pooled memory without a new device allocation.
 void free_slot(lbm_batch *b, Slot &s) {
-    for (void *p : {(void *)s.f[0], (void *)s.f[1], (void *)s.links, (void *)s.flags})
-        if (p) cudaFreeAsync(p, b->stream);
+    if (s.f[0]) cudaFreeAsync(s.f[0], b->stream);  // the slot's one allocation (see slot_layout)
     s.f[0] = s.f[1] = nullptr;
     s.links = nullptr;
     s.flags = nullptr;
@@ -406,16 +407,13 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
             SlotDescP &d = p.d[p.n];
             const int64_t adv = advance_of(s, nsteps);
             d.stop = s.limit < 0 ? INT32_MAX : (int)std::min<int64_t>(adv, INT32_MAX);
-            d.f[0] = s.f[0];
-            d.f[1] = s.f[1];
-            d.links = s.links;
+            d.base = s.f[0];
             d.nx = s.desc.nx;
             d.ny = s.desc.ny;
-            d.pitch = s.pitch;
-            d.plane = (int)s.plane;
             const bool force = s.desc.body_force[0] != 0.0f || s.desc.body_force[1] != 0.0f;
             d.bits = (s.desc.periodic & 3) | (force ? 4 : 0) | (s.cur ? 8 : 0);
-            d.chunks = (s.pitch / b->v + b->tx - 1) / b->tx;
+            const int chunks = (s.pitch / b->v + b->tx - 1) / b->tx;
+            d.chunks = chunks;
             const D2Q9Params prm = d2q9_params(s.desc);
             d.omega = prm.omega;
             d.fx = prm.fx;
@@ -423,7 +421,7 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
             d.uwx = prm.uwx;
             d.uwy = prm.uwy;
             p.start[p.n] = ntiles;
-            ntiles += d.chunks * ((s.desc.ny + b->ty - 1) / b->ty);
+            ntiles += chunks * ((s.desc.ny + b->ty - 1) / b->ty);
             ++p.n;
         }
         p.ntiles = ntiles;
@@ -703,10 +701,16 @@ LBM_API lbm_status lbm_batch_add(lbm_batch *b, const lbm_desc *desc, const uint8
         cudaStreamSynchronize(b->stream);
     };
     const size_t ncell = (size_t)desc->nx * desc->ny;
-    cudaError_t e = cudaMallocAsync(&s.f[0], pop, b->stream);
-    if (e == cudaSuccess) e = cudaMallocAsync(&s.f[1], pop, b->stream);
-    if (e == cudaSuccess) e = cudaMallocAsync(&s.links, (size_t)s.plane * sizeof(uint16_t), b->stream);
-    if (e == cudaSuccess) e = cudaMallocAsync(&s.flags, flags_bytes(desc->nx, desc->ny), b->stream);
+    // one allocation per slot: population buffers A and B, link words, flags and the fluid count
+    // (the parameter-block kernel derives every pointer from the first)
+    cudaError_t e = cudaMallocAsync(&s.f[0], 2 * pop + (size_t)s.plane * sizeof(uint16_t) + flags_bytes(desc->nx, desc->ny),
+                                    b->stream);
+    if (e == cudaSuccess) {
+        char *base = static_cast<char *>(s.f[0]);
+        s.f[1] = base + pop;
+        s.links = reinterpret_cast<uint16_t *>(base + 2 * pop);
+        s.flags = reinterpret_cast<uint8_t *>(base + 2 * pop + (size_t)s.plane * sizeof(uint16_t));
+    }
     if (e != cudaSuccess) {
         cudaGetLastError();
         cleanup();
