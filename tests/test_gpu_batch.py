@@ -198,3 +198,38 @@ def test_batch_rejects_bad_input():
             B.remove(3)
         with pytest.raises(lbm.LBMError):
             B.set_launch(8, 32, 1)  # FP32 vectors are 2 or 4 wide
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f16s"])
+def test_many_slots_table_path_and_back(dtype):
+    """Past 540 live slots the batch reads its descriptors and tiles from global-memory tables, below
+    that from the kernel's parameter block: 600 small slots of varied shape and kind (table path),
+    then 120 of them removed mid-run (parameter path), every slot equal to its solo run bit for bit."""
+    rng = np.random.default_rng(11)
+    kinds = []
+    for i in range(600):
+        nx, ny = int(rng.integers(3, 70)), int(rng.integers(2, 12))
+        per = int(rng.integers(0, 4))
+        fl = np.zeros((ny, nx), np.uint8)
+        if not per & 2:
+            fl[0, :] = 1
+            fl[-1, :] = 2 if i % 3 == 0 else 1
+        kinds.append((nx, ny, float(rng.uniform(0.55, 1.1)), fl, per, (float(rng.uniform(0, 2e-5)), 0.0),
+                      (0.03 if i % 3 == 0 else 0.0, 0.0)))
+    first, second = 7, 5
+    with lbm.Batch(dtype) as B:
+        slots = [B.add(*k[:4], k[4], k[5], k[6]) for k in kinds]
+        for i, sl in enumerate(slots):
+            B.load_populations(sl, init_state(kinds[i][0], kinds[i][1], 1000 + i))
+        B.step(first)
+        removed = set(range(0, 600, 5))
+        early = {i: B.retrieve_populations(slots[i], np.float64) for i in removed}
+        for i in removed:
+            B.remove(slots[i])
+        B.step(second)
+        late = {i: B.retrieve_populations(slots[i], np.float64) for i in range(600) if i not in removed}
+    for i, got in early.items():
+        assert np.array_equal(got, single(kinds[i], init_state(kinds[i][0], kinds[i][1], 1000 + i), first, dtype)), i
+    for i, got in list(late.items())[::7]:
+        assert np.array_equal(got, single(kinds[i], init_state(kinds[i][0], kinds[i][1], 1000 + i), first + second,
+                                          dtype)), i
