@@ -67,7 +67,7 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=2000)
     ap.add_argument("--batch-shape", default="", help="v,tx,ty: fixed batch tile shape instead of the tuner "
                                                        "(reproducible profiling)")
-    ap.add_argument("--serve-rates", default="2,6,10,15,25", help="requests per second, comma separated")
+    ap.add_argument("--serve-rates", default="2,6,10,15,25,60", help="requests per second, comma separated")
     ap.add_argument("--serve-duration", type=float, default=6.0, help="seconds of arrivals per rate")
     ap.add_argument("--round-steps", type=int, default=200)
     return ap.parse_args()
