@@ -1,16 +1,18 @@
 // Batched D2Q9: many independent domains of uneven size, tau, forcing and obstacle mask advance
 // together, one kernel launch per time step for all of them.
 //
-// Each domain (a "slot") owns its two population buffers and link words, allocated when it is
-// added, so slots come and go without moving anyone else's state (the serving loop admits and
-// retires requests between rounds).  A device table holds one descriptor per slot (sizes,
-// pointers, relaxation rate, force, wall velocity, periodicity, buffer parity).  The launch grid
-// is a flat list of tiles (slot, x-chunk, first row): every block updates TY rows x (TX * V)
-// cells of one slot with the same vectorised update as the single-domain kernel, so a domain's
-// populations are bit-identical whether it runs alone or in any mix.  Tiles are ordered slot by
-// slot, rows ascending; odd steps walk the list backwards (each step starts where the previous
-// one ended, on data still in L2).  The tile shape (V, TX, TY) is picked by the autotuner from
-// timings on the batch itself.
+// Each domain (a "slot") owns one allocation -- its two population buffers, link words, flags and
+// fluid-cell count -- made when it is added, so slots come and go without moving anyone else's
+// state (the serving loop admits and retires requests between rounds).  Every block of a launch
+// updates one tile, TY rows x (TX * V) cells of one slot, with the same vectorised update as the
+// single-domain kernel, so a domain's populations are bit-identical whether it runs alone or in
+// any mix.  Tiles are ordered slot by slot, rows ascending; odd steps walk them backwards (each
+// step starts where the previous one ended, on data still in L2).  Up to PARAM_SLOTS live slots
+// (FP32, 16-bit storage) the slot descriptors (size, buffer base, parity, step budget, relaxation
+// rate, force, wall velocity, periodicity) and the first tile of every slot travel in the kernel's
+// parameter block and a block derives its tile from its index; beyond that, and for FP64, a device
+// table of descriptors and a flat tile list (slot, x-chunk, first row) do.  The tile shape
+// (V, TX, TY) is picked by the autotuner from timings on the batch itself.
 //
 // Nothing on the serving path waits for the device: adding a slot (flags upload, link words,
 // fluid-cell count, equilibrium), the table uploads before a launch sequence, freeing a slot and
@@ -86,9 +88,9 @@ struct Slot {
 // bytes of a slot's flag allocation: the flags, padded to 8 bytes, then the fluid-cell count
 size_t flags_bytes(int nx, int ny) { return ((size_t)nx * ny + 7) / 8 * 8 + 8; }
 
-// One block per tile.  The tile's slot descriptor is copied into registers, so no field is re-read
-// from global memory after the population stores.  (A persistent grid-stride loop over the tiles
-// measured slower: it keeps ~40 more registers live and halves the occupancy.)
+// Table path: one block per tile.  The tile's slot descriptor is copied into registers, so no field
+// is re-read from global memory after the population stores.  (A persistent grid-stride loop over
+// the tiles measured slower: it keeps ~40 more registers live and halves the occupancy.)
 template <class S, int V>
 __device__ __forceinline__ void batch_tile(const SlotDesc *__restrict__ slots, const Tile *__restrict__ tiles,
                                            int ntiles, int step, int reverse) {
