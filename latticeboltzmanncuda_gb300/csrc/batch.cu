@@ -150,21 +150,47 @@ struct BatchParams {
     int start[PARAM_SLOTS];
     SlotDescP d[PARAM_SLOTS];
 };
+
+// a tile of the parameter-block path for 16-bit storage: the block's slot (an index into the
+// parameter block), row band and column chunk, one 8-byte load.  (FP32 blocks find their slot by a
+// binary search over the slots' first tiles instead: measured on the serve domains, the 16-bit
+// kernel, bound by instruction issue, runs 3 % faster with the load, the FP32 kernel, bound by
+// memory latency, 5 % slower.)
+struct TileP {
+    int slot;
+    unsigned short band, xchunk;
+};
+
+template <class S>
+constexpr bool tile_records() {
+    return sizeof(S) == 2;
+}
 static_assert(sizeof(BatchParams) <= 32764, "kernel parameter block limit");
 
 template <class S, int V>
-__device__ __forceinline__ void batch_tile_p(const BatchParams &p, int step, int reverse) {
+__device__ __forceinline__ void batch_tile_p(const BatchParams &p, const TileP *__restrict__ tiles, int step,
+                                             int reverse) {
     const int t = reverse ? p.ntiles - 1 - (int)blockIdx.x : (int)blockIdx.x;
-    int lo = 0, hi = p.n - 1;
-    while (lo < hi) {  // the last slot whose first tile is at or before t (uniform per block)
-        const int mid = (lo + hi + 1) >> 1;
-        if (p.start[mid] <= t) lo = mid; else hi = mid - 1;
+    int slot, band, xchunk;
+    if constexpr (tile_records<S>()) {
+        const TileP tile = tiles[t];
+        slot = tile.slot;
+        band = tile.band;
+        xchunk = tile.xchunk;
+    } else {
+        int lo = 0, hi = p.n - 1;
+        while (lo < hi) {  // the last slot whose first tile is at or before t (uniform per block)
+            const int mid = (lo + hi + 1) >> 1;
+            if (p.start[mid] <= t) lo = mid; else hi = mid - 1;
+        }
+        slot = lo;
+        const int i = t - p.start[lo];
+        band = i / p.d[lo].chunks;
+        xchunk = i - band * p.d[lo].chunks;
     }
-    const SlotDescP &D = p.d[lo];
+    const SlotDescP &D = p.d[slot];
     if (step >= D.stop) return;  // the slot has used its step budget
     const int pitch = (D.nx + 31) & ~31, plane = pitch * D.ny;
-    const int i = t - p.start[lo];
-    const int band = i / D.chunks, xchunk = i - band * D.chunks;
     const int y = band * (int)blockDim.y + (int)threadIdx.y;
     if (y >= D.ny) return;  // uniform per warp
     const int x0 = (xchunk * (int)blockDim.x + (int)threadIdx.x) * V;
@@ -193,14 +219,16 @@ __host__ __device__ constexpr int batch_min_blocks(int v) { return v == 8 ? 2 : 
 
 template <class S, int V>
 __global__ void __launch_bounds__(256, batch_min_blocks(V)) batch_step_kernel_p(const __grid_constant__ BatchParams p,
+                                                                               const TileP *__restrict__ tiles,
                                                                                int step, int reverse) {
-    batch_tile_p<S, V>(p, step, reverse);
+    batch_tile_p<S, V>(p, tiles, step, reverse);
 }
 
 template <class S, int V>
-__global__ void __launch_bounds__(256, 4) batch_step_kernel_p_occ(const __grid_constant__ BatchParams p, int step,
+__global__ void __launch_bounds__(256, 4) batch_step_kernel_p_occ(const __grid_constant__ BatchParams p,
+                                                                  const TileP *__restrict__ tiles, int step,
                                                                   int reverse) {
-    batch_tile_p<S, V>(p, step, reverse);
+    batch_tile_p<S, V>(p, tiles, step, reverse);
 }
 
 size_t dsize(int dtype) { return dtype == LBM_F64 ? 8 : (dtype == LBM_F32 ? 4 : 2); }
@@ -245,6 +273,8 @@ struct lbm_batch {
     std::map<int64_t, Pending> pending;  // read-backs by ticket
     bool use_params = false;             // the launch takes the descriptors in its parameter block
     BatchParams params{};
+    TileP *ptiles_d = nullptr;           // tiles of the parameter-block path
+    size_t ptiles_cap = 0;
     int64_t next_ticket = 1;
 };
 
@@ -400,7 +430,13 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
         live += s.live ? 1 : 0;
     }
     if (!b->dirty && !b->tiles_dirty && !limited) return LBM_OK;
-    if (b->dtype != LBM_F64 && live <= PARAM_SLOTS) {  // descriptors and tile offsets as kernel parameters
+    // the parameter-block path: FP32 / 16-bit storage, at most PARAM_SLOTS slots, and row bands and
+    // column chunks that fit the 16-bit fields of its tiles
+    bool params_ok = b->dtype != LBM_F64 && live <= PARAM_SLOTS;
+    for (const Slot &s : b->slots)
+        if (params_ok && s.live)
+            params_ok = (s.desc.ny + b->ty - 1) / b->ty <= 65535 && (s.pitch / b->v + b->tx - 1) / b->tx <= 65535;
+    if (params_ok) {  // descriptors as kernel parameters
         BatchParams &p = b->params;
         p.n = 0;
         int ntiles = 0;
@@ -427,6 +463,20 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
             ++p.n;
         }
         p.ntiles = ntiles;
+        if (dsize(b->dtype) == 2 && (b->tiles_dirty || !b->use_params)) {  // 16-bit: tile records, rebuilt with the live set or the shape
+            std::vector<TileP> tl;
+            tl.reserve((size_t)ntiles);
+            for (int k = 0; k < p.n; ++k) {
+                const int bands = (p.d[k].ny + b->ty - 1) / b->ty;
+                for (int band = 0; band < bands; ++band)
+                    for (int xc = 0; xc < p.d[k].chunks; ++xc)
+                        tl.push_back(TileP{k, (unsigned short)band, (unsigned short)xc});
+            }
+            lbm_status st = grow_table(b, (void **)&b->ptiles_d, &b->ptiles_cap, tl.size(), sizeof(TileP), 1024,
+                                       "batch: tile table");
+            if (st == LBM_OK) st = upload_async(b, b->ptiles_d, tl.data(), tl.size() * sizeof(TileP), "batch: upload tiles");
+            if (st != LBM_OK) return st;
+        }
         b->ntiles = ntiles;
         b->use_params = true;
         b->dirty = false;
@@ -484,9 +534,9 @@ cudaError_t launch_v(lbm_batch *b, int step, int reverse) {
     dim3 grid((unsigned)b->ntiles);
     if (b->use_params) {
         if constexpr (sizeof(S) == 2 && V == 4)
-            batch_step_kernel_p_occ<S, V><<<grid, block, 0, b->stream>>>(b->params, step, reverse);
+            batch_step_kernel_p_occ<S, V><<<grid, block, 0, b->stream>>>(b->params, b->ptiles_d, step, reverse);
         else if constexpr (sizeof(S) <= 4)
-            batch_step_kernel_p<S, V><<<grid, block, 0, b->stream>>>(b->params, step, reverse);
+            batch_step_kernel_p<S, V><<<grid, block, 0, b->stream>>>(b->params, b->ptiles_d, step, reverse);
         return cudaGetLastError();
     }
     if constexpr (sizeof(S) == 2 && V == 4)
@@ -663,6 +713,7 @@ LBM_API lbm_status lbm_batch_destroy(lbm_batch *b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     cudaFree(b->desc_d);
     cudaFree(b->tiles_d);
+    cudaFree(b->ptiles_d);
     cudaFree(b->staging);
     cudaFree(b->result_d);
     for (PinnedBlock &pb : b->pinned) {
