@@ -282,6 +282,79 @@ def test_bulk_protocol_simulation_catches_a_missing_release():
         simulate_bulk_protocol(20, 4, False, 0, consumers=NC - 1)
 
 
+# ------------------------------------------------------------------ batch parameter-block path
+# csrc/batch.cu: slots are one allocation each (buffer A, buffer B: 9 planes of pitch x ny elements
+# each; then pitch x ny uint16 link words; then flags and the fluid count), tiles are ordered slot
+# by slot, row bands ascending, column chunks inside a band.  16-bit blocks read (slot, band,
+# chunk) from a tile record, FP32 blocks binary-search the slots' first tiles.
+
+
+def batch_tiles(shapes, V, tx, ty):
+    """The tile list of rebuild(): (slot, band, xchunk) per tile, and the slots' first tiles."""
+    tiles, start = [], []
+    for k, (nx, ny) in enumerate(shapes):
+        pitch = (nx + 31) // 32 * 32
+        chunks = (pitch // V + tx - 1) // tx
+        start.append(len(tiles))
+        for band in range((ny + ty - 1) // ty):
+            for xc in range(chunks):
+                tiles.append((k, band, xc))
+    return tiles, start
+
+
+def search_tile(start, t, chunks):
+    """batch_tile_p's binary search and division for tile t."""
+    lo, hi = 0, len(start) - 1
+    while lo < hi:
+        mid = (lo + hi + 1) >> 1
+        if start[mid] <= t:
+            lo = mid
+        else:
+            hi = mid - 1
+    i = t - start[lo]
+    return lo, i // chunks[lo], i - (i // chunks[lo]) * chunks[lo]
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_batch_parameter_path_tiles_and_addresses(seed):
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(1, 30))
+    shapes = [(int(rng.integers(1, 700)), int(rng.integers(1, 300))) for _ in range(n)]
+    for elem, V, tx, ty in ((2, 4, 32, 4), (2, 8, 32, 2), (2, 2, 64, 1), (4, 4, 32, 2), (4, 2, 128, 2)):
+        tiles, start = batch_tiles(shapes, V, tx, ty)
+        chunks = [((nx + 31) // 32 * 32 // V + tx - 1) // tx for nx, _ in shapes]
+        # the binary search (FP32) finds every tile's record (16-bit), and the fields fit 16 bits
+        for t, rec in enumerate(tiles):
+            assert search_tile(start, t, chunks) == rec
+            assert rec[1] <= 65535 and rec[2] <= 65535
+        # every cell of every slot is covered by exactly one (tile, thread row, lane, element)
+        for k, (nx, ny) in enumerate(shapes):
+            pitch = (nx + 31) // 32 * 32
+            plane = pitch * ny
+            pop = 9 * plane * elem
+            alloc = 2 * pop + plane * 2 + ((nx * ny + 7) // 8 * 8 + 8)
+            seen = np.zeros((ny, pitch), int)
+            for (kk, band, xc) in (r for r in tiles if r[0] == k):
+                for ti in range(ty):
+                    y = band * ty + ti
+                    if y >= ny:
+                        continue
+                    x0 = (xc * tx + np.arange(tx)) * V
+                    xa = np.minimum(x0, pitch - V)
+                    for cur in (0, 1):
+                        src = cur * 9 * plane  # elements from the base
+                        dst = (cur ^ 1) * 9 * plane
+                        for base in (src, dst):
+                            offs = base + 8 * plane + y * pitch + xa + V - 1  # the highest plane and element
+                            assert offs.max() * elem < pop * (2 if base else 1)
+                    links = 18 * plane * elem  # byte offset of the link words
+                    assert links == 2 * pop and links + (y * pitch + xa.max() + V) * 2 <= alloc
+                    act = x0 < nx
+                    for x in x0[act]:
+                        seen[y, x:x + V] += 1
+            assert (seen[:, :nx] == 1).all()
+
+
 def test_invariant_division_formula():
     """The D3Q27 kernels turn cell indices into (x, y, z) by the multiply-high division of
     csrc/d3q27.cu (FastDiv, Granlund-Montgomery 1994): checked against integer division for every
