@@ -733,7 +733,7 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
 float *cur(lbm_ctx *ctx) { return static_cast<float *>(ctx->f[ctx->cur]); }
 float *nxt(lbm_ctx *ctx) { return static_cast<float *>(ctx->f[ctx->cur ^ 1]); }
 
-// Tau of the context, with RN(1/tau) and the verdict of the exhaustive division check, cached per
+// Tau of the context, with RN(1/tau) and the outcome of the exhaustive division check, cached per
 // tau value for the process (the check runs once per value, a few milliseconds on the GPU).
 Tau tau_of(lbm_ctx *ctx) {
     static std::mutex mu;
