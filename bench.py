@@ -154,7 +154,12 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def channel_flags():
+def channel_flags(product=True):
+    """The benchmark channel's flags: from the library's generator, or (product=False, the CPU arms)
+    from the oracle's restatement of it, which gives the same bytes without loading the library."""
+    if not product:
+        import oracle
+        return oracle.channel_flags(NX, NY, NDISKS, RMIN, RMAX, SEED)
     import latticeboltzmanncuda_gb300 as lbm
     flags, _ = lbm.gen_channel(NX, NY, NDISKS, RMIN, RMAX, SEED)
     return flags
@@ -221,7 +226,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     import oracle
-    flags = channel_flags()
+    flags = channel_flags(product=False)
     per = max(args.cpu_seconds / max(args.steps + args.warmup, 1), 0.5)
     # each bench step is a bounded sample of the solve: the same steps count every time
     _, steps, threads = cpu_port_mlups(flags, per)

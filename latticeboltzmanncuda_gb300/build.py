@@ -1,9 +1,10 @@
 """Build liblbm_gb300.so in-tree: every CUDA / C++ source of csrc/ compiled by nvcc for sm_103a only,
 in parallel, then linked into one shared library with the C ABI of include/lbm_capi.h.
 
-    python -m latticeboltzmanncuda_gb300.build [--force] [--debug]
+    python -m latticeboltzmanncuda_gb300.build [--force] [-v]
 
---debug adds -DLBM_CHECK_BOUNDS (bounds-checked kernels) and -G-free host asserts.
+The kernels' index arithmetic is checked on the CPU instead of by a bounds-checked device build:
+tests/test_index_bounds.py replays every launch shape's addressing against the buffer sizes.
 """
 from __future__ import annotations
 
@@ -37,13 +38,10 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build liblbm_gb300.so")
 
 
-def _flags(debug: bool):
+def _flags():
     # host code: no floating-point contraction, so x86-64 and aarch64 builds give the same results
-    f = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
-         "-I", INCLUDE, "-I", CSRC, "--expt-relaxed-constexpr"]
-    if debug:
-        f += ["-DLBM_CHECK_BOUNDS"]
-    return f
+    return ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
+            "-I", INCLUDE, "-I", CSRC, "--expt-relaxed-constexpr"]
 
 
 def _digest(paths, extra: str) -> str:
@@ -61,17 +59,17 @@ def _inputs():
     return [os.path.join(CSRC, s) for s in SOURCES] + hdrs
 
 
-def build(force: bool = False, debug: bool = False, verbose: bool = False) -> str:
+def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     stamp = os.path.join(OUT_DIR, "stamp")
-    digest = _digest(_inputs(), " ".join(_flags(debug)) + " ".join(ARCH))
+    digest = _digest(_inputs(), " ".join(_flags()) + " ".join(ARCH))
     if not force and os.path.exists(LIB) and os.path.exists(stamp):
         with open(stamp) as fh:
             if fh.read().strip() == digest:
                 build_compat()
                 return LIB
     cc = nvcc()
-    flags = _flags(debug)
+    flags = _flags()
 
     def compile_one(src):
         obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
@@ -106,6 +104,17 @@ def _cxx() -> str:
     raise RuntimeError("no C++ compiler found for the compatibility layer")
 
 
+def cuda_dirs():
+    """(include dir, library dir holding libcudart.so) of the CUDA toolkit that nvcc belongs to."""
+    root = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+    lib = os.path.join(root, "lib64")
+    if not os.path.exists(os.path.join(lib, "libcudart.so")):
+        import glob
+        found = glob.glob(os.path.join(root, "targets", "*", "lib", "libcudart.so"))
+        lib = os.path.dirname(found[0]) if found else lib
+    return os.path.join(root, "include"), lib
+
+
 def build_compat(force: bool = False) -> str:
     """The reference's C++ API (compat/include, compat/src/compat.cpp) as liblbm_compat.so on top of
     liblbm_gb300.so, and the reference's command line as bin/LatticeBoltzmannCuda."""
@@ -117,15 +126,17 @@ def build_compat(force: bool = False) -> str:
         with open(stamp) as fh:
             if fh.read().strip() == digest:
                 return COMPAT_LIB
-    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "include")
+    cuda_inc, cuda_lib = cuda_dirs()
     common = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-I", os.path.join(COMPAT, "include"),
               "-I", INCLUDE, "-I", cuda_inc]
+    # the layer itself calls the CUDA runtime (device ReflectionData objects of the reference's launcher)
+    cudart = ["-L", cuda_lib, "-lcudart", f"-Wl,-rpath,{cuda_lib}"]
     os.makedirs(os.path.dirname(CLI), exist_ok=True)
     steps = [
         [_cxx(), *common, "-shared", srcs[0], "-o", COMPAT_LIB + ".tmp", "-L", PKG, "-llbm_gb300",
-         "-Wl,-rpath,$ORIGIN"],
+         "-Wl,-rpath,$ORIGIN", *cudart],
         [_cxx(), *common, srcs[1], "-o", CLI + ".tmp", "-L", PKG, "-llbm_compat", "-llbm_gb300",
-         "-Wl,-rpath,$ORIGIN/.."],
+         "-Wl,-rpath,$ORIGIN/..", *cudart],
     ]
     for cmd, out in zip(steps, (COMPAT_LIB, CLI)):
         if cmd is steps[1]:
@@ -142,10 +153,9 @@ def build_compat(force: bool = False) -> str:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--force", action="store_true")
-    ap.add_argument("--debug", action="store_true")
     ap.add_argument("-v", "--verbose", action="store_true")
     a = ap.parse_args()
-    print(build(force=a.force, debug=a.debug, verbose=a.verbose))
+    print(build(force=a.force, verbose=a.verbose))
 
 
 if __name__ == "__main__":

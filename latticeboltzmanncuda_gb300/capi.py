@@ -23,6 +23,7 @@ ORDER_STREAM_COLLIDE, ORDER_CLI = 0, 1
 EQ_FLOAT_FLOAT, EQ_FP64 = 0, 1
 OP_STREAM, OP_REFLECT, OP_COLLIDE, OP_FLOW = 1, 2, 4, 8
 FORCE_REFERENCE, FORCE_MOMENTUM_EXCHANGE = 0, 1
+NOALLOC_MAX_ROWS = 32768  # LBM_NOALLOC_MAX_ROWS
 
 DTYPES = {"f32": F32, "f16s": F16S, "bf16s": BF16S, "f64": F64}
 MODES = {"d2q9": D2Q9, "d3q27_ref": D3Q27_REF}

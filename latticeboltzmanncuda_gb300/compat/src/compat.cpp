@@ -10,6 +10,8 @@
 //
 // Error behaviour follows the reference: failures are printed ("<method> failed: <reason>") and the
 // call returns; retrieve_data returns nullptr on failure.
+#include <cuda_runtime.h>
+
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -429,10 +431,28 @@ namespace RunCudaFunctions
             report(w, "null ReflectionData");
             return;
         }
-        // the pass adds its force to *reflection; the lattice's own accumulation state is restored after
+        // The reference passes the device copy that Lattice::setReflectionData made with cudaMalloc
+        // (Lattice.cpp:58, 192); a host object works too.  A device object is read and written back
+        // with cudaMemcpy, as Lattice::retrieve_reflection_data reads it (Lattice.cpp:440).
+        cudaPointerAttributes attr{};
+        bool on_device = false;
+        if (cudaPointerGetAttributes(&attr, reflection) == cudaSuccess)
+            on_device = attr.type == cudaMemoryTypeDevice;
+        else
+            cudaGetLastError();  // an unregistered host pointer: clear the error the query left
+        ReflectionData value{};
+        if (on_device) {
+            if (cudaMemcpy(&value, reflection, sizeof(ReflectionData), cudaMemcpyDeviceToHost) != cudaSuccess) {
+                report(w, cudaGetErrorString(cudaGetLastError()));
+                return;
+            }
+        } else {
+            value = *reflection;
+        }
+        // the pass adds its force to the object; the lattice's own accumulation state is restored after
         const int32_t was = lbm_force_accumulation(c);
         float keep[3] = {0.0f, 0.0f, 0.0f};
-        const float in[3] = {reflection->x, reflection->y, reflection->z};
+        const float in[3] = {value.x, value.y, value.z};
         float out[3];
         int st = lbm_get_force(c, keep);
         if (st == LBM_OK) st = lbm_set_force(c, in, 1);
@@ -440,10 +460,14 @@ namespace RunCudaFunctions
         if (st == LBM_OK) st = lbm_get_force(c, out);
         if (st == LBM_OK) st = lbm_set_force(c, keep, was);
         run(c, st, w);
-        if (st == LBM_OK) {
-            reflection->x = out[0];
-            reflection->y = out[1];
-            reflection->z = out[2];
+        if (st != LBM_OK) return;
+        value.x = out[0];
+        value.y = out[1];
+        value.z = out[2];
+        if (!on_device) {
+            *reflection = value;
+        } else if (cudaMemcpy(reflection, &value, sizeof(ReflectionData), cudaMemcpyHostToDevice) != cudaSuccess) {
+            report(w, cudaGetErrorString(cudaGetLastError()));
         }
     }
 

@@ -319,7 +319,7 @@ __global__ void store_kernel(const S *__restrict__ src, H *__restrict__ host, in
     } else {
 #pragma unroll
         for (int q = 0; q < 9; ++q)
-            host[q * n + (int64_t)y * nx + x] = (H)(d2q9::ldq<S>(src + q * plane + c, q) + d2q9::w<R>(q));
+            host[q * n + (int64_t)y * nx + x] = (H)d2q9::ldq<S>(src + q * plane + c, q) + d2q9::w<H>(q);
     }
 }
 

@@ -10,8 +10,13 @@
 //
 // The array is a file-scope static __device__ array of LBM_NOALLOC_MAX_ROWS / 4 partial triples
 // (192 KiB); every GPU that loads the library holds it until the process exits.  Host code reaches
-// it through the address that cudaGetSymbolAddress returns for the current device, looked up once
-// per device on the first call (with that device current) and cached.
+// it through the address that cudaGetSymbolAddress returns for the current CUDA context, looked up
+// on the first call made in that context (with its device current) and cached under the context's
+// unique id (cuCtxGetId): a caller on its own context (cuCtxCreate) or on a primary context created
+// anew after cudaDeviceReset gets that context's own address, never one of another context.
+#include <cuda.h>
+
+#include <map>
 #include <mutex>
 
 #include "lbm_internal.h"
@@ -26,32 +31,69 @@ namespace {
 constexpr int kRowsPerBlock = 4;
 constexpr int kMaxRows = LBM_NOALLOC_MAX_ROWS;
 constexpr int kMaxBlocks = kMaxRows / kRowsPerBlock;
-constexpr int kMaxDevices = 64;
 
 // One (mass, momentum x, momentum y) partial per block of kRowsPerBlock rows.  Every block writes its
 // own triple before the finaliser reads it, so nothing carries over from the previous call.
 static __device__ __align__(256) double g_partials[kMaxBlocks * 3];
 
-std::mutex g_mu;
-double *g_partials_addr[kMaxDevices] = {};
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
 
-// Device address of g_partials on the current device (looked up once per device).
-lbm_status partials_on_current_device(double **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return lbm::set_thread_error(LBM_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return lbm::set_thread_error(LBM_ERR_UNSUPPORTED, "device ordinal beyond 63");
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_partials_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_partials);
-        if (e != cudaSuccess || !p)
-            return lbm::set_thread_error(LBM_ERR_CUDA, std::string("cudaGetSymbolAddress of the static partials: ") +
-                                                           cudaGetErrorString(e));
-        g_partials_addr[dev] = static_cast<double *>(p);
+std::mutex g_mu;
+std::map<unsigned long long, double *> g_partials_addr;  // context id -> device address of g_partials
+CtxGetIdFn g_ctx_get_id = nullptr;
+bool g_ctx_get_id_looked_up = false;
+
+// Unique id of the current context (0 when the driver entry point is unavailable or no context is
+// current).  The driver function is reached through the runtime, so the library needs no link
+// against libcuda.  Called with g_mu held.
+unsigned long long current_context_id() {
+    if (!g_ctx_get_id_looked_up) {
+        g_ctx_get_id_looked_up = true;
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(fn);
     }
-    *out = g_partials_addr[dev];
+    unsigned long long id = 0;
+    if (!g_ctx_get_id || g_ctx_get_id(nullptr, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+lbm_status symbol_address(double **out) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_partials);
+    if (e != cudaSuccess || !p)
+        return lbm::set_thread_error(LBM_ERR_CUDA, std::string("cudaGetSymbolAddress of the static partials: ") +
+                                                       cudaGetErrorString(e));
+    *out = static_cast<double *>(p);
     return LBM_OK;
+}
+
+// Device address of g_partials in the current context (looked up once per context).
+lbm_status partials_in_current_context(double **out) {
+    int dev = 0;
+    const cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return lbm::set_thread_error(LBM_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    std::lock_guard<std::mutex> lk(g_mu);
+    unsigned long long id = current_context_id();
+    if (id == 0) {
+        // no context current yet: the symbol lookup makes the device's primary context current
+        lbm_status st = symbol_address(out);
+        if (st != LBM_OK) return st;
+        id = current_context_id();
+        if (id == 0) return LBM_OK;  // no context ids from this driver: the address just looked up
+        g_partials_addr[id] = *out;
+        return LBM_OK;
+    }
+    auto it = g_partials_addr.find(id);
+    if (it != g_partials_addr.end()) {
+        *out = it->second;
+        return LBM_OK;
+    }
+    lbm_status st = symbol_address(out);
+    if (st == LBM_OK) g_partials_addr[id] = *out;
+    return st;
 }
 
 // FP64 sums of the unshifted populations over fluid cells, kRowsPerBlock rows per block
@@ -95,10 +137,10 @@ extern "C" LBM_API lbm_status lbm_d2q9_conservation_noalloc(const void *dev_popu
         return lbm::set_thread_error(LBM_ERR_INVALID, "lbm_d2q9_conservation_noalloc: ny = " + std::to_string(ny) +
                                                           " rows exceeds the maximum of " + std::to_string(kMaxRows) +
                                                           " rows that its fixed scratch array holds");
-    if ((int64_t)9 * row_pitch * ny > ((int64_t)1 << 40))
+    if (row_pitch > (((int64_t)1 << 40) / 9) / ny)  // 9 * row_pitch * ny > 2^40, without overflowing
         return lbm::set_thread_error(LBM_ERR_INVALID, "lbm_d2q9_conservation_noalloc: population buffer too large");
     double *partials = nullptr;
-    lbm_status st = partials_on_current_device(&partials);
+    lbm_status st = partials_in_current_context(&partials);
     if (st != LBM_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int nblocks = (ny + kRowsPerBlock - 1) / kRowsPerBlock;

@@ -228,3 +228,65 @@ def d2q9_conservation(f, flags):
     fn = getattr(lib(), f"orc_d2q9_conservation_{_real(f.dtype)}")
     _chk(fn(nx, ny, _p(flags), _p(f), _p(out)), "conservation")
     return out
+
+
+# ----------------------------------------------------------------------------- seeded channel geometry
+_M64 = (1 << 64) - 1
+
+
+class _SplitMix64:
+    """SplitMix64 (Steele, Lea, Flood 2014), the generator behind the library's seeded geometry;
+    restated here so that the CPU baseline builds the benchmark channel without the GPU library."""
+
+    def __init__(self, seed):
+        self.s = int(seed) & _M64
+
+    def next(self):
+        self.s = (self.s + 0x9E3779B97F4A7C15) & _M64
+        z = self.s
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _M64
+        return z ^ (z >> 31)
+
+    def u01(self):
+        return float(self.next() >> 11) * (1.0 / 9007199254740992.0)
+
+
+def channel_flags(nx, ny, ndisks, rmin, rmax, seed):
+    """D2Q9 channel flags: walls on rows 0 and ny-1, `ndisks` non-overlapping disks (x-periodic
+    distance) with centres uniform in [0,nx) x [0,ny) and radius uniform in [rmin, rmax], placed by
+    rejection in SplitMix64 order; a cell is solid when its centre lies inside a disk (x wraps).
+    The same flags as the library's lbm_gen_channel for the same arguments."""
+    flags = np.zeros((ny, nx), np.uint8)
+    flags[0, :] = 1
+    flags[-1, :] = 1
+    rng = _SplitMix64(seed)
+    rmin32, span32 = float(np.float32(rmin)), float(np.float32(rmax)) - float(np.float32(rmin))
+    placed = []
+    for _ in range(1000000):
+        if len(placed) >= ndisks:
+            break
+        d = (rng.u01() * nx, rng.u01() * ny, rmin32 + rng.u01() * span32)
+        ok = True
+        for p in placed:
+            dx = abs(d[0] - p[0])
+            dx = min(dx, nx - dx)
+            dy = d[1] - p[1]
+            if dx * dx + dy * dy < (d[2] + p[2]) * (d[2] + p[2]):
+                ok = False
+                break
+        if ok:
+            placed.append(d)
+    if len(placed) < ndisks:
+        raise ValueError(f"could not place {ndisks} non-overlapping disks")
+    for cx, cy, r in placed:
+        y0, y1 = max(0, int(np.floor(cy - r - 1.0))), min(ny - 1, int(np.ceil(cy + r + 1.0)))
+        x0, x1 = int(np.floor(cx - r - 1.0)), int(np.ceil(cx + r + 1.0))
+        ys = np.arange(y0, y1 + 1)
+        xs = np.arange(x0, x1 + 1)
+        dy = (ys + 0.5) - cy
+        dx = (xs + 0.5) - cx
+        inside = dx[None, :] ** 2 + dy[:, None] ** 2 <= r * r
+        yy, xx = np.nonzero(inside)
+        flags[ys[yy], np.mod(xs[xx], nx)] = 1
+    return flags

@@ -1,7 +1,8 @@
 """The reference's own CUDA kernels as a GPU oracle -- TEST INFRASTRUCTURE, NOT PRODUCT CODE.
 
 Recipe (``build()``):
-  1. Where the reference sources are readable (REFERENCE_ROOT, default /root/reference), compile
+  1. Where the reference sources are readable (the directory given to build(), else the
+     REFERENCE_ROOT environment variable; there is no built-in default), compile
      simulation/source/SimCalcFuncs.cu with simulation/source/FlowCriterion.cu force-included as one
      translation unit, for sm_103a, into oracle/_ref/ref_kernels.cubin.  The sources are compiled
      where they lie; nothing is copied.  (The reference builds these two files with separable
@@ -25,7 +26,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 CUBIN = os.path.join(REF_DIR, "ref_kernels.cubin")
 HARNESS = os.path.join(REF_DIR, "libref_harness.so")
-REFERENCE_ROOT = os.environ.get("REFERENCE_ROOT", "/root/reference")
 
 LATTICE_POINT = np.dtype({
     "names": ["x", "y", "z", "f", "isReflected", "isInternal", "reflections", "d_reflections"],
@@ -41,10 +41,15 @@ def _nvcc():
     raise RuntimeError("nvcc not found")
 
 
-def build_cubin(force=False) -> bool:
-    src = os.path.join(REFERENCE_ROOT, "simulation", "source", "SimCalcFuncs.cu")
-    flow = os.path.join(REFERENCE_ROOT, "simulation", "source", "FlowCriterion.cu")
-    inc = os.path.join(REFERENCE_ROOT, "simulation", "include")
+def build_cubin(reference_root=None, force=False) -> bool:
+    """Compile the reference kernels from the sources under `reference_root` (or $REFERENCE_ROOT).
+    Without either, or where the sources are absent, an existing cubin is kept as it is."""
+    root = reference_root or os.environ.get("REFERENCE_ROOT")
+    if not root:
+        return os.path.exists(CUBIN)
+    src = os.path.join(root, "simulation", "source", "SimCalcFuncs.cu")
+    flow = os.path.join(root, "simulation", "source", "FlowCriterion.cu")
+    inc = os.path.join(root, "simulation", "include")
     if not os.path.exists(src):
         return os.path.exists(CUBIN)
     if os.path.exists(CUBIN) and not force and os.path.getmtime(CUBIN) > os.path.getmtime(src):
@@ -67,8 +72,8 @@ def build_harness(force=False) -> bool:
     return True
 
 
-def build(force=False) -> bool:
-    ok = build_cubin(force)
+def build(reference_root=None, force=False) -> bool:
+    ok = build_cubin(reference_root, force)
     build_harness(force)
     return ok
 

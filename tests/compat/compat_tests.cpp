@@ -8,6 +8,8 @@
 //
 // usage: compat_tests <dir with the test meshes as OBJ files> [--host-only]
 // --host-only runs the cases that need no GPU (Model, Geometry, compressInts, distributeVector).
+#include <cuda_runtime.h>
+
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -123,6 +125,49 @@ static void TestReflections(bool withData)
         got(name, 196, reflection->z);
     }
     delete reflection;
+}
+
+// TestReflectionsData with the launcher called as Lattice::simulateReflections calls it
+// (Lattice.cpp:192): the ReflectionData is the device copy that Lattice::allocateReflectionData makes
+// with cudaMalloc (Lattice.cpp:58), read back with cudaMemcpy as retrieve_reflection_data does
+// (Lattice.cpp:440).
+static void TestReflectionsDeviceData()
+{
+    const char* name = "CalculationsTest.TestReflectionsData";
+    dim3 threads(3, 3, 3), blocks(1, 1, 1);
+    Lattice lattice(3, 3, 3, blocks, threads, FluidData(1.0, 1.0), 0.5);
+    LatticeData data(lattice.getCudaDataPointer(), lattice.getDimensions());
+    lattice.insertModel(mesh("cube_angled.obj"));
+    lattice.preProcessModel();
+    LatticePoint* a = lattice.retrieve_data();
+    a[at(lattice, 1, 1, 1)].particle_distribution[1] = 1.0;
+    lattice.load_data(a);
+    delete[] a;
+    ReflectionData start;
+    ReflectionData* d_reflection = nullptr;
+    if (cudaMalloc(&d_reflection, sizeof(ReflectionData)) != cudaSuccess ||
+        cudaMemcpy(d_reflection, &start, sizeof(ReflectionData), cudaMemcpyHostToDevice) != cudaSuccess) {
+        fprintf(stderr, "cudaMalloc / cudaMemcpy of the ReflectionData failed\n");
+        return;
+    }
+    RunCudaFunctions::run_prime_points(blocks, threads, data);
+    RunCudaFunctions::run_calculate_reflections_data(blocks, threads, data, data, d_reflection);
+    a = lattice.retrieve_data();
+    got(name, 186, a[at(lattice, 2, 1, 2)].particle_distribution[17]);
+    got(name, 187, a[at(lattice, 1, 1, 2)].particle_distribution[4]);
+    got(name, 188, a[at(lattice, 2, 2, 2)].particle_distribution[26]);
+    got(name, 190, a[at(lattice, 1, 1, 1)].particle_distribution[1]);
+    delete[] a;
+    ReflectionData back;
+    if (cudaMemcpy(&back, d_reflection, sizeof(ReflectionData), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        fprintf(stderr, "cudaMemcpy of the ReflectionData failed\n");
+        cudaFree(d_reflection);
+        return;
+    }
+    cudaFree(d_reflection);
+    got(name, 194, back.x);
+    got(name, 195, back.y);
+    got(name, 196, back.z);
 }
 
 static void TestFlowGeneration(bool plane)
@@ -318,6 +363,7 @@ int main(int argc, char** argv)
     TestFull();
     TestReflections(false);
     TestReflections(true);
+    TestReflectionsDeviceData();
     TestFlowGeneration(false);
     TestFlowGeneration(true);
     TestCoordsMatch();

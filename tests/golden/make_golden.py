@@ -2,7 +2,7 @@
 
 Run once, where the reference sources are readable:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout>
 
 It reads the reference's GoogleTest files as text and records every EXPECT_NEAR / EXPECT_EQ /
 EXPECT_TRUE / EXPECT_FALSE assertion of the tests that pin the collide-stream path, with the test
@@ -151,7 +151,9 @@ def extract(root: str) -> dict:
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference checkout>")
+    root = sys.argv[1]
     data = extract(root)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_known_answers.json")
     with open(dst, "w") as fh:

@@ -33,10 +33,11 @@ def meshes(tmp_path_factory, golden):
 def compat_tests(tmp_path_factory):
     lbm_build.build()
     exe = str(tmp_path_factory.mktemp("compat") / "compat_tests")
-    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(lbm_build.nvcc()))), "include")
+    cuda_inc, cuda_lib = lbm_build.cuda_dirs()
     cmd = ["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-I", os.path.join(lbm_build.COMPAT, "include"),
            "-I", lbm_build.INCLUDE, "-I", cuda_inc, os.path.join(HERE, "compat", "compat_tests.cpp"), "-o", exe,
-           "-L", lbm_build.PKG, "-llbm_compat", "-llbm_gb300", f"-Wl,-rpath,{lbm_build.PKG}"]
+           "-L", lbm_build.PKG, "-llbm_compat", "-llbm_gb300", f"-Wl,-rpath,{lbm_build.PKG}",
+           "-L", cuda_lib, "-lcudart", f"-Wl,-rpath,{cuda_lib}"]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     return exe
 
@@ -106,6 +107,9 @@ def test_compat_all_reference_cases(golden, compat_tests, meshes):
     records = run_records(compat_tests, meshes, host_only=False)
     check_records(golden, records, minimum=60)
     tests = {r["test"] for r in records}
+    # TestReflectionsData runs twice: host ReflectionData through Lattice, device ReflectionData
+    # (cudaMalloc, as Lattice.cpp:58 makes it) through RunCudaFunctions::run_calculate_reflections_data
+    assert sum(r["test"] == "CalculationsTest.TestReflectionsData" and r["line"] == 194 for r in records) == 2
     for t in ("CalculationsTest.TestStreaming", "CalculationsTest.TestCollision", "CalculationsTest.TestFull",
               "CalculationsTest.TestReflections", "CalculationsTest.TestReflectionsData",
               "CalculationsTest.TestFlowGeneration", "CalculationsTest.TestPlaneFlowGeneration",

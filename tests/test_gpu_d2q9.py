@@ -4,8 +4,9 @@ Tolerances (stated per storage type):
   FP64 storage  max |f_gpu - f_oracle| <= 1e-12   (same arithmetic, different evaluation order)
   FP32 storage  max |f_gpu - f_oracle64| <= 1e-5 * max|f|, and velocity field within 1e-4 of max|u|
                 relative after the run (FP32 rounding accumulated over the run)
-  FP16/BF16-shifted storage: velocity within 2e-2 / 1e-1 of max|u| (storage precision 2^-11 / 2^-8
-                of the shifted populations)
+  FP16/BF16-shifted storage on a 48 x 40 lid-driven cavity after 400 steps: relative velocity L2
+                within 1e-3 / 1e-2 and max within 2e-3 / 2e-2 (storage precision 2^-11 / 2^-8 of the
+                shifted populations; the benchmark-size cases are in test_gpu_configs.py)
 """
 import zlib
 
@@ -112,8 +113,8 @@ def test_fp32_gpu_within_tolerance_of_fp64_oracle(name):
     assert err <= 1e-5 * np.max(np.abs(ref)), err
 
 
-@pytest.mark.parametrize("dtype,tol", [("f16s", 2e-2), ("bf16s", 1e-1)])
-def test_shifted_half_storage_velocity(dtype, tol):
+@pytest.mark.parametrize("dtype,tol_l2,tol_max", [("f16s", 1e-3, 2e-3), ("bf16s", 1e-2, 2e-2)])
+def test_shifted_half_storage_velocity(dtype, tol_l2, tol_max):
     nx, ny = 48, 40
     flags = box(nx, ny, lid=True)
     f0 = oracle.d2q9_equilibrium(np.ones((ny, nx)), np.zeros((ny, nx)), np.zeros((ny, nx)))
@@ -122,7 +123,9 @@ def test_shifted_half_storage_velocity(dtype, tol):
     _, (rho, ux, uy), _ = gpu_run(flags, f0, 0.6, 400, 0, (0, 0), (0.05, 0), dtype)
     umax = np.max(np.hypot(rux, ruy))
     err = np.max(np.hypot(ux - rux, uy - ruy)) / umax
-    assert err < tol, err
+    l2 = float(np.sqrt(np.sum((ux - rux) ** 2 + (uy - ruy) ** 2) / np.sum(rux ** 2 + ruy ** 2)))
+    print(f"PARITY {{\"case\": \"cavity 48x40 {dtype}\", \"vel_max\": {err:.3e}, \"vel_l2\": {l2:.3e}}}")
+    assert l2 <= tol_l2 and err <= tol_max, (l2, err)
 
 
 def test_cavity_128_2000_steps_fp32():

@@ -144,3 +144,12 @@ def test_f32_tracks_f64():
     a = oracle.d2q9_run(f64, fl, 0.6, 300, wall_velocity=(0.05, 0.0))
     b = oracle.d2q9_run(f64.astype(np.float32), fl, np.float32(0.6), 300, wall_velocity=(0.05, 0.0))
     assert np.max(np.abs(a - b)) < 1e-5
+
+
+def test_oracle_channel_flags_equal_the_library_generator():
+    """The CPU baseline builds the benchmark channel with the oracle's restatement of the seeded
+    generator; it must give the library's bytes (the headline channel and smaller cases)."""
+    import latticeboltzmanncuda_gb300 as lbm
+    for args in ((4096, 1024, 64, 8.0, 24.0, 20261203), (300, 77, 9, 3.0, 9.5, 1), (64, 20, 2, 2.0, 4.0, 3)):
+        want, _ = lbm.gen_channel(*args)
+        assert np.array_equal(oracle.channel_flags(*args), want), args

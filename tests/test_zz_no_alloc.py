@@ -75,3 +75,59 @@ def test_noalloc_rejects_too_many_rows_and_bad_arguments():
     assert rc == capi.ERR_INVALID and "maximum" in capi.last_thread_error()
     assert noalloc(f_dev, 7, flags_dev, 8, 1, 8, out, 0) == capi.ERR_INVALID
     assert noalloc(f_dev, capi.F32, flags_dev, 8, 1, 4, out, 0) == capi.ERR_INVALID
+
+
+def _state(nx, ny, seed, steps=9):
+    flags, rho, ux, uy = domain(nx, ny, seed)
+    with lbm.Lattice(nx, ny, dtype="f64", tau=0.7, wall_velocity=(0.03, 0, 0)) as L:
+        L.set_flags(flags)
+        L.init_equilibrium(rho, ux, uy)
+        L.step(steps)
+        return flags, L.conservation()[:3], L.retrieve_populations(np.float64)
+
+
+def test_noalloc_at_the_row_limit():
+    """ny == LBM_NOALLOC_MAX_ROWS fills every partial triple of the fixed array."""
+    torch = pytest.importorskip("torch")
+    nx, ny = 4, capi.NOALLOC_MAX_ROWS
+    flags = np.zeros((ny, nx), np.uint8)
+    flags[:, 0] = lbm.WALL
+    rng = np.random.default_rng(11)
+    with lbm.Lattice(nx, ny, dtype="f64", tau=0.8, periodic=2) as L:
+        L.set_flags(flags)
+        L.init_equilibrium((1 + 0.01 * rng.standard_normal((ny, nx))).astype(np.float32),
+                           (0.02 * rng.standard_normal((ny, nx))).astype(np.float32),
+                           (0.02 * rng.standard_normal((ny, nx))).astype(np.float32))
+        L.step(5)
+        want = L.conservation()[:3]
+        host = L.retrieve_populations(np.float64)
+    dev = torch.device("cuda", 0)
+    f_dev = torch.from_numpy(host).to(dev).contiguous()
+    flags_dev = torch.from_numpy(flags).to(dev)
+    out = torch.full((3,), float("nan"), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    assert noalloc(f_dev, capi.F64, flags_dev, nx, ny, nx, out, stream) == capi.OK, capi.last_thread_error()
+    torch.cuda.synchronize(dev)
+    got = out.cpu().numpy()
+    scale = np.array([abs(want[0]), abs(want[0]) * 1e-3, abs(want[0]) * 1e-3])
+    assert np.all(np.abs(got - want) <= 1e-12 * scale), (got, want)
+
+
+def test_noalloc_two_calls_in_one_stream_keep_their_own_results():
+    """Calls queued back to back on one stream share the fixed array but are ordered, so each gives
+    the sums of its own inputs."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", 0)
+    (fa, wa, ha), (fb, wb, hb) = _state(90, 61, 21), _state(57, 130, 22)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    bufs = []
+    for flags, host in ((fa, ha), (fb, hb)):
+        bufs.append((torch.from_numpy(host).to(dev).contiguous(), torch.from_numpy(flags).to(dev),
+                     torch.full((3,), float("nan"), dtype=torch.float64, device=dev), flags.shape))
+    for f_dev, flags_dev, out, (ny, nx) in bufs:
+        assert noalloc(f_dev, capi.F64, flags_dev, nx, ny, nx, out, stream) == capi.OK, capi.last_thread_error()
+    torch.cuda.synchronize(dev)
+    for (_, _, out, _), want in zip(bufs, (wa, wb)):
+        got = out.cpu().numpy()
+        scale = np.array([abs(want[0]), abs(want[0]) * 1e-3, abs(want[0]) * 1e-3])
+        assert np.all(np.abs(got - want) <= 1e-12 * scale), (got, want)
