@@ -15,6 +15,13 @@ Arm "mine" (default) prints one JSON line with
              host->device, 10,000 steps, density/velocity device->host, every step
   roofline   step kernel: algorithmic bytes per launch (72 B x cells) / average launch duration
   cpu_baseline  the CPU oracle (OpenMP, all host cores) on a bounded sample of the same workload
+  batched_vs_plain / served_vs_plain (one GPU only; --no-legs skips them): the other half of the
+             metric, each leg run once after the headline -- the 512-domain batch (2000 steps) in
+             FP16-shifted and FP32 storage against plain FP32 solves one context after another, and a
+             60 requests/s Poisson stream (6 s of arrivals) through the continuous-batching server in
+             FP16-shifted storage against serial plain FP32 solves with every launch shape tuned
+             beforehand (p50/p99 latency, aggregate MLUPS); velocity and density errors of the 16-bit
+             results against FP64 solves of the same domains; details under "legs"
 Arm "reference" times the CPU restatement of the step on the host cores (the reference has no CPU
 implementation of its own) on the same workload and prints the same kind of line.
 """
@@ -70,6 +77,10 @@ def parse():
     ap.add_argument("--serve-rates", default="2,6,10,15,25,60", help="requests per second, comma separated")
     ap.add_argument("--serve-duration", type=float, default=6.0, help="seconds of arrivals per rate")
     ap.add_argument("--round-steps", type=int, default=200)
+    ap.add_argument("--serve-rate", type=float, default=60.0,
+                    help="Poisson rate of the serve leg of the default line (requests per second)")
+    ap.add_argument("--no-legs", action="store_true",
+                    help="default line without its batch (512 domains) and serve (60 requests/s) legs")
     return ap.parse_args()
 
 
@@ -344,6 +355,14 @@ def run_mine(args):
         cpu = {"value": round(mlups, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
                "sample": f"{NX}x{NY} channel, {steps} FP32 time steps (of {args.lbm_steps}), OpenMP"}
 
+    L.close()
+    legs = {}
+    if rank == 0 and ws == 1 and not args.no_legs:
+        # the other half of the metric, each leg once: batched and served 16-bit storage against the
+        # plain FP32 path on the batch and serve workloads, with their errors against FP64
+        legs["batch"] = batch_leg(args.batch_count, args.batch_steps, args.warmup, args.batch_shape)
+        legs["serve"] = serve_leg(args.serve_rate, args.serve_duration, args.round_steps)
+
     if rank == 0:
         traffic = ncu_traffic(f"d2q9_step_{args.dtype}")
         line = {
@@ -364,8 +383,23 @@ def run_mine(args):
             "clocks": clk.summary(),
             "mass": cons[0],
         }
+        if legs:
+            b, v = legs["batch"], legs["serve"]
+            line["batched_vs_plain"] = {
+                "speedup_f16s": b["speedup_f16s_vs_plain"], "speedup_f32": b["speedup_f32_vs_plain"],
+                "batched_f16s_mlups": b["batched_f16s"]["mlups"], "plain_f32_mlups": b["plain_f32"]["mlups"],
+                "f16s_vel_l2_max_vs_f64": b["error_vs_f64"]["f16s"]["vel_l2_max"],
+                "f16s_rho_l2_max_vs_f64": b["error_vs_f64"]["f16s"]["rho_l2_max"]}
+            line["served_vs_plain"] = {
+                "speedup_f16s": v["speedup_f16s_vs_plain"],
+                "served_f16s_mlups": v["served_f16s"]["aggregate_mlups"],
+                "plain_f32_mlups": v["plain_f32_shapes_cached"]["aggregate_mlups"],
+                "p50_s": [v["served_f16s"]["p50_s"], v["plain_f32_shapes_cached"]["p50_s"]],
+                "p99_s": [v["served_f16s"]["p99_s"], v["plain_f32_shapes_cached"]["p99_s"]],
+                "f16s_vel_l2_max_vs_f64": v["error_vs_f64"]["f16s"]["vel_l2_max"],
+                "f16s_rho_l2_max_vs_f64": v["error_vs_f64"]["f16s"]["rho_l2_max"]}
+            line["legs"] = legs
         print(json.dumps(line), flush=True)
-    L.close()
     if dist:
         dist.destroy_process_group()
     return 0
@@ -382,23 +416,42 @@ def _timed(stream, fn):
     return e0.elapsed_time(e1) / 1000.0
 
 
-def _vel_err(u, v, u64, v64):
-    """(max-norm, L2-norm) relative velocity error against the FP64 run"""
+def _vel_err(u, v, u64, v64, mask=None):
+    """(max-norm, L2-norm) relative velocity error against the FP64 run, over `mask` (default all)"""
+    if mask is not None:
+        u, v, u64, v64 = u[mask], v[mask], u64[mask], v64[mask]
     ref = float(np.max(np.hypot(u64, v64)))
     d = np.hypot(u - u64, v - v64)
     l2 = float(np.sqrt(np.sum(d * d) / max(float(np.sum(u64 * u64 + v64 * v64)), 1e-300)))
     return float(np.max(d)) / max(ref, 1e-30), l2
 
 
-def run_batch(args):
-    """512 independent domains (seeded): batched FP32 and FP16-shifted, one launch per step for all
-    domains, against serial plain FP32 solves (one single-domain context after another)."""
+def _rho_err(r, r64, mask=None):
+    """L2 density error relative to the FP64 run's density deviation sqrt(sum (r - r64)^2 / sum (r64 - 1)^2)"""
+    if mask is not None:
+        r, r64 = r[mask], r64[mask]
+    d = np.asarray(r, np.float64) - r64
+    return float(np.sqrt(np.sum(d * d) / max(float(np.sum((r64 - 1.0) ** 2)), 1e-300)))
+
+
+def _err_summary(errs):
+    """errs: list of (vel max-norm, vel L2, density L2) per domain"""
+    mx, l2, rl2 = [e[0] for e in errs], [e[1] for e in errs], [e[2] for e in errs]
+    return {"vel_l2_max": float(f"{max(l2):.3e}"), "vel_l2_median": float(f"{np.median(l2):.3e}"),
+            "vel_max_norm_max": float(f"{max(mx):.3e}"), "rho_l2_max": float(f"{max(rl2):.3e}"),
+            "rho_l2_median": float(f"{np.median(rl2):.3e}")}
+
+
+def batch_leg(count, nsteps, warmup, shape=""):
+    """Seeded C4 batch (`count` independent domains, `nsteps` steps each): batched FP32 and
+    FP16-shifted storage (one launch per step for all domains) against plain FP32 solves one after
+    another (one single-domain context each, its launch shape tuned before the timed region), with
+    velocity and density errors against FP64 on 16 of the domains."""
     import torch
     import latticeboltzmanncuda_gb300 as lbm
     from latticeboltzmanncuda_gb300 import workloads
 
-    nsteps = args.batch_steps
-    doms = workloads.batch(args.batch_count, SEED, nsteps)
+    doms = workloads.batch(count, SEED, nsteps)
     cells = sum(d.cells for d in doms)
     fluid_total = None
     subset = list(range(0, len(doms), max(1, len(doms) // 16)))
@@ -409,28 +462,31 @@ def run_batch(args):
         with lbm.Batch(dtype, stream=stream.cuda_stream) as B:
             slots = {i: B.add(doms[i].nx, doms[i].ny, doms[i].tau, doms[i].flags, doms[i].periodic,
                               doms[i].body_force, doms[i].wall_velocity) for i in idx}
-            if args.batch_shape and dtype != "f64":
-                B.set_launch(*[int(v) for v in args.batch_shape.split(",")])
+            if shape and dtype != "f64":
+                B.set_launch(*[int(v) for v in shape.split(",")])
                 info = B.info()
             else:
                 info = B.autotune()
             if dtype != "f64":
-                B.step(args.warmup * 10)
+                B.step(warmup * 10)
                 B.synchronize()
                 # restart from equilibrium so every domain runs exactly nsteps inside the timed region
-                for i, s in slots.items():
-                    B.remove(s)
+                for i, sl in slots.items():
+                    B.remove(sl)
                 slots = {i: B.add(d.nx, d.ny, d.tau, d.flags, d.periodic, d.body_force, d.wall_velocity)
                          for i, d in enumerate(doms)}
                 fluid_total = B.info()["fluid_cells"]
                 with ClockSampler(0) as clk:
                     t = _timed(stream, lambda: B.step(nsteps))
-                res[dtype] = {"mlups": cells * nsteps / t / 1e6, "seconds": t, "clocks": clk.summary(),
+                res[dtype] = {"mlups": round(cells * nsteps / t / 1e6, 1), "seconds": round(t, 3),
+                              "clocks": clk.summary(),
                               "shape": [info["cells_per_thread"], info["block_threads"], info["rows_per_block"]],
                               "tiles": B.info()["tiles"]}
             else:
                 B.step(nsteps)
-            vel[dtype] = {i: B.moments(slots[i]) for i in subset}
+            # density: the sum of the stored populations read back in FP64; velocity: lbm moments
+            vel[dtype] = {i: (B.retrieve_populations(slots[i], np.float64).sum(axis=0), *B.moments(slots[i])[1:])
+                          for i in subset}
     # plain: the same domains solved one after another, one single-domain FP32 context each
     t_plain = 0.0
     for d in doms:
@@ -444,29 +500,37 @@ def run_batch(args):
     plain = cells * nsteps / t_plain / 1e6
     errs = {}
     for dtype in ("f32", "f16s"):
-        e = [_vel_err(vel[dtype][i][1], vel[dtype][i][2], vel["f64"][i][1], vel["f64"][i][2]) for i in subset]
-        mx, l2 = [a for a, _ in e], [b for _, b in e]
-        errs[dtype] = {"max_norm_max": max(mx), "max_norm_median": float(np.median(mx)),
-                       "l2_max": max(l2), "l2_median": float(np.median(l2))}
+        e = []
+        for i in subset:
+            fluid = doms[i].flags == 0
+            r, u, v = vel[dtype][i]
+            r64, u64, v64 = vel["f64"][i]
+            e.append((*_vel_err(u, v, u64, v64, fluid), _rho_err(r, r64, fluid)))
+        errs[dtype] = _err_summary(e)
     peak, peak_kind = peaks()
-    line = {
-        "metric": "aggregate MLUPS, batched vs plain", "workload": "batch", "unit": "MLUPS",
-        "value": round(res["f16s"]["mlups"], 1), "higher_is_better": True, "data": "synthetic",
-        "config": {"workload": f"{len(doms)} independent D2Q9 domains, area log-uniform in [64^2, 1024^2], aspect 1-4, "
-                               f"tau 0.52-1.2, disks to 0-30% solid, lid 0.05 or force 1e-6 (p = 1/2), {nsteps} steps "
-                               f"each, seed {SEED}", "cells": cells, "fluid_cells": fluid_total},
-        "batched_f32": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in res["f32"].items()},
-        "batched_f16s": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in res["f16s"].items()},
-        "plain_f32": {"mlups": round(plain, 1), "seconds": round(t_plain, 3)},
+    return {
+        "workload": f"{len(doms)} independent D2Q9 domains, area log-uniform in [64^2, 1024^2], aspect 1-4, "
+                    f"tau 0.52-1.2, disks to 0-30% solid, lid 0.05 or force 1e-6 (p = 1/2), {nsteps} steps each, "
+                    f"seed {SEED}", "cells": cells, "fluid_cells": fluid_total,
+        "batched_f32": res["f32"], "batched_f16s": res["f16s"],
+        "plain_f32": {"mlups": round(plain, 1), "seconds": round(t_plain, 3),
+                      "note": "one context per domain, launch shape tuned before the timed region"},
         "speedup_f16s_vs_plain": round(res["f16s"]["mlups"] / plain, 3),
         "speedup_f32_vs_plain": round(res["f32"]["mlups"] / plain, 3),
-        "velocity_error_vs_f64": {"domains": len(subset), **{k: {kk: float(f"{vv:.3e}") for kk, vv in v.items()}
-                                                             for k, v in errs.items()}},
+        "error_vs_f64": {"domains": len(subset), **errs},
         "roofline_f32": {"achieved": round(res["f32"]["mlups"] * 72 / 1000, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(res["f32"]["mlups"] * 72 / 1000 / peak, 4), "peak_kind": peak_kind},
         "roofline_f16s": {"achieved": round(res["f16s"]["mlups"] * 36 / 1000, 1), "peak": peak, "unit": "GB/s",
                           "frac": round(res["f16s"]["mlups"] * 36 / 1000 / peak, 4), "peak_kind": peak_kind},
     }
+
+
+def run_batch(args):
+    line = {"metric": "aggregate MLUPS, batched vs plain", "workload": "batch", "unit": "MLUPS",
+            "higher_is_better": True, "data": "synthetic"}
+    leg = batch_leg(args.batch_count, args.batch_steps, args.warmup, args.batch_shape)
+    line["value"] = leg["batched_f16s"]["mlups"]
+    line.update(leg)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -492,15 +556,92 @@ def _serial_plain(reqs, dtype="f32"):
     return lat, work, time.perf_counter() - t0
 
 
+def _pretune(reqs, dtype="f32"):
+    """Run the plain path's launch-shape tuner once for every request size (cached in the process), so
+    that a later serial run times the solves alone."""
+    import latticeboltzmanncuda_gb300 as lbm
+    seen = set()
+    for r in reqs:
+        key = (r.nx, r.ny, r.periodic, tuple(r.body_force))
+        if key in seen:
+            continue
+        seen.add(key)
+        with lbm.Lattice(r.nx, r.ny, dtype=dtype, tau=r.tau, periodic=r.periodic, body_force=(*r.body_force, 0),
+                         wall_velocity=(*r.wall_velocity, 0)) as L:
+            L.set_flags(r.flags)
+            L.init_equilibrium()
+            L.autotune()
+
+
 def _pct(v, p):
     return float(np.percentile(np.asarray(v), p)) if len(v) else None
 
 
-def run_serve(args):
-    """Poisson streams of solve requests (side 128-2048 log-uniform, aspect 1-4, 0-30 % solid, tau
-    0.52-1.2, 1k-50k steps) at a sweep of rates, served by the continuous-batching server (150 GB
-    budget) and, for comparison, by serial plain single-domain solves."""
+def _served(reqs, dtype, round_steps, outputs=None):
     import latticeboltzmanncuda_gb300 as lbm
+    with ClockSampler(0) as clk:
+        res, st, status = lbm.serve(reqs, dtype=dtype, budget_bytes=150e9, round_steps=round_steps, outputs=outputs)
+    lat = [r["latency"] for r in res if r["status"] == 0]
+    out = {"status": status, "ok": len(lat), "p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99),
+           "aggregate_mlups": st["cell_updates"] / st["makespan"] / 1e6, "makespan_s": st["makespan"],
+           "peak_slots": st["peak_slots"], "peak_gb": st["peak_bytes"] / 1e9, "rounds": st["rounds"],
+           "round_device_s": st["round_seconds"], "tile_shape": st["tile_shape"], "tunings": st["tunings"],
+           "clocks": clk.summary()}
+    return out, res
+
+
+def _rounded(d):
+    if isinstance(d, dict):
+        return {k: _rounded(v) for k, v in d.items()}
+    if isinstance(d, float):
+        return round(d, 4) if abs(d) >= 1e-3 or d == 0 else float(f"{d:.3e}")
+    return d
+
+
+def serve_leg(rate, duration, round_steps, check=8):
+    """Seeded C5 stream at one Poisson rate: served FP16-shifted (continuous batching, 150 GB budget)
+    against serial plain FP32 solves with every launch shape tuned beforehand; the served results of
+    `check` requests (evenly spread over the lighter half of the stream) against their FP64 solves."""
+    import latticeboltzmanncuda_gb300 as lbm
+    from latticeboltzmanncuda_gb300 import workloads
+
+    reqs = workloads.requests(rate, duration, SEED)
+    work = np.array([r.nx * r.ny * r.steps for r in reqs], float)
+    light = [int(i) for i in np.argsort(work)[: max(1, len(reqs) // 2)]]
+    picks = sorted(light[int(k)] for k in np.linspace(0, len(light) - 1, min(check, len(light))))
+    served, res = _served(reqs, "f16s", round_steps, outputs=set(picks))
+    _pretune(reqs)
+    lat, done, makespan = _serial_plain(reqs)
+    plain = {"p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99), "aggregate_mlups": done / makespan / 1e6,
+             "makespan_s": makespan, "note": "every launch shape tuned before the run"}
+    errs = []
+    for i in picks:
+        r = reqs[i]
+        with lbm.Lattice(r.nx, r.ny, dtype="f64", tau=r.tau, periodic=r.periodic, body_force=(*r.body_force, 0),
+                         wall_velocity=(*r.wall_velocity, 0)) as L:
+            L.set_flags(r.flags)
+            L.init_equilibrium()
+            L.step(r.steps)
+            r64, u64, v64 = L.moments()
+        rho, ux, uy = res[i]["moments"]
+        fluid = r.flags == 0
+        errs.append((*_vel_err(ux.astype(np.float64), uy.astype(np.float64), u64.astype(np.float64),
+                               v64.astype(np.float64), fluid),
+                     _rho_err(rho, r64.astype(np.float64), fluid)))
+    return _rounded({
+        "workload": f"Poisson arrivals at {rate:g}/s for {duration:g} s ({len(reqs)} requests), side 128-2048 "
+                    f"log-uniform, aspect 1-4, solid 0-30 %, tau 0.52-1.2, steps 1k-50k log-uniform, 150 GB budget, "
+                    f"round {round_steps} steps, seed {SEED}",
+        "requests": len(reqs), "cell_updates": float(work.sum()),
+        "served_f16s": served, "plain_f32_shapes_cached": plain,
+        "speedup_f16s_vs_plain": served["aggregate_mlups"] / plain["aggregate_mlups"],
+        "error_vs_f64": {"requests_checked": len(picks), "f16s": _err_summary(errs),
+                         "density_note": "served densities are FP32 moments"}})
+
+
+def run_serve(args):
+    """Poisson streams of solve requests at a sweep of rates, served by the continuous-batching server
+    (150 GB budget) and, for comparison, by serial plain single-domain solves."""
     from latticeboltzmanncuda_gb300 import workloads
 
     rates = [float(r) for r in args.serve_rates.split(",")]
@@ -510,14 +651,7 @@ def run_serve(args):
         row = {"rate_per_s": rate, "requests": len(reqs),
                "cell_updates": float(sum(r.nx * r.ny * r.steps for r in reqs))}
         for dtype in ("f16s", "f32"):
-            res, st, status = lbm.serve(reqs, dtype=dtype, budget_bytes=150e9, round_steps=args.round_steps)
-            lat = [r["latency"] for r in res if r["status"] == 0]
-            row[f"served_{dtype}"] = {"status": status, "ok": len(lat), "p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99),
-                                      "aggregate_mlups": st["cell_updates"] / st["makespan"] / 1e6,
-                                      "makespan_s": st["makespan"], "peak_slots": st["peak_slots"],
-                                      "peak_gb": st["peak_bytes"] / 1e9, "rounds": st["rounds"],
-                                      "round_device_s": round(st["round_seconds"], 3),
-                                      "tile_shape": st["tile_shape"], "tunings": st["tunings"]}
+            row[f"served_{dtype}"], _ = _served(reqs, dtype, args.round_steps)
         # the plain path as a user meets it: every new domain size runs the launch-shape tuner once
         # (its timing inside the makespan); then again with the tuner's choices cached, which leaves
         # only the solves themselves -- the stricter baseline
@@ -539,9 +673,7 @@ def run_serve(args):
             "config": {"workload": f"Poisson arrivals for {args.serve_duration} s per rate, side 128-2048 log-uniform, "
                                    f"aspect 1-4, solid 0-30 %, tau 0.52-1.2, steps 1k-50k log-uniform, 150 GB budget, "
                                    f"round {args.round_steps} steps, seed {SEED}"},
-            "sweep": [{k: (round(v, 4) if isinstance(v, float) else
-                           ({kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()}
-                            if isinstance(v, dict) else v)) for k, v in r.items()} for r in sweep]}
+            "sweep": [_rounded(r) for r in sweep]}
     print(json.dumps(line), flush=True)
     return 0
 

@@ -478,7 +478,8 @@ def serve(requests, dtype="f32", budget_bytes=150e9, max_slots=0, round_steps=20
     """Play `requests` (objects with nx, ny, tau, flags, periodic, body_force, wall_velocity, steps
     and arrival in seconds) through the continuous-batching server (lbm_server_run).  Returns
     (results, stats, run_status): per request a dict with status, admitted, finished, latency and,
-    with outputs=True, (rho, ux, uy)."""
+    with outputs=True (every request) or a collection of request indices (those requests),
+    (rho, ux, uy)."""
     L = capi.lib()
     cfg = capi.ServerConfig()
     L.lbm_server_config_init(ctypes.byref(cfg))
@@ -499,7 +500,7 @@ def serve(requests, dtype="f32", budget_bytes=150e9, max_slots=0, round_steps=20
         keep.append(fl)
         q.flags = None if fl is None else fl.ctypes.data
         q.steps, q.arrival = int(r.steps), float(r.arrival)
-        if outputs:
+        if outputs is True or (outputs and i in outputs):
             o = [np.zeros((r.ny, r.nx), np.float32) for _ in range(3)]
             outs.append(o)
             q.out_rho, q.out_ux, q.out_uy = (a.ctypes.data for a in o)
@@ -515,7 +516,7 @@ def serve(requests, dtype="f32", budget_bytes=150e9, max_slots=0, round_steps=20
     for i in range(n):
         d = {"status": res[i].status, "admitted": res[i].admitted, "finished": res[i].finished,
              "latency": res[i].finished - float(requests[i].arrival)}
-        if outputs:
+        if outs[i] is not None:
             d["moments"] = tuple(outs[i])
         results.append(d)
     stats = {k: getattr(st, k) for k, _ in capi.ServerStats._fields_}

@@ -138,9 +138,10 @@ constexpr int PARAM_SLOTS = 540;
 struct SlotDescP {  // 56 bytes; pitch, plane, buffers and link words follow from these
     void *base;  // the slot's allocation: buffer A, buffer B (9 planes each), link words
     int nx, ny;
-    int bits;    // periodic (bits 0-1), force (bit 2), current buffer at the sequence start (bit 3)
+    int bits;    // periodic (bits 0-1), force (bit 2), current buffer at the sequence start (bit 3),
+                 // shift of the division by the pitch (bits 8-12)
     int stop;    // steps this slot takes in the launch sequence
-    int chunks;  // column chunks per row band
+    unsigned magic;  // multiplier of the division by the pitch (Granlund-Montgomery)
     float omega, fx, fy, uwx, uwy;
 };
 
@@ -152,13 +153,13 @@ struct BatchParams {
 };
 
 // a tile of the parameter-block path for 16-bit storage: the block's slot (an index into the
-// parameter block), row band and column chunk, one 8-byte load.  (FP32 blocks find their slot by a
-// binary search over the slots' first tiles instead: measured on the serve domains, the 16-bit
-// kernel, bound by instruction issue, runs 3 % faster with the load, the FP32 kernel, bound by
-// memory latency, 5 % slower.)
+// parameter block) and the tile's index within the slot, one 8-byte load.  (FP32 blocks find their
+// slot by a binary search over the slots' first tiles instead: measured on the serve domains, the
+// 16-bit kernel, bound by instruction issue, runs 3 % faster with the load, the FP32 kernel, bound
+// by memory latency, 5 % slower.)
 struct TileP {
     int slot;
-    unsigned short band, xchunk;
+    unsigned tile;
 };
 
 template <class S>
@@ -167,16 +168,19 @@ constexpr bool tile_records() {
 }
 static_assert(sizeof(BatchParams) <= 32764, "kernel parameter block limit");
 
+// Parameter-block tiles are flat: tile j of a slot is the run of blockDim.x * blockDim.y * V
+// consecutive cells starting at j * blockDim.x * blockDim.y * V of the slot's padded cell array
+// [0, pitch * ny), row after row (step_vec_flat), so a row costs at most its 31 padding cells of
+// idle lanes instead of the rest of a column chunk, and only a slot's last tile is ragged.
 template <class S, int V>
 __device__ __forceinline__ void batch_tile_p(const BatchParams &p, const TileP *__restrict__ tiles, int step,
                                              int reverse) {
     const int t = reverse ? p.ntiles - 1 - (int)blockIdx.x : (int)blockIdx.x;
-    int slot, band, xchunk;
+    int slot, tile;
     if constexpr (tile_records<S>()) {
-        const TileP tile = tiles[t];
-        slot = tile.slot;
-        band = tile.band;
-        xchunk = tile.xchunk;
+        const TileP rec = tiles[t];
+        slot = rec.slot;
+        tile = (int)rec.tile;
     } else {
         int lo = 0, hi = p.n - 1;
         while (lo < hi) {  // the last slot whose first tile is at or before t (uniform per block)
@@ -184,16 +188,21 @@ __device__ __forceinline__ void batch_tile_p(const BatchParams &p, const TileP *
             if (p.start[mid] <= t) lo = mid; else hi = mid - 1;
         }
         slot = lo;
-        const int i = t - p.start[lo];
-        band = i / p.d[lo].chunks;
-        xchunk = i - band * p.d[lo].chunks;
+        tile = t - p.start[lo];
     }
     const SlotDescP &D = p.d[slot];
     if (step >= D.stop) return;  // the slot has used its step budget
     const int pitch = (D.nx + 31) & ~31, plane = pitch * D.ny;
-    const int y = band * (int)blockDim.y + (int)threadIdx.y;
-    if (y >= D.ny) return;  // uniform per warp
-    const int x0 = (xchunk * (int)blockDim.x + (int)threadIdx.x) * V;
+    const int k = (int)threadIdx.y * (int)blockDim.x + (int)threadIdx.x;
+    const int first = tile * (int)(blockDim.x * blockDim.y) * V;
+    if (first + (k & ~31) * V >= plane) return;  // the warp lies past the slot's last cell (uniform)
+    int i = first + k * V;
+    const bool active = i < plane;
+    if (!active) i = plane - V;  // in bounds; shuffles only, no store
+    // i / pitch by multiply-high (pitch >= 32, so the pre-shift is 1)
+    const uint32_t th = __umulhi(D.magic, (uint32_t)i);
+    const int y = (int)((th + (((uint32_t)i - th) >> 1)) >> ((D.bits >> 8) & 31));
+    const int x0 = i - y * pitch;
     const int cur = ((D.bits >> 3) + step) & 1;
     S *const a = static_cast<S *>(D.base);
     const S *src = a + (size_t)cur * 9 * plane;
@@ -208,9 +217,9 @@ __device__ __forceinline__ void batch_tile_p(const BatchParams &p, const TileP *
     prm.omega_d = prm.fx_d = prm.fy_d = prm.uwx_d = prm.uwy_d = 0.0;  // FP64 storage uses the table path
     const int periodic = D.bits & 3;
     if (D.bits & 4)
-        d2q9::step_vec<S, V, true, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm);
+        d2q9::step_vec_flat<S, V, true, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm, active);
     else
-        d2q9::step_vec<S, V, false, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm);
+        d2q9::step_vec_flat<S, V, false, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm, active);
 }
 
 // registers held to what the table kernel uses (2-wide 64, 4-wide 85, 8-wide 128): the descriptor
@@ -430,12 +439,8 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
         live += s.live ? 1 : 0;
     }
     if (!b->dirty && !b->tiles_dirty && !limited) return LBM_OK;
-    // the parameter-block path: FP32 / 16-bit storage, at most PARAM_SLOTS slots, and row bands and
-    // column chunks that fit the 16-bit fields of its tiles
-    bool params_ok = b->dtype != LBM_F64 && live <= PARAM_SLOTS;
-    for (const Slot &s : b->slots)
-        if (params_ok && s.live)
-            params_ok = (s.desc.ny + b->ty - 1) / b->ty <= 65535 && (s.pitch / b->v + b->tx - 1) / b->tx <= 65535;
+    // the parameter-block path: FP32 / 16-bit storage and at most PARAM_SLOTS slots
+    const bool params_ok = b->dtype != LBM_F64 && live <= PARAM_SLOTS;
     if (params_ok) {  // descriptors as kernel parameters
         BatchParams &p = b->params;
         p.n = 0;
@@ -449,9 +454,13 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
             d.nx = s.desc.nx;
             d.ny = s.desc.ny;
             const bool force = s.desc.body_force[0] != 0.0f || s.desc.body_force[1] != 0.0f;
-            d.bits = (s.desc.periodic & 3) | (force ? 4 : 0) | (s.cur ? 8 : 0);
-            const int chunks = (s.pitch / b->v + b->tx - 1) / b->tx;
-            d.chunks = chunks;
+            // division by the pitch (>= 32): multiplier m and shift l - 1, l = ceil(log2 pitch)
+            int l = 0;
+            while ((1ll << l) < s.pitch) ++l;
+            d.magic = (unsigned)((((uint64_t)1 << 32) * (((uint64_t)1 << l) - (uint64_t)s.pitch)) / (uint64_t)s.pitch + 1);
+            d.bits = (s.desc.periodic & 3) | (force ? 4 : 0) | (s.cur ? 8 : 0) | ((l - 1) << 8);
+            const int per_tile = b->tx * b->ty * b->v;
+            const int ntile_slot = (int)((s.plane + per_tile - 1) / per_tile);
             const D2Q9Params prm = d2q9_params(s.desc);
             d.omega = prm.omega;
             d.fx = prm.fx;
@@ -459,7 +468,7 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
             d.uwx = prm.uwx;
             d.uwy = prm.uwy;
             p.start[p.n] = ntiles;
-            ntiles += chunks * ((s.desc.ny + b->ty - 1) / b->ty);
+            ntiles += ntile_slot;
             ++p.n;
         }
         p.ntiles = ntiles;
@@ -467,10 +476,8 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
             std::vector<TileP> tl;
             tl.reserve((size_t)ntiles);
             for (int k = 0; k < p.n; ++k) {
-                const int bands = (p.d[k].ny + b->ty - 1) / b->ty;
-                for (int band = 0; band < bands; ++band)
-                    for (int xc = 0; xc < p.d[k].chunks; ++xc)
-                        tl.push_back(TileP{k, (unsigned short)band, (unsigned short)xc});
+                const int end = k + 1 < p.n ? p.start[k + 1] : ntiles;
+                for (int j = 0; j < end - p.start[k]; ++j) tl.push_back(TileP{k, (unsigned)j});
             }
             lbm_status st = grow_table(b, (void **)&b->ptiles_d, &b->ptiles_cap, tl.size(), sizeof(TileP), 1024,
                                        "batch: tile table");

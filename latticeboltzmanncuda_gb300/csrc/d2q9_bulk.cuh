@@ -239,7 +239,8 @@ __device__ __forceinline__ void update(const uint16_t *sl, const S *__restrict__
         else
             ld_pack<S, V>(mine + (int64_t)q * plane, out);
     };
-    finish_row<S, V, FORCE, int, 0>(ld, own, dst, x0, nx, plane, periodic, prm, 0);
+    finish_row<S, V, FORCE, int, 0>(ld, own, dst, x0, nx, plane, periodic, prm, 0, ld.e, ld.e, lane == 0, lane == 31,
+                                    true);
 }
 
 template <class S, int V, bool FORCE, int K>

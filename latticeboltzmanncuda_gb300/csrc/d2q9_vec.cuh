@@ -45,8 +45,10 @@ struct RowLoad {
     using LT = typename RawPack<2 * V < 4 ? 4 : 2 * V>::T;
     T q0, q2, q4, a1, a5, a8, b3, b6, b7;  // populations at x0 .. x0+V-1 of rows y (0, 1, 3), y-1 (2, 5, 6), y+1 (4, 7, 8)
     LT links;
-    S e[3];  // lane 0: populations 1, 5, 8 at x0 - 1; lane 31: populations 3, 6, 7 at x0 + V
-    S w[3];  // periodic row, the vector holding the last column: populations 3, 6, 7 at x = 0
+    S e[3];   // lane 0: populations 1, 5, 8 at x0 - 1; lane 31: populations 3, 6, 7 at x0 + V
+              // (flat mapping: the left edge only)
+    S er[3];  // flat mapping: populations 3, 6, 7 at x0 + V
+    S w[3];   // periodic row, the vector holding the last column: populations 3, 6, 7 at x = 0
     I r0, rm, rp;
     int xa;
 };
@@ -114,9 +116,10 @@ __device__ __forceinline__ void load_row(RowLoad<S, V, I> &ld, const S *__restri
 // (bounce-back takes the opposite population of the cell itself; solid cells keep their own).
 template <class S, int V, bool FORCE, class I, int POL, class Own>
 __device__ __forceinline__ void finish_row(const RowLoad<S, V, I> &ld, Own own, S *__restrict__ dst, int x0, int nx,
-                                           I plane, int periodic, const D2Q9Params &prm, uint64_t pol_st) {
+                                           I plane, int periodic, const D2Q9Params &prm, uint64_t pol_st,
+                                           const S (&el)[3], const S (&er)[3], bool left_own, bool right_own,
+                                           bool active) {
     using R = typename Store<S>::R;
-    const int lane = threadIdx.x & 31;
     const I r0 = ld.r0;
     R f[9][V];
     R a1[V], a5[V], a8[V], b3[V], b6[V], b7[V];
@@ -147,15 +150,15 @@ __device__ __forceinline__ void finish_row(const RowLoad<S, V, I> &ld, Own own, 
     R n3 = __shfl_down_sync(0xffffffffu, b3[0], 1);
     R n6 = __shfl_down_sync(0xffffffffu, b6[0], 1);
     R n7 = __shfl_down_sync(0xffffffffu, b7[0], 1);
-    if (lane == 0) {
-        p1 = Store<S>::to(ld.e[0]);
-        p5 = Store<S>::to(ld.e[1]);
-        p8 = Store<S>::to(ld.e[2]);
+    if (left_own) {
+        p1 = Store<S>::to(el[0]);
+        p5 = Store<S>::to(el[1]);
+        p8 = Store<S>::to(el[2]);
     }
-    if (lane == 31) {
-        n3 = Store<S>::to(ld.e[0]);
-        n6 = Store<S>::to(ld.e[1]);
-        n7 = Store<S>::to(ld.e[2]);
+    if (right_own) {
+        n3 = Store<S>::to(er[0]);
+        n6 = Store<S>::to(er[1]);
+        n7 = Store<S>::to(er[2]);
     }
 #pragma unroll
     for (int k = 0; k < V; ++k) {
@@ -233,7 +236,7 @@ __device__ __forceinline__ void finish_row(const RowLoad<S, V, I> &ld, Own own, 
         }
     }
 
-    if (x0 >= nx) return;  // vector entirely in the row padding
+    if (!active || x0 >= nx) return;  // vector entirely in the row padding (or past the end of a flat tile)
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         if (solid_any) {
@@ -258,7 +261,82 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
     // own populations at the clamped xa (equal to x0 for every vector that is stored)
     const S *mine = src + ld.r0 + ld.xa;
     auto own = [&](int q, typename Store<S>::R (&out)[V]) { ld_pack<S, V>(mine + q * plane, out); };
-    finish_row<S, V, FORCE, I, POL>(ld, own, dst, x0, nx, plane, periodic, prm, pol_st);
+    const int lane = threadIdx.x & 31;
+    finish_row<S, V, FORCE, I, POL>(ld, own, dst, x0, nx, plane, periodic, prm, pol_st, ld.e, ld.e, lane == 0,
+                                    lane == 31, true);
+}
+
+// Flat mapping (the batch kernel): the 32 lanes of a warp hold 32 consecutive vectors of the slot's
+// padded cell array [0, pitch * ny), row after row, so a warp may span rows.  The caller gives each
+// lane its own (x0, y) with x0 a multiple of V below pitch (a vector never straddles rows, pitch
+// being a multiple of 32).  A lane takes its x - 1 neighbours from the previous lane unless it starts
+// a row or is lane 0 (left_own: it loads them, wrapped or clamped at x = 0 as above), and its x + V
+// neighbours from the next lane unless it ends a padded row or is lane 31 (right_own).  Lanes past
+// the slot's last vector are given that vector and active = false: they load in bounds, take part
+// in the shuffles and store nothing.  Per cell the arithmetic is that of step_vec, so the results
+// are bit-identical to the row mapping and to the single-domain kernel.
+template <class S, int V, class I>
+__device__ __forceinline__ void load_row_flat(RowLoad<S, V, I> &ld, const S *__restrict__ src,
+                                              const uint16_t *__restrict__ links, int x0, int y, int nx, int ny,
+                                              I pitch, I plane, int periodic, bool left_own, bool right_own) {
+    using T = typename RowLoad<S, V, I>::T;
+    using LT = typename RowLoad<S, V, I>::LT;
+    int ym = y - 1, yp = y + 1;
+    if (ym < 0) ym = (periodic & 2) ? ny - 1 : 0;
+    if (yp >= ny) yp = (periodic & 2) ? 0 : ny - 1;
+    const I r0 = (I)y * pitch, rm = (I)ym * pitch, rp = (I)yp * pitch;
+    ld.r0 = r0;
+    ld.rm = rm;
+    ld.rp = rp;
+    ld.xa = x0;
+    auto at = [&](int q, I r) { return reinterpret_cast<const T *>(src + q * plane + r + x0); };
+    ld.q0 = __ldg(at(0, r0));
+    ld.q2 = __ldg(at(2, rm));
+    ld.q4 = __ldg(at(4, rp));
+    ld.a1 = __ldg(at(1, r0));
+    ld.a5 = __ldg(at(5, rm));
+    ld.a8 = __ldg(at(8, rp));
+    ld.b3 = __ldg(at(3, r0));
+    ld.b6 = __ldg(at(6, rm));
+    ld.b7 = __ldg(at(7, rp));
+    if constexpr (V == 1)
+        ld.links = __ldg(links + r0 + x0);
+    else
+        ld.links = __ldg(reinterpret_cast<const LT *>(links + r0 + x0));
+    if (left_own) {
+        int xm = x0 - 1;
+        if (xm < 0) xm = (periodic & 1) ? nx - 1 : 0;  // unused (bounce-back) when not periodic
+        ld.e[0] = __ldg(src + 1 * plane + r0 + xm);
+        ld.e[1] = __ldg(src + 5 * plane + rm + xm);
+        ld.e[2] = __ldg(src + 8 * plane + rp + xm);
+    }
+    if (right_own) {
+        const int xq = min(x0 + V, (int)pitch - 1);
+        ld.er[0] = __ldg(src + 3 * plane + r0 + xq);
+        ld.er[1] = __ldg(src + 6 * plane + rm + xq);
+        ld.er[2] = __ldg(src + 7 * plane + rp + xq);
+    }
+    const int kl = nx - 1 - x0;
+    if ((periodic & 1) && kl >= 0 && kl < V) {
+        ld.w[0] = __ldg(src + 3 * plane + r0);
+        ld.w[1] = __ldg(src + 6 * plane + rm);
+        ld.w[2] = __ldg(src + 7 * plane + rp);
+    }
+}
+
+template <class S, int V, bool FORCE, class I>
+__device__ __forceinline__ void step_vec_flat(const S *__restrict__ src, S *__restrict__ dst,
+                                              const uint16_t *__restrict__ links, int x0, int y, int nx, int ny,
+                                              I pitch, I plane, int periodic, const D2Q9Params &prm, bool active) {
+    const int lane = threadIdx.x & 31;
+    const bool left_own = lane == 0 || x0 == 0;
+    const bool right_own = lane == 31 || x0 + V == (int)pitch;
+    RowLoad<S, V, I> ld;
+    load_row_flat<S, V, I>(ld, src, links, x0, y, nx, ny, pitch, plane, periodic, left_own, right_own);
+    const S *mine = src + ld.r0 + x0;
+    auto own = [&](int q, typename Store<S>::R (&out)[V]) { ld_pack<S, V>(mine + q * plane, out); };
+    finish_row<S, V, FORCE, I, 0>(ld, own, dst, x0, nx, plane, periodic, prm, 0, ld.e, ld.er, left_own, right_own,
+                                  active);
 }
 
 }  // namespace d2q9

@@ -284,26 +284,26 @@ def test_bulk_protocol_simulation_catches_a_missing_release():
 
 # ------------------------------------------------------------------ batch parameter-block path
 # csrc/batch.cu: slots are one allocation each (buffer A, buffer B: 9 planes of pitch x ny elements
-# each; then pitch x ny uint16 link words; then flags and the fluid count), tiles are ordered slot
-# by slot, row bands ascending, column chunks inside a band.  16-bit blocks read (slot, band,
-# chunk) from a tile record, FP32 blocks binary-search the slots' first tiles.
+# each; then pitch x ny uint16 link words; then flags and the fluid count).  Tiles are flat: tile j
+# of a slot covers the tx * ty * V consecutive cells from j * tx * ty * V of the slot's padded cell
+# array, thread k of the block the vector at j * tx * ty * V + k * V (d2q9_vec.cuh: step_vec_flat).
+# 16-bit blocks read (slot, tile) from a tile record, FP32 blocks binary-search the slots' first
+# tiles.
 
 
 def batch_tiles(shapes, V, tx, ty):
-    """The tile list of rebuild(): (slot, band, xchunk) per tile, and the slots' first tiles."""
+    """The tile list of rebuild(): (slot, tile within the slot) per tile, and the slots' first tiles."""
     tiles, start = [], []
+    per_tile = tx * ty * V
     for k, (nx, ny) in enumerate(shapes):
         pitch = (nx + 31) // 32 * 32
-        chunks = (pitch // V + tx - 1) // tx
         start.append(len(tiles))
-        for band in range((ny + ty - 1) // ty):
-            for xc in range(chunks):
-                tiles.append((k, band, xc))
+        tiles += [(k, j) for j in range((pitch * ny + per_tile - 1) // per_tile)]
     return tiles, start
 
 
-def search_tile(start, t, chunks):
-    """batch_tile_p's binary search and division for tile t."""
+def search_tile(start, t):
+    """batch_tile_p's binary search for tile t: (slot, tile within the slot)."""
     lo, hi = 0, len(start) - 1
     while lo < hi:
         mid = (lo + hi + 1) >> 1
@@ -311,8 +311,71 @@ def search_tile(start, t, chunks):
             lo = mid
         else:
             hi = mid - 1
-    i = t - start[lo]
-    return lo, i // chunks[lo], i - (i // chunks[lo]) * chunks[lo]
+    return lo, t - start[lo]
+
+
+def pitch_division(pitch):
+    """(multiplier, shift) of batch_tile_p's division by the pitch, as rebuild() computes them."""
+    l = 0
+    while (1 << l) < pitch:
+        l += 1
+    return ((1 << 32) * ((1 << l) - pitch) // pitch + 1) & 0xFFFFFFFF, l - 1
+
+
+def divide(i, magic, shift):
+    """batch_tile_p's multiply-high division (i: int or uint64 array below 2^31)"""
+    th = (np.uint64(magic) * np.asarray(i, np.uint64)) >> np.uint64(32)
+    return (th + ((np.asarray(i, np.uint64) - th) >> np.uint64(1))) >> np.uint64(shift)
+
+
+def flat_thread_offsets(nx, ny, pitch, V, x0, y, lane, periodic, active):
+    """(population offsets, link offsets) one lane of step_vec_flat touches (element indices)."""
+    plane = pitch * ny
+    ym = np.where(y - 1 < 0, ny - 1 if periodic & 2 else 0, y - 1)
+    yp = np.where(y + 1 >= ny, 0 if periodic & 2 else ny - 1, y + 1)
+    r0, rm, rp = y * pitch, ym * pitch, yp * pitch
+    pop, lnk = [], []
+    for q, r in {0: r0, 2: rm, 4: rp, 1: r0, 5: rm, 8: rp, 3: r0, 6: rm, 7: rp}.items():
+        for k in range(V):
+            pop.append(q * plane + r + x0 + k)
+            pop.append(q * plane + r0 + x0 + k)  # own populations (bounce-back, solid copies)
+    for k in range(V):
+        lnk.append(r0 + x0 + k)
+    left = (lane == 0) | (x0 == 0)
+    right = (lane == 31) | (x0 + V == pitch)
+    xm = np.where(x0 - 1 < 0, nx - 1 if periodic & 1 else 0, x0 - 1)
+    xq = np.minimum(x0 + V, pitch - 1)
+    for q, r in ((1, r0), (5, rm), (8, rp)):
+        pop.append(np.where(left, q * plane + r + xm, 0))
+    for q, r in ((3, r0), (6, rm), (7, rp)):
+        pop.append(np.where(right, q * plane + r + xq, 0))
+    kl = nx - 1 - x0
+    mp = bool(periodic & 1) & (kl >= 0) & (kl < V)
+    for q, r in ((3, r0), (6, rm), (7, rp)):
+        pop.append(np.where(mp, q * plane + r, 0))
+    st = active & (x0 < nx)
+    for q in range(9):
+        for k in range(V):
+            pop.append(np.where(st, q * plane + r0 + x0 + k, 0))
+    return np.stack(pop), np.stack(lnk)
+
+
+def flat_lanes(nx, ny, V, tx, ty, j):
+    """x0, y, lane, active of the lanes of tile j (an int, or an array of tiles: their lanes one tile
+    after another) that run (warps past the slot's end return)."""
+    pitch = (nx + 31) // 32 * 32
+    plane = pitch * ny
+    magic, shift = pitch_division(pitch)
+    k = np.tile(np.arange(tx * ty), np.size(j))
+    first = np.repeat(np.asarray(j).reshape(-1) * tx * ty * V, tx * ty)
+    runs = first + (k & ~31) * V < plane
+    k, first = k[runs], first[runs]
+    i = first + k * V
+    active = i < plane
+    i = np.where(active, i, plane - V)
+    y = divide(i, magic, shift).astype(np.int64)
+    assert np.array_equal(y, i // pitch)
+    return i - y * pitch, y, k % 32, active
 
 
 @pytest.mark.parametrize("seed", range(3))
@@ -320,39 +383,51 @@ def test_batch_parameter_path_tiles_and_addresses(seed):
     rng = np.random.default_rng(seed)
     n = int(rng.integers(1, 30))
     shapes = [(int(rng.integers(1, 700)), int(rng.integers(1, 300))) for _ in range(n)]
-    for elem, V, tx, ty in ((2, 4, 32, 4), (2, 8, 32, 2), (2, 2, 64, 1), (4, 4, 32, 2), (4, 2, 128, 2)):
+    shapes += [(1, 1), (32, 1), (33, 3), (64, 5)]
+    for elem, V, tx, ty in ((2, 4, 32, 4), (2, 8, 32, 2), (2, 2, 64, 1), (4, 4, 32, 2), (4, 2, 128, 2), (2, 8, 256, 1)):
         tiles, start = batch_tiles(shapes, V, tx, ty)
-        chunks = [((nx + 31) // 32 * 32 // V + tx - 1) // tx for nx, _ in shapes]
-        # the binary search (FP32) finds every tile's record (16-bit), and the fields fit 16 bits
+        # the binary search (FP32) finds every tile's record (16-bit)
         for t, rec in enumerate(tiles):
-            assert search_tile(start, t, chunks) == rec
-            assert rec[1] <= 65535 and rec[2] <= 65535
-        # every cell of every slot is covered by exactly one (tile, thread row, lane, element)
+            assert search_tile(start, t) == rec
         for k, (nx, ny) in enumerate(shapes):
             pitch = (nx + 31) // 32 * 32
             plane = pitch * ny
             pop = 9 * plane * elem
             alloc = 2 * pop + plane * 2 + ((nx * ny + 7) // 8 * 8 + 8)
             seen = np.zeros((ny, pitch), int)
-            for (kk, band, xc) in (r for r in tiles if r[0] == k):
-                for ti in range(ty):
-                    y = band * ty + ti
-                    if y >= ny:
-                        continue
-                    x0 = (xc * tx + np.arange(tx)) * V
-                    xa = np.minimum(x0, pitch - V)
-                    for cur in (0, 1):
-                        src = cur * 9 * plane  # elements from the base
-                        dst = (cur ^ 1) * 9 * plane
-                        for base in (src, dst):
-                            offs = base + 8 * plane + y * pitch + xa + V - 1  # the highest plane and element
-                            assert offs.max() * elem < pop * (2 if base else 1)
-                    links = 18 * plane * elem  # byte offset of the link words
-                    assert links == 2 * pop and links + (y * pitch + xa.max() + V) * 2 <= alloc
-                    act = x0 < nx
-                    for x in x0[act]:
-                        seen[y, x:x + V] += 1
-            assert (seen[:, :nx] == 1).all()
+            js = np.array([j for (kk, j) in tiles if kk == k])
+            for j in (js,):
+                x0, y, lane, active = flat_lanes(nx, ny, V, tx, ty, j)
+                assert (x0 % V == 0).all() and (x0 >= 0).all() and (x0 + V <= pitch).all()
+                for periodic in range(4):
+                    offs, lnk = flat_thread_offsets(nx, ny, pitch, V, x0, y, lane, periodic, active)
+                    assert offs.min() >= 0 and offs.max() < 9 * plane, (nx, ny, V, tx, ty, periodic)
+                    assert lnk.min() >= 0 and lnk.max() < plane
+                # byte offsets from the slot's base: both buffers and the link words lie in the allocation
+                assert (9 * plane + 9 * plane) * elem == 2 * pop
+                assert 2 * pop + (int(lnk.max()) + 1) * 2 <= alloc
+                st = active & (x0 < nx)
+                for e in range(V):
+                    np.add.at(seen, (y[st], x0[st] + e), 1)
+            # every cell of every slot is stored by exactly one lane
+            assert (seen[:, :nx] == 1).all(), (nx, ny, V, tx, ty)
+
+
+def test_flat_lane_edges_take_their_own_neighbours():
+    """A lane that starts a padded row (or is lane 0) loads its x - 1 neighbours, a lane that ends one
+    (or is lane 31) its x + V neighbours; every other lane's neighbours are the adjacent lanes' own
+    vectors in the same row, so the shuffles never carry a value across a row boundary."""
+    for nx, ny, V, tx, ty in ((40, 9, 4, 32, 4), (31, 17, 8, 32, 2), (100, 3, 2, 64, 1), (1, 70, 4, 32, 1)):
+        pitch = (nx + 31) // 32 * 32
+        for j in range((pitch * ny + tx * ty * V - 1) // (tx * ty * V)):
+            x0, y, lane, active = flat_lanes(nx, ny, V, tx, ty, j)
+            left = (lane == 0) | (x0 == 0)
+            right = (lane == 31) | (x0 + V == pitch)
+            for a in range(len(x0)):
+                if not left[a] and active[a]:  # lanes past the slot's end store nothing
+                    assert lane[a - 1] == lane[a] - 1 and y[a - 1] == y[a] and x0[a - 1] == x0[a] - V
+                if not right[a] and active[a]:
+                    assert lane[a + 1] == lane[a] + 1 and y[a + 1] == y[a] and x0[a + 1] == x0[a] + V
 
 
 def test_invariant_division_formula():
