@@ -228,6 +228,13 @@ LBM_API lbm_status lbm_set_launch(lbm_ctx *ctx, int32_t cells_per_thread, int32_
 /* D2Q9: visit rows in alternating order on successive steps (default 1), so each step starts on
  * the rows that the previous step wrote last and that are still in L2. */
 LBM_API lbm_status lbm_set_sweep_alternation(lbm_ctx *ctx, int32_t enabled);
+/* D2Q9 bulk-copy pipeline (cells_per_thread 0): every wait of its blocks gives up after wait_ns
+ * nanoseconds (default 1e9; 1e3..1e10).  Diagnostic: skip_task >= 0 makes the copying warp leave
+ * out the copies of that (strip, row) task in every launch, so the wait for them gives up: the next
+ * call that synchronises the context returns LBM_ERR_TIMEOUT and the populations of the steps since
+ * the previous synchronisation are not valid (reload them).  skip_task = -1 (the default) copies
+ * every task.  No counterpart in the reference, whose kernels have no waits. */
+LBM_API lbm_status lbm_set_pipeline_wait(lbm_ctx *ctx, int64_t wait_ns, int32_t skip_task);
 
 /* ---------------------------------------------------------------- results */
 /* Density and velocity per cell (host arrays of cells floats, any may be NULL).

@@ -202,6 +202,11 @@ class Lattice:
     def set_sweep_alternation(self, enabled):
         self._call("lbm_set_sweep_alternation", int(bool(enabled)))
 
+    def set_pipeline_wait(self, wait_ns=1_000_000_000, skip_task=-1):
+        """Bulk-copy pipeline: the limit of its waits, and (diagnostic) a task whose copies it leaves
+        out so that the wait for them gives up (the next synchronisation raises LBM_ERR_TIMEOUT)."""
+        self._call("lbm_set_pipeline_wait", int(wait_ns), int(skip_task))
+
     # ------------------------------------------------------------------ results
     def moments(self, out=None):
         """(rho, ux, uy) for D2Q9, (rho, ux, uy, uz) for D3Q27_REF; `out` may give float32 arrays

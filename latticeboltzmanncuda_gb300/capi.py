@@ -129,6 +129,7 @@ SIGNATURES = [
     ("lbm_autotune", _S, [_P, _I32]),
     ("lbm_set_launch", _S, [_P, _I32, _I32, _I32, _I32]),
     ("lbm_set_sweep_alternation", _S, [_P, _I32]),
+    ("lbm_set_pipeline_wait", _S, [_P, _I64, _I32]),
     ("lbm_moments", _S, [_P, _P, _P, _P, _P]),
     ("lbm_conservation", _S, [_P, _P]),
     ("lbm_batch_create", _S, [_I32, _I32, _P, _P]),

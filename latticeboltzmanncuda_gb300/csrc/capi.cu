@@ -690,6 +690,16 @@ LBM_API lbm_status lbm_set_sweep_alternation(lbm_ctx *ctx, int32_t enabled) {
     return LBM_OK;
 }
 
+LBM_API lbm_status lbm_set_pipeline_wait(lbm_ctx *ctx, int64_t wait_ns, int32_t skip_task) {
+    CHECK_CTX(ctx);
+    if (wait_ns < 1000 || wait_ns > 10000000000ll)
+        return fail(ctx, LBM_ERR_INVALID, "lbm_set_pipeline_wait: wait_ns must be in [1e3, 1e10]");
+    if (skip_task < -1) return fail(ctx, LBM_ERR_INVALID, "lbm_set_pipeline_wait: skip_task must be >= -1");
+    ctx->pipe_wait_ns = (unsigned long long)wait_ns;
+    ctx->pipe_skip_task = skip_task;
+    return LBM_OK;
+}
+
 LBM_API lbm_status lbm_apply(lbm_ctx *ctx, int32_t op) {
     CHECK_CTX(ctx);
     if (ctx->desc.mode != LBM_D3Q27_REF) return fail(ctx, LBM_ERR_UNSUPPORTED, "lbm_apply is D3Q27_REF only");

@@ -129,9 +129,11 @@ __global__ void __launch_bounds__(256, vec_min_blocks(V)) step_vec_kernel(const 
 template <class S, int V, bool FORCE, int K, int MINB>
 __global__ void __launch_bounds__(d2q9::bulk::threads<V>(), MINB)
     bulk_kernel(const S *__restrict__ src, S *__restrict__ dst, const uint16_t *__restrict__ links, int nx, int ny,
-                int pitch, int plane, int periodic, D2Q9Params prm, int reverse, unsigned *status) {
+                int pitch, int plane, int periodic, D2Q9Params prm, int reverse, unsigned *status,
+                unsigned long long wait_ns, int skip_task) {
     extern __shared__ __align__(128) unsigned char smem[];
-    d2q9::bulk::pipeline<S, V, FORCE, K>(smem, src, dst, links, nx, ny, pitch, plane, periodic, prm, reverse, status);
+    d2q9::bulk::pipeline<S, V, FORCE, K>(smem, src, dst, links, nx, ny, pitch, plane, periodic, prm, reverse, status,
+                                         wait_ns, skip_task);
 }
 
 // Resident blocks of a kernel per SM times the SMs of `device` (cached per kernel and device).
@@ -175,7 +177,8 @@ cudaError_t launch_bulk(lbm_ctx *ctx, const S *src, S *dst, int reverse) {
     const int grid = std::min(ntasks, resident);
     ctx->pipe_used = true;
     kern<<<grid, threads, bytes, ctx->stream>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic,
-                                                d2q9_params(d), reverse, ctx->pipe_status_d);
+                                                d2q9_params(d), reverse, ctx->pipe_status_d, ctx->pipe_wait_ns,
+                                                ctx->pipe_skip_task);
     return cudaGetLastError();
 }
 

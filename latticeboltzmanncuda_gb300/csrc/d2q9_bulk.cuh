@@ -30,9 +30,11 @@
 // released the position after updating its row.  Lanes 0 and 1 refill a slot only once its previous
 // position has been released, so the producer runs up to K - 1 rows ahead of the consumers.
 //
-// Every wait is bounded (WAIT_NS of wall time, or an abort raised by another warp of the block):
-// on a timeout the block sets PIPE_TIMEOUT in *status, the consumers stop, and lane 0 stops issuing
-// and waits (bounded) for the copies it has issued before the block exits.
+// Every wait is bounded (wait_ns of wall time, 1 s unless the host sets another limit, or an abort
+// raised by another warp of the block): on a timeout the block sets PIPE_TIMEOUT in *status, the
+// consumers stop, and lane 0 stops issuing and waits (bounded) for the copies it has issued before
+// the block exits.  For testing that path the host can name a task whose copies lane 0 leaves out
+// (skip_task >= 0): the consumers' wait for that slot runs out, nothing faults and nothing hangs.
 #pragma once
 
 #include "d2q9_vec.cuh"
@@ -57,7 +59,6 @@ constexpr int WRAP = 9 * SEG + W;      // wrapped columns: populations 1, 5, 8 a
                                        // y - 1, y + 1, then populations 3, 6, 7 at x = 0 of those rows
 constexpr int SLOT = 9 * SEG + W + 8;  // 16-bit elements per slot
 constexpr unsigned PIPE_TIMEOUT = 1u;  // status bit: a bounded wait gave up
-constexpr unsigned long long WAIT_NS = 1000000000ull;
 static_assert((SLOT * 2) % 16 == 0 && (SEG * 2) % 16 == 0, "slot geometry keeps 16-byte alignment");
 
 // ring of K slots, then K full and K empty barriers, then the abort word
@@ -94,15 +95,16 @@ __device__ __forceinline__ unsigned long long now_ns() {
     return t;
 }
 
-// Wait for the phase of parity `parity` of barrier b: false after WAIT_NS or, when abort is not
+// Wait for the phase of parity `parity` of barrier b: false after limit_ns or, when abort is not
 // null, once another warp has raised it.
-__device__ __forceinline__ bool wait(unsigned long long *b, unsigned parity, const volatile int *abort) {
+__device__ __forceinline__ bool wait(unsigned long long *b, unsigned parity, const volatile int *abort,
+                                     unsigned long long limit_ns) {
     if (mbar_try_wait(b, parity)) return true;
     const unsigned long long t0 = now_ns();
     for (;;) {
         if (mbar_try_wait(b, parity)) return true;
         if (abort && *abort) return false;
-        if (now_ns() - t0 > WAIT_NS) return false;
+        if (now_ns() - t0 > limit_ns) return false;
     }
 }
 
@@ -246,7 +248,8 @@ __device__ __forceinline__ void update(const uint16_t *sl, const S *__restrict__
 template <class S, int V, bool FORCE, int K>
 __device__ __forceinline__ void pipeline(unsigned char *smem, const S *__restrict__ src, S *__restrict__ dst,
                                          const uint16_t *__restrict__ links, int nx, int ny, int pitch, int plane,
-                                         int periodic, const D2Q9Params &prm, int reverse, unsigned *status) {
+                                         int periodic, const D2Q9Params &prm, int reverse, unsigned *status,
+                                         unsigned long long wait_ns, int skip_task) {
     static_assert(sizeof(S) == 2, "the bulk-copy pipeline is for 16-bit storage");
     static_assert(K >= 2, "a ring of at least two slots");
     uint16_t *ring = reinterpret_cast<uint16_t *>(smem);
@@ -272,26 +275,32 @@ __device__ __forceinline__ void pipeline(unsigned char *smem, const S *__restric
         if (lane > 1 || (lane == 1 && !wrap_x)) return;
         unsigned pos = 0;
         bool ok = true;
+        int skipped = -1;  // position whose copies were left out (skip_task)
         for (int i = blockIdx.x; i < ntasks; i += gridDim.x, ++pos) {
             const unsigned s = pos % K;
-            if (pos >= (unsigned)K && !wait(&empty[s], ((pos / K) - 1) & 1u, abort)) {
+            if (pos >= (unsigned)K && !wait(&empty[s], ((pos / K) - 1) & 1u, abort, wait_ns)) {
                 ok = false;
                 break;
             }
             int x0, y;
             task_of(i, ntasks, nstrips, reverse, x0, y);
             uint16_t *slot = ring + (size_t)s * SLOT;
-            if (lane == 0)
-                stage_task<S>(slot, &full[s], src, links, y, x0, ny, pitch, plane, periodic);
-            else
+            if (lane == 0) {
+                if (i == skip_task)
+                    skipped = (int)pos;  // no copy and no arrival: the consumers' wait runs out
+                else
+                    stage_task<S>(slot, &full[s], src, links, y, x0, ny, pitch, plane, periodic);
+            } else {
                 stage_wrap<S>(slot, &full[s], src, y, x0, nx, ny, pitch, plane, periodic);
+            }
         }
         if (!ok) {
             *abort = 1;
             atomicOr(status, PIPE_TIMEOUT);
             // the copies lane 0 issued land before the block's shared memory goes away
             if (lane == 0)
-                for (unsigned q = pos > (unsigned)K ? pos - K : 0u; q < pos; ++q) wait(&full[q % K], (q / K) & 1u, nullptr);
+                for (unsigned q = pos > (unsigned)K ? pos - K : 0u; q < pos; ++q)
+                    if ((int)q != skipped) wait(&full[q % K], (q / K) & 1u, nullptr, wait_ns);
         }
         return;
     }
@@ -301,7 +310,7 @@ __device__ __forceinline__ void pipeline(unsigned char *smem, const S *__restric
     unsigned pos = 0;
     for (int i = blockIdx.x; i < ntasks; i += gridDim.x, ++pos) {
         const unsigned s = pos % K;
-        if (!__all_sync(0xffffffffu, wait(&full[s], (pos / K) & 1u, abort))) {
+        if (!__all_sync(0xffffffffu, wait(&full[s], (pos / K) & 1u, abort, wait_ns))) {
             if (lane == 0) {
                 *abort = 1;
                 atomicOr(status, PIPE_TIMEOUT);

@@ -119,6 +119,8 @@ struct lbm_ctx {
     int l2_policy = 0;             // vector path: L2 eviction hints (0 none, 1 ld first/st last, 2 ld first)
     unsigned *pipe_status_d = nullptr;  // D2Q9 bulk-copy pipeline: status bits set by a block whose wait gave up
     bool pipe_used = false;             // the pipeline ran since the status was last read
+    unsigned long long pipe_wait_ns = 1000000000ull;  // limit of every pipeline wait (lbm_set_pipeline_wait)
+    int pipe_skip_task = -1;            // test: task whose copies the producer leaves out (-1: none)
     bool tuned = false;
     bool alternate_sweeps = true;  // visit rows in alternating order on successive steps
     unsigned sweep = 0;

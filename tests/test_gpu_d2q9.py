@@ -359,3 +359,45 @@ def test_domain_past_32bit_indexing_reproduces_its_tile(dtype):
         assert np.array_equal(g4, np.broadcast_to(w[None, :, None, :], g4.shape))
     for c, w in zip(cons[:3], want_cons[:3]):
         assert abs(c - ntiles * w) <= 1e-9 * max(1.0, abs(ntiles * w))
+
+
+@pytest.mark.parametrize("periodic", [0, 1])
+def test_bulk_pipeline_wait_gives_up_and_the_context_recovers(periodic):
+    """The bulk-copy pipeline's bounded waits, exercised without any fault: with a 1 ms limit and the
+    copies of one task left out, the consumer warps' wait for that slot runs out, the block records
+    the timeout and exits, and the next synchronisation returns LBM_ERR_TIMEOUT.  The context stays
+    usable: with the defaults back and the populations reloaded, its steps equal, bit for bit, the
+    vector kernel's on a fresh context."""
+    nx, ny = 777, 70
+    flags, _ = lbm.gen_channel(nx, ny, 9, 3.0, 9.0, 11)
+    f0 = random_state(nx, ny, 17)
+    kw = dict(dtype="f16s", tau=0.61, periodic=periodic, body_force=(1e-5, 0, 0))
+    with lbm.Lattice(nx, ny, **kw) as L:
+        L.set_flags(flags)
+        L.load_populations(f0)
+        L.set_launch(0, 160, 1, 0)
+        L.set_pipeline_wait(1_000_000, skip_task=5)
+        L.step(3)
+        with pytest.raises(lbm.LBMError) as err:
+            L.synchronize()
+        assert err.value.status == lbm.capi.ERR_TIMEOUT and "bounded wait" in str(err.value)
+        L.synchronize()  # the status was taken: nothing left to report
+        L.set_pipeline_wait()
+        L.load_populations(f0)
+        L.step(23)
+        got = L.retrieve_populations()
+    with lbm.Lattice(nx, ny, **kw) as R:
+        R.set_flags(flags)
+        R.load_populations(f0)
+        R.set_launch(8, 64, 2, 0)
+        R.step(23)
+        want = R.retrieve_populations()
+    assert np.array_equal(got, want)
+
+
+def test_pipeline_wait_arguments_checked():
+    with lbm.Lattice(64, 8, dtype="f16s") as L:
+        with pytest.raises(lbm.LBMError):
+            L.set_pipeline_wait(10)  # below 1 microsecond
+        with pytest.raises(lbm.LBMError):
+            L.set_pipeline_wait(1_000_000, skip_task=-2)
