@@ -770,8 +770,8 @@ def d3q27_case(n):
 def run_d3q27(args):
     """The reference-compatible D3Q27 step (stream, reflect, collide, flow, with the reflection
     force accumulated as the reference CLI does) on n^3 through the library: MLUPS and the HBM
-    roofline at 216 algorithmic bytes per cell update, for the float-float equilibrium (default)
-    and for the FP64 expression."""
+    roofline at 216 algorithmic bytes per cell update, for the float-float equilibrium (default, the
+    reference's FP64 value bit for bit), the FP64 expression, and the FP32 equilibrium."""
     import torch
     import latticeboltzmanncuda_gb300 as lbm
 
@@ -780,29 +780,36 @@ def run_d3q27(args):
     cells = n ** 3
     stream = torch.cuda.Stream()
     res = {}
-    for fp64 in (False, True):
+    for mode in ("float_float", "fp64", "fp32"):
         with lbm.Lattice(n, n, n, mode="d3q27_ref", tau=0.8, order=lbm.ORDER_CLI, stream=stream.cuda_stream) as L:
-            L.set_equilibrium_evaluation(fp64)
+            L.set_equilibrium_evaluation(mode)
             L.set_flags(flags)
             L.set_reflection_tables(cells_t, recs)
             L.set_flow(plane, induced)
             L.load_populations(f)
             L.set_force((0, 0, 0), True)
             L.step(args.warmup)
-            t = _timed(stream, lambda: L.step(steps))
-            res[fp64] = (cells * steps / t / 1e6, L.retrieve_populations())
-    mlups = res[False][0]
+            with ClockSampler(0) as clk:
+                t = _timed(stream, lambda: L.step(steps))
+            res[mode] = (cells * steps / t / 1e6, L.retrieve_populations(), clk.summary())
     peak, kind = peaks()
-    achieved = mlups * 216 / 1000
-    line = {"metric": "MLUPS", "workload": "d3q27", "value": round(mlups, 1), "unit": "MLUPS", "steps": steps,
+
+    def roof(mlups):
+        return {"bound": "hbm", "achieved": round(mlups * 216 / 1000, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(mlups * 216 / 1000 / peak, 4), "peak_kind": kind, "bytes_per_update": 216}
+
+    ff, f64, f32 = res["float_float"], res["fp64"], res["fp32"]
+    scale = float(np.max(np.abs(ff[1])))
+    line = {"metric": "MLUPS", "workload": "d3q27", "value": round(ff[0], 1), "unit": "MLUPS", "steps": steps,
             "higher_is_better": True, "dtype": "f32 (equilibrium as the reference's FP64 value)", "data": "synthetic",
             "config": {"workload": f"D3Q27 reference step {n}^3, order stream-reflect-collide-flow with force, tau 0.8, "
                                    f"sphere model r = n/6 ({len(cells_t)} reflecting cells), source plane x = 0",
                        "cells": cells},
-            "fp64_equilibrium": {"mlups": round(res[True][0], 1),
-                                 "bitwise_equal": bool(np.array_equal(res[False][1], res[True][1]))},
-            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "peak_kind": kind, "bytes_per_update": 216}}
+            "roofline": roof(ff[0]), "clocks": ff[2],
+            "fp64_equilibrium": {"mlups": round(f64[0], 1), "bitwise_equal": bool(np.array_equal(ff[1], f64[1])),
+                                 "roofline": roof(f64[0])},
+            "fp32_equilibrium": {"mlups": round(f32[0], 1), "roofline": roof(f32[0]), "clocks": f32[2],
+                                 "max_abs_diff_rel": float(f"{np.max(np.abs(f32[1] - ff[1])) / scale:.3e}")}}
     print(json.dumps(line), flush=True)
     return 0
 

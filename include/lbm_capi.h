@@ -181,12 +181,15 @@ LBM_API lbm_status lbm_step(lbm_ctx *ctx, int32_t nsteps);
 /* D3Q27_REF: one separate pass (LBM_OP_*), as the reference's Lattice::simulate* methods. */
 LBM_API lbm_status lbm_apply(lbm_ctx *ctx, int32_t op);
 /* D3Q27_REF equilibrium evaluation.  The reference evaluates eq_i in FP64 and rounds it to FP32
- * (SimCalcFuncs.cu:122-155).  Both modes give that value bit for bit:
+ * (SimCalcFuncs.cu:122-155).  The first two modes give that value bit for bit:
  *   LBM_EQ_FLOAT_FLOAT (default)  float-float arithmetic with a proven error bound, falling back to
  *                                 the FP64 expression when the bound cannot decide the FP32 rounding
  *   LBM_EQ_FP64                   the FP64 expression for every direction (GB300's FP64 rate bounds
- *                                 the step) */
-enum { LBM_EQ_FLOAT_FLOAT = 0, LBM_EQ_FP64 = 1 };
+ *                                 the step)
+ *   LBM_EQ_FP32                   the same expression in FP32 (a few ulps from the FP64 value; the
+ *                                 populations stay within 1e-5 relative of the reference's), for
+ *                                 speed.  Cells next to reflecting cells keep the FP64 expression. */
+enum { LBM_EQ_FLOAT_FLOAT = 0, LBM_EQ_FP64 = 1, LBM_EQ_FP32 = 2 };
 LBM_API lbm_status lbm_set_equilibrium_evaluation(lbm_ctx *ctx, int32_t mode);
 /* Diagnostic: both evaluations on `samples` pseudo-random (rho, u) draws (|u| up to 2) x the 27
  * directions on `device`; out[0] = float-float results accepted by their bound that differ from
@@ -245,6 +248,20 @@ LBM_API lbm_status lbm_moments(lbm_ctx *ctx, float *host_rho, float *host_ux, fl
                                float *host_uz);
 /* FP64 sums over non-solid cells of the stored populations: mass, momentum x, y, z. */
 LBM_API lbm_status lbm_conservation(lbm_ctx *ctx, double host_out[4]);
+
+/* ---------------------------------------------------------------- checkpoint and resume */
+/* No counterpart in the reference, whose only host snapshot is Lattice::retrieve_data / load_data
+ * (Lattice.cpp:73-113, the populations alone).  lbm_save writes the context's state to a file: the
+ * descriptor (size, storage type, tau, force, wall velocity, periodicity, step order, force mode),
+ * the step count, the cell flags, the current populations in their storage type and device layout
+ * (so a resumed run continues bit for bit), and for D3Q27_REF the reflection tables, the flow
+ * source, the accumulated force and the equilibrium evaluation.  lbm_load restores it into a
+ * context of the same mode, storage type and size (the other descriptor fields are taken from the
+ * file); lbm_checkpoint_desc reads a file's descriptor, to create such a context.  The file is
+ * written to path + ".tmp" and renamed; a checksum guards the payload.  Host byte order. */
+LBM_API lbm_status lbm_save(lbm_ctx *ctx, const char *path);
+LBM_API lbm_status lbm_load(lbm_ctx *ctx, const char *path);
+LBM_API lbm_status lbm_checkpoint_desc(const char *path, lbm_desc *out);
 
 /* ---------------------------------------------------------------- batched domains */
 /* Many independent D2Q9 domains ("slots": own size, tau, force, wall velocity, periodicity and

@@ -176,9 +176,12 @@ class Lattice:
     def apply(self, op):
         self._call("lbm_apply", int(op))
 
-    def set_equilibrium_evaluation(self, fp64):
-        """D3Q27_REF: False = float-float with FP64 fallback (default), True = FP64 throughout."""
-        self._call("lbm_set_equilibrium_evaluation", 1 if fp64 else 0)
+    def set_equilibrium_evaluation(self, mode):
+        """D3Q27_REF: "float_float" (or False; the default, float-float with FP64 fallback, bit for bit
+        the reference's FP64 value), "fp64" (or True; FP64 throughout), "fp32" (FP32 throughout)."""
+        modes = {"float_float": capi.EQ_FLOAT_FLOAT, "fp64": capi.EQ_FP64, "fp32": capi.EQ_FP32,
+                 False: capi.EQ_FLOAT_FLOAT, True: capi.EQ_FP64}
+        self._call("lbm_set_equilibrium_evaluation", modes[mode] if mode in modes else int(mode))
 
     def set_order(self, order):
         """D3Q27_REF: step order of later step() calls (ORDER_STREAM_COLLIDE or ORDER_CLI)."""
@@ -206,6 +209,27 @@ class Lattice:
         """Bulk-copy pipeline: the limit of its waits, and (diagnostic) a task whose copies it leaves
         out so that the wait for them gives up (the next synchronisation raises LBM_ERR_TIMEOUT)."""
         self._call("lbm_set_pipeline_wait", int(wait_ns), int(skip_task))
+
+    # ------------------------------------------------------------------ checkpoint
+    def save(self, path):
+        """Write the context's state to `path` (lbm_save); load() resumes it bit for bit."""
+        self._call("lbm_save", str(path).encode())
+
+    def load(self, path):
+        """Restore a checkpoint written by save() into this context (same mode, storage and size)."""
+        self._call("lbm_load", str(path).encode())
+
+    @classmethod
+    def from_checkpoint(cls, path, device=0, stream=None):
+        """A context created from a checkpoint's descriptor with its state loaded."""
+        d = capi.Desc()
+        check(capi.lib().lbm_checkpoint_desc(str(path).encode(), ctypes.byref(d)))
+        names = {v: k for k, v in capi.MODES.items()}
+        L = cls(d.nx, d.ny, d.nz, mode=names[d.mode], dtype=d.dtype, tau=d.tau, periodic=d.periodic,
+                body_force=tuple(d.body_force), wall_velocity=tuple(d.wall_velocity), order=d.order,
+                force_mode=d.force_mode, device=device, stream=stream)
+        L.load(path)
+        return L
 
     # ------------------------------------------------------------------ results
     def moments(self, out=None):

@@ -28,7 +28,7 @@ CLI = os.path.join(PKG, "bin", "LatticeBoltzmannCuda")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["common.cu", "capi.cu", "d2q9.cu", "d3q27.cu", "geometry.cpp", "mesh.cpp", "noalloc.cu", "batch.cu",
-           "server.cpp"]
+           "server.cpp", "checkpoint.cpp"]
 
 
 def nvcc() -> str:

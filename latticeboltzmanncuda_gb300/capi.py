@@ -20,7 +20,7 @@ F32, F16S, BF16S, F64 = 0, 1, 2, 3
 FLUID, WALL, MOVING_WALL = 0, 1, 2
 INTERNAL, REFLECTED, SOURCE = 1, 2, 4
 ORDER_STREAM_COLLIDE, ORDER_CLI = 0, 1
-EQ_FLOAT_FLOAT, EQ_FP64 = 0, 1
+EQ_FLOAT_FLOAT, EQ_FP64, EQ_FP32 = 0, 1, 2
 OP_STREAM, OP_REFLECT, OP_COLLIDE, OP_FLOW = 1, 2, 4, 8
 FORCE_REFERENCE, FORCE_MOMENTUM_EXCHANGE = 0, 1
 NOALLOC_MAX_ROWS = 32768  # LBM_NOALLOC_MAX_ROWS
@@ -130,6 +130,9 @@ SIGNATURES = [
     ("lbm_set_launch", _S, [_P, _I32, _I32, _I32, _I32]),
     ("lbm_set_sweep_alternation", _S, [_P, _I32]),
     ("lbm_set_pipeline_wait", _S, [_P, _I64, _I32]),
+    ("lbm_save", _S, [_P, ctypes.c_char_p]),
+    ("lbm_load", _S, [_P, ctypes.c_char_p]),
+    ("lbm_checkpoint_desc", _S, [ctypes.c_char_p, _P]),
     ("lbm_moments", _S, [_P, _P, _P, _P, _P]),
     ("lbm_conservation", _S, [_P, _P]),
     ("lbm_batch_create", _S, [_I32, _I32, _P, _P]),

@@ -611,8 +611,9 @@ LBM_API lbm_status lbm_step_force_series(lbm_ctx *ctx, int32_t nsteps, float *ho
 LBM_API lbm_status lbm_set_equilibrium_evaluation(lbm_ctx *ctx, int32_t mode) {
     CHECK_CTX(ctx);
     if (ctx->desc.mode != LBM_D3Q27_REF) return fail(ctx, LBM_ERR_UNSUPPORTED, "equilibrium evaluation is D3Q27_REF only");
-    if (mode != LBM_EQ_FLOAT_FLOAT && mode != LBM_EQ_FP64) return fail(ctx, LBM_ERR_INVALID, "unknown equilibrium evaluation");
-    ctx->eq_fp64 = mode == LBM_EQ_FP64;
+    if (mode != LBM_EQ_FLOAT_FLOAT && mode != LBM_EQ_FP64 && mode != LBM_EQ_FP32)
+        return fail(ctx, LBM_ERR_INVALID, "unknown equilibrium evaluation");
+    ctx->eq_mode = mode;
     return LBM_OK;
 }
 

@@ -476,6 +476,69 @@ __device__ __forceinline__ bool collide(float v[27], const Tau &tau) {
     return all_ok;
 }
 
+// calculate_collision with the equilibrium in FP32 (LBM_EQ_FP32): the same FP32 density and
+// SPLIT-weighted velocity as above, then eq_i = W_i rho (1 + 3 ct + 4.5 ct^2 - 1.5 usq) in FP32 --
+// for a pair of opposite directions W rho ((1 - 1.5 usq) + 4.5 ct^2 +- 3 ct) shares everything but
+// the sign of 3 ct -- and f += (eq - f) / tau by the corrected reciprocal product (the IEEE quotient
+// for a tau that passed the exhaustive check and |x| in [2^-96, 2^96]; within an ulp elsewhere).
+// Against the FP64-evaluated equilibrium of the reference each value differs by a few FP32 ulps, far
+// inside a 1e-5 relative tolerance.  Two pairs per paired FP32 instruction.
+__device__ __forceinline__ void collide_fp32(float v[27], const Tau &tau) {
+    float density = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
+    Unroll<27>::run([&](auto ii) {
+        constexpr int i = decltype(ii)::value;
+        density += v[i];
+        split_moment<i>(v[i], ux, uy, uz);
+    });
+    if (density != 0.0f) {
+        ux /= density;
+        uy /= density;
+        uz /= density;
+    }
+    const float base = __fmaf_rn(-1.5f, usq_of(ux, uy, uz), 1.0f);
+    float wr[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) wr[k] = __fmul_rn(kWhi(k), density);
+    auto rel = [&](float x) {
+        const float q = __fmul_rn(x, tau.y);
+        return __fmaf_rn(__fmaf_rn(-q, tau.b, x), tau.y, q);
+    };
+    v[0] = __fadd_rn(v[0], rel(__fsub_rn(__fmul_rn(wr[0], base), v[0])));
+    const float2 y2 = make_float2(tau.y, tau.y), b2 = make_float2(tau.b, tau.b);
+    auto rel2 = [&](float2 x) {
+        const float2 q = __fmul2_rn(x, y2);
+        return __ffma2_rn(__ffma2_rn(make_float2(-q.x, -q.y), b2, x), y2, q);
+    };
+    const float2 base2 = make_float2(base, base), three = make_float2(3.0f, 3.0f), four5 = make_float2(4.5f, 4.5f);
+    Unroll<6>::run([&](auto nn) {
+        constexpr int n = decltype(nn)::value;
+        constexpr int i0 = pair_rep(2 * n), i1 = pair_rep(2 * n + 1);
+        constexpr int j0 = opp27(i0), j1 = opp27(i1);
+        const float2 ct = make_float2(cdot<i0>(ux, uy, uz), cdot<i1>(ux, uy, uz));
+        const float2 w = make_float2(wr[wclass(i0)], wr[wclass(i1)]);
+        const float2 sym = __ffma2_rn(__fmul2_rn(four5, ct), ct, base2);  // 1 - 1.5 usq + 4.5 ct^2
+        const float2 a = __fmul2_rn(three, ct);
+        const float2 ep = __fmul2_rn(w, __fadd2_rn(sym, a));
+        const float2 en = __fmul2_rn(w, __fadd2_rn(sym, make_float2(-a.x, -a.y)));
+        const float2 qp = rel2(__fadd2_rn(ep, make_float2(-v[i0], -v[i1])));
+        const float2 qn = rel2(__fadd2_rn(en, make_float2(-v[j0], -v[j1])));
+        v[i0] = __fadd_rn(v[i0], qp.x);
+        v[i1] = __fadd_rn(v[i1], qp.y);
+        v[j0] = __fadd_rn(v[j0], qn.x);
+        v[j1] = __fadd_rn(v[j1], qn.y);
+    });
+    {
+        constexpr int i = pair_rep(12), j = opp27(i);
+        const float ct = cdot<i>(ux, uy, uz), w = wr[wclass(i)];
+        const float sym = __fmaf_rn(__fmul_rn(4.5f, ct), ct, base), a = __fmul_rn(3.0f, ct);
+        v[i] = __fadd_rn(v[i], rel(__fsub_rn(__fmul_rn(w, __fadd_rn(sym, a)), v[i])));
+        v[j] = __fadd_rn(v[j], rel(__fsub_rn(__fmul_rn(w, __fsub_rn(sym, a)), v[j])));
+    }
+}
+
+// equilibrium evaluations of the kernels' EQ template parameter (lbm_set_equilibrium_evaluation)
+constexpr int EQ_FF = LBM_EQ_FLOAT_FLOAT, EQ_F64 = LBM_EQ_FP64, EQ_F32 = LBM_EQ_FP32;
+
 struct StepArgs {
     const float *src;
     float *dst;
@@ -487,7 +550,7 @@ struct StepArgs {
 };
 
 // one cell of the fused step: pull, zero internal cells, collide, flow source, store
-template <bool EQ64>
+template <int EQ>
 __device__ __forceinline__ bool fused_cell(const StepArgs &a, int64_t c, int x, int y, int z, uint8_t fl) {
     float v[27];
     pull(a.src, a.d, c, x, y, z, v);
@@ -495,7 +558,10 @@ __device__ __forceinline__ bool fused_cell(const StepArgs &a, int64_t c, int x, 
 #pragma unroll
         for (int j = 0; j < 27; ++j) v[j] = 0.0f;
     }
-    if (!collide<EQ64>(v, a.tau)) return false;
+    if constexpr (EQ == EQ_F32)
+        collide_fp32(v, a.tau);
+    else if (!collide<EQ == EQ_F64>(v, a.tau))
+        return false;
     if (a.cli && a.induced && (fl & F_SOURCE)) {
 #pragma unroll
         for (int j = 0; j < 27; ++j) v[j] = v[j] + __ldg(a.induced + j);
@@ -507,22 +573,23 @@ __device__ __forceinline__ bool fused_cell(const StepArgs &a, int64_t c, int x, 
 
 // the rare cell whose float-float equilibrium the bound could not decide, recomputed in FP64
 __device__ __noinline__ void fused_cell_fp64(StepArgs a, int64_t c, int x, int y, int z, uint8_t fl) {
-    fused_cell<true>(a, c, x, y, z, fl);
+    fused_cell<EQ_F64>(a, c, x, y, z, fl);
 }
 
 // 128-thread blocks, registers bounded for 5 per SM (20 warps): the paired float-float evaluation
-// needs ~100 registers without spilling
+// needs ~100 registers without spilling; the FP32 equilibrium fits 8 blocks per SM (32 warps)
 constexpr int FUSED_THREADS = 128;
+__host__ __device__ constexpr int fused_min_blocks(int eq) { return eq == EQ_F32 ? 8 : 5; }
 
-template <bool EQ64>
-__global__ void __launch_bounds__(FUSED_THREADS, 5) fused_kernel(StepArgs a) {
+template <int EQ>
+__global__ void __launch_bounds__(FUSED_THREADS, fused_min_blocks(EQ)) fused_kernel(StepArgs a) {
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= a.d.n) return;
     const uint8_t fl = a.flags[c];
     if (a.cli && (fl & F_GATHER)) return;  // written by gather_kernel
     int x, y, z;
     decode(a.d, c, x, y, z);
-    if (!fused_cell<EQ64>(a, c, x, y, z, fl)) fused_cell_fp64(a, c, x, y, z, fl);
+    if (!fused_cell<EQ>(a, c, x, y, z, fl)) fused_cell_fp64(a, c, x, y, z, fl);
 }
 
 struct GatherArgs {
@@ -617,14 +684,16 @@ __global__ void reflect_copy_kernel(const float *__restrict__ src, float *__rest
     for (int j = 0; j < 27; ++j) dst[(int64_t)j * d.n + c] = zero ? 0.0f : __ldg(src + (int64_t)j * d.n + c);
 }
 
-template <bool EQ64>
+template <int EQ>
 __global__ void collide_kernel(float *__restrict__ f, Dims d, Tau tau) {
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= d.n) return;
     float v[27];
 #pragma unroll
     for (int j = 0; j < 27; ++j) v[j] = f[(int64_t)j * d.n + c];
-    if (!collide<EQ64>(v, tau)) {  // undecided by the float-float bound: the cell again in FP64
+    if constexpr (EQ == EQ_F32) {
+        collide_fp32(v, tau);
+    } else if (!collide<EQ == EQ_F64>(v, tau)) {  // undecided by the float-float bound: the cell again in FP64
 #pragma unroll
         for (int j = 0; j < 27; ++j) v[j] = f[(int64_t)j * d.n + c];
         collide<true>(v, tau);
@@ -900,10 +969,12 @@ cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps, double *series_d) {
         a.tau = tau;
         a.cli = ctx->desc.order == LBM_ORDER_CLI;
         a.induced = (a.cli && ctx->flow_on) ? ctx->induced_d : nullptr;
-        if (ctx->eq_fp64)
-            fused_kernel<true><<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
+        if (ctx->eq_mode == EQ_F64)
+            fused_kernel<EQ_F64><<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
+        else if (ctx->eq_mode == EQ_F32)
+            fused_kernel<EQ_F32><<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
         else
-            fused_kernel<false><<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
+            fused_kernel<EQ_FF><<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         double *copy = series_d ? series_d + 3 * (int64_t)s : nullptr;
@@ -949,10 +1020,12 @@ cudaError_t d3q27_apply(lbm_ctx *ctx, int op) {
             break;
         }
         case LBM_OP_COLLIDE:
-            if (ctx->eq_fp64)
-                collide_kernel<true><<<nb, threads, 0, ctx->stream>>>(cur(ctx), d, tau_of(ctx));
+            if (ctx->eq_mode == EQ_F64)
+                collide_kernel<EQ_F64><<<nb, threads, 0, ctx->stream>>>(cur(ctx), d, tau_of(ctx));
+            else if (ctx->eq_mode == EQ_F32)
+                collide_kernel<EQ_F32><<<nb, threads, 0, ctx->stream>>>(cur(ctx), d, tau_of(ctx));
             else
-                collide_kernel<false><<<nb, threads, 0, ctx->stream>>>(cur(ctx), d, tau_of(ctx));
+                collide_kernel<EQ_FF><<<nb, threads, 0, ctx->stream>>>(cur(ctx), d, tau_of(ctx));
             e = cudaGetLastError();
             break;
         case LBM_OP_FLOW:

@@ -105,7 +105,7 @@ struct lbm_ctx {
     std::vector<uint8_t> flags_h;    // D3Q27_REF: host copy of the user flag bits
     std::vector<std::pair<int32_t, lbm::ReflRecord>> tables_h;
     bool d3_dirty = true;            // gather lists / device flags need a rebuild
-    bool eq_fp64 = false;            // D3Q27_REF: evaluate the equilibrium in FP64 throughout
+    int eq_mode = LBM_EQ_FLOAT_FLOAT;  // D3Q27_REF: equilibrium evaluation (lbm_set_equilibrium_evaluation)
 
     lbm::Scratch scratch;
     double *result_d = nullptr;      // small device result buffer (16 doubles)

@@ -151,3 +151,16 @@ def test_server_rejects_bad_configuration():
     # two population buffers, link words, flags padded to 8 bytes and the 8-byte fluid count
     assert L.lbm_batch_slot_bytes(capi.F16S, 64, 64) == 2 * 9 * 64 * 64 * 2 + 64 * 64 * 2 + 64 * 64 + 8
     assert L.lbm_batch_slot_bytes(capi.F32, 33, 3) == 2 * 9 * 64 * 3 * 4 + 64 * 3 * 2 + 104 + 8
+
+
+def test_checkpoint_header_errors_without_a_gpu(tmp_path):
+    """lbm_checkpoint_desc reads only the file: a missing file and a file that is not a checkpoint
+    are rejected with LBM_ERR_INVALID."""
+    import ctypes
+    from latticeboltzmanncuda_gb300 import capi
+    d = capi.Desc()
+    assert capi.lib().lbm_checkpoint_desc(str(tmp_path / "missing.lbm").encode(), ctypes.byref(d)) == capi.ERR_INVALID
+    junk = tmp_path / "junk.lbm"
+    junk.write_bytes(b"not a checkpoint" * 20)
+    assert capi.lib().lbm_checkpoint_desc(str(junk).encode(), ctypes.byref(d)) == capi.ERR_INVALID
+    assert "not a checkpoint" in capi.last_thread_error()

@@ -2,7 +2,9 @@
 cubin compiled from the reference sources (oracle/refkern.py, oracle/ref_harness.cpp).
 
 Parity bar (as stated for this mode): flags bit-exact (the same bytes go to both), populations
-within max |f_lib - f_ref| <= 1e-5 * max |f_ref| after the run, force within 1e-5 relative.
+within max |f_lib - f_ref| <= 1e-5 * max |f_ref| after the run, force within 1e-5 relative -- for the
+default float-float equilibrium (the reference's FP64 value bit for bit) and for the FP32
+equilibrium (LBM_EQ_FP32, a few ulps from it).
 The reference's reflection scatter uses float atomics in no fixed order, so bit equality of the
 populations is not expected.
 """
@@ -70,10 +72,12 @@ def restrict_slots(recs, max_pop):
 
 
 CASES = [((6, 5, 6), (1, 1, 6)), ((12, 8, 12), (2, 4, 12)), ((32, 16, 32), (1, 16, 32))]
+EQ = ["float_float", "fp32"]  # equilibrium evaluations (lbm_set_equilibrium_evaluation)
 
 
 @pytest.mark.parametrize("dims,threads", CASES)
-def test_stream_collide_matches_reference(dims, threads):
+@pytest.mark.parametrize("eq", EQ)
+def test_stream_collide_matches_reference(dims, threads, eq):
     f, flags, cells, recs, _ = random_lattice(dims, 11 + dims[0])
     steps = 8
     # reflected cells carry their tables, as in a lattice prepared by Lattice::preProcessModel; the
@@ -81,6 +85,7 @@ def test_stream_collide_matches_reference(dims, threads):
     ref = refkern.run(dims, points_from(f, flags), "SC", nsteps=steps, tau=0.75, tab_cells=cells,
                       tab_records=recs, threads=threads)
     with lbm.Lattice(*dims, mode="d3q27_ref", tau=0.75, order=lbm.ORDER_STREAM_COLLIDE) as L:
+        L.set_equilibrium_evaluation(eq)
         L.load_aos(points_from(f, flags))
         L.step(steps)
         got = L.retrieve_aos()
@@ -90,7 +95,8 @@ def test_stream_collide_matches_reference(dims, threads):
 
 
 @pytest.mark.parametrize("dims,threads", CASES)
-def test_cli_order_matches_reference(dims, threads):
+@pytest.mark.parametrize("eq", EQ)
+def test_cli_order_matches_reference(dims, threads, eq):
     """stream, reflect, collide, flow (LatticeBoltzmannCuda.cpp:85-93) with mesh-style reflection
     tables on every slot and the flow plane x = 0 (FlowCriterion.cu:10-13)."""
     f, flags, cells, recs, induced = random_lattice(dims, 5 + dims[1])
@@ -98,6 +104,7 @@ def test_cli_order_matches_reference(dims, threads):
     ref = refkern.run(dims, points_from(f, flags), "SRCF", nsteps=steps, tau=0.7, tab_cells=cells,
                       tab_records=recs, flow_criterion=2, induced=induced, threads=threads)
     with lbm.Lattice(*dims, mode="d3q27_ref", tau=0.7, order=lbm.ORDER_CLI) as L:
+        L.set_equilibrium_evaluation(eq)
         L.load_aos(points_from(f, flags))
         L.set_reflection_tables(cells, recs)
         L.set_flow(flags & SOURCE, induced)
@@ -107,7 +114,8 @@ def test_cli_order_matches_reference(dims, threads):
 
 
 @pytest.mark.parametrize("dims,threads", CASES[:2])
-def test_force_matches_reference(dims, threads):
+@pytest.mark.parametrize("eq", EQ)
+def test_force_matches_reference(dims, threads, eq):
     f, flags, cells, recs, induced = random_lattice(dims, 17 + dims[2])
     recs = restrict_slots(recs, 9)
     start = np.array([0.5, -0.25, 0.125], np.float32)
@@ -116,6 +124,7 @@ def test_force_matches_reference(dims, threads):
     ref = refkern.run(dims, points_from(f, flags), "SRCF", nsteps=steps, tau=0.9, tab_cells=cells,
                       tab_records=recs, flow_criterion=2, induced=induced, force=ref_force, threads=threads)
     with lbm.Lattice(*dims, mode="d3q27_ref", tau=0.9, order=lbm.ORDER_CLI) as L:
+        L.set_equilibrium_evaluation(eq)
         L.load_aos(points_from(f, flags))
         L.set_reflection_tables(cells, recs)
         L.set_flow(flags & SOURCE, induced)
@@ -127,11 +136,13 @@ def test_force_matches_reference(dims, threads):
     assert np.max(np.abs(force - ref_force)) <= 1e-5 * np.max(np.abs(ref_force)), (force, ref_force)
 
 
-def test_separate_passes_match_reference():
+@pytest.mark.parametrize("eq", EQ)
+def test_separate_passes_match_reference(eq):
     """Lattice::simulateStreaming / simulateReflections / simulateCollision / simulateFlow one by one."""
     dims, threads = (9, 6, 9), (1, 2, 9)
     f, flags, cells, recs, induced = random_lattice(dims, 99)
     with lbm.Lattice(*dims, mode="d3q27_ref", tau=0.85) as L:
+        L.set_equilibrium_evaluation(eq)
         L.load_aos(points_from(f, flags))
         L.set_reflection_tables(cells, recs)
         L.set_flow(flags & SOURCE, induced)
@@ -143,7 +154,8 @@ def test_separate_passes_match_reference():
             close(L.retrieve_aos()["f"], pts["f"])
 
 
-def test_sphere_mesh_cli_matches_reference():
+@pytest.mark.parametrize("eq", EQ)
+def test_sphere_mesh_cli_matches_reference(eq):
     """A sphere mesh through the front end (flags, tables), then 6 CLI-order steps: library vs the
     reference's own kernels on the same flags and tables (X == Z, grid tiled exactly)."""
     from refcases import icosphere
@@ -163,6 +175,7 @@ def test_sphere_mesh_cli_matches_reference():
     ref = refkern.run(dims, points_from(f, flags), "SRCF", nsteps=6, tau=0.75, tab_cells=cells, tab_records=recs,
                       flow_criterion=2, induced=induced, threads=threads)
     with lbm.Lattice(*dims, mode="d3q27_ref", tau=0.75, order=lbm.ORDER_CLI) as L:
+        L.set_equilibrium_evaluation(eq)
         L.load_aos(points_from(f, flags))
         L.set_reflection_tables(cells, recs)
         L.set_flow(flags & SOURCE, induced)
