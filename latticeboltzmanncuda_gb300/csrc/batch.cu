@@ -4,15 +4,16 @@
 // Each domain (a "slot") owns one allocation -- its two population buffers, link words, flags and
 // fluid-cell count -- made when it is added, so slots come and go without moving anyone else's
 // state (the serving loop admits and retires requests between rounds).  Every block of a launch
-// updates one tile, TY rows x (TX * V) cells of one slot, with the same vectorised update as the
-// single-domain kernel, so a domain's populations are bit-identical whether it runs alone or in
-// any mix.  Tiles are ordered slot by slot, rows ascending; odd steps walk them backwards (each
-// step starts where the previous one ended, on data still in L2).  Up to PARAM_SLOTS live slots
-// (FP32, 16-bit storage) the slot descriptors (size, buffer base, parity, step budget, relaxation
-// rate, force, wall velocity, periodicity) and the first tile of every slot travel in the kernel's
-// parameter block and a block derives its tile from its index; beyond that, and for FP64, a device
-// table of descriptors and a flat tile list (slot, x-chunk, first row) do.  The tile shape
-// (V, TX, TY) is picked by the autotuner from timings on the batch itself.
+// updates one tile of one slot with the same vectorised update as the single-domain kernel, so a
+// domain's populations are bit-identical whether it runs alone or in any mix.  Tiles are ordered
+// slot by slot, rows ascending; odd steps walk them backwards (each step starts where the previous
+// one ended, on data still in L2).  Up to PARAM_SLOTS live slots (FP32, 16-bit storage) the slot
+// descriptors (size, buffer base, parity, step budget, relaxation rate, force, wall velocity,
+// periodicity) and the first tile of every slot travel in the kernel's parameter block, a block
+// finds its slot by a binary search over those, and a tile is a run of TX * TY * V consecutive
+// cells of the slot's padded cell array; beyond that, and for FP64, a device table of descriptors
+// and a tile list (slot, x-chunk, first row: TY rows x TX * V cells) do.  The tile shape (V, TX,
+// TY) is picked by the autotuner from timings on the batch itself.
 //
 // Nothing on the serving path waits for the device: adding a slot (flags upload, link words,
 // fluid-cell count, equilibrium), the table uploads before a launch sequence, freeing a slot and
@@ -152,44 +153,25 @@ struct BatchParams {
     SlotDescP d[PARAM_SLOTS];
 };
 
-// a tile of the parameter-block path for 16-bit storage: the block's slot (an index into the
-// parameter block) and the tile's index within the slot, one 8-byte load.  (FP32 blocks find their
-// slot by a binary search over the slots' first tiles instead: measured on the serve domains, the
-// 16-bit kernel, bound by instruction issue, runs 3 % faster with the load, the FP32 kernel, bound
-// by memory latency, 5 % slower.)
-struct TileP {
-    int slot;
-    unsigned tile;
-};
-
-template <class S>
-constexpr bool tile_records() {
-    return sizeof(S) == 2;
-}
 static_assert(sizeof(BatchParams) <= 32764, "kernel parameter block limit");
 
 // Parameter-block tiles are flat: tile j of a slot is the run of blockDim.x * blockDim.y * V
 // consecutive cells starting at j * blockDim.x * blockDim.y * V of the slot's padded cell array
 // [0, pitch * ny), row after row (step_vec_flat), so a row costs at most its 31 padding cells of
 // idle lanes instead of the rest of a column chunk, and only a slot's last tile is ragged.
+// A block finds its slot by a binary search over the slots' first tiles in the parameter block: the
+// loop and its loads are uniform, so the descriptor fields come from the constant bank into uniform
+// registers.  (An 8-byte tile record per block read from global memory instead measured 1-4 %
+// slower with the flat tiles on the serve and batch domains.)
 template <class S, int V>
-__device__ __forceinline__ void batch_tile_p(const BatchParams &p, const TileP *__restrict__ tiles, int step,
-                                             int reverse) {
+__device__ __forceinline__ void batch_tile_p(const BatchParams &p, int step, int reverse) {
     const int t = reverse ? p.ntiles - 1 - (int)blockIdx.x : (int)blockIdx.x;
-    int slot, tile;
-    if constexpr (tile_records<S>()) {
-        const TileP rec = tiles[t];
-        slot = rec.slot;
-        tile = (int)rec.tile;
-    } else {
-        int lo = 0, hi = p.n - 1;
-        while (lo < hi) {  // the last slot whose first tile is at or before t (uniform per block)
-            const int mid = (lo + hi + 1) >> 1;
-            if (p.start[mid] <= t) lo = mid; else hi = mid - 1;
-        }
-        slot = lo;
-        tile = t - p.start[lo];
+    int lo = 0, hi = p.n - 1;
+    while (lo < hi) {  // the last slot whose first tile is at or before t (uniform per block)
+        const int mid = (lo + hi + 1) >> 1;
+        if (p.start[mid] <= t) lo = mid; else hi = mid - 1;
     }
+    const int slot = lo, tile = t - p.start[lo];
     const SlotDescP &D = p.d[slot];
     if (step >= D.stop) return;  // the slot has used its step budget
     const int pitch = (D.nx + 31) & ~31, plane = pitch * D.ny;
@@ -228,16 +210,14 @@ __host__ __device__ constexpr int batch_min_blocks(int v) { return v == 8 ? 2 : 
 
 template <class S, int V>
 __global__ void __launch_bounds__(256, batch_min_blocks(V)) batch_step_kernel_p(const __grid_constant__ BatchParams p,
-                                                                               const TileP *__restrict__ tiles,
                                                                                int step, int reverse) {
-    batch_tile_p<S, V>(p, tiles, step, reverse);
+    batch_tile_p<S, V>(p, step, reverse);
 }
 
 template <class S, int V>
-__global__ void __launch_bounds__(256, 4) batch_step_kernel_p_occ(const __grid_constant__ BatchParams p,
-                                                                  const TileP *__restrict__ tiles, int step,
+__global__ void __launch_bounds__(256, 4) batch_step_kernel_p_occ(const __grid_constant__ BatchParams p, int step,
                                                                   int reverse) {
-    batch_tile_p<S, V>(p, tiles, step, reverse);
+    batch_tile_p<S, V>(p, step, reverse);
 }
 
 size_t dsize(int dtype) { return dtype == LBM_F64 ? 8 : (dtype == LBM_F32 ? 4 : 2); }
@@ -282,8 +262,6 @@ struct lbm_batch {
     std::map<int64_t, Pending> pending;  // read-backs by ticket
     bool use_params = false;             // the launch takes the descriptors in its parameter block
     BatchParams params{};
-    TileP *ptiles_d = nullptr;           // tiles of the parameter-block path
-    size_t ptiles_cap = 0;
     int64_t next_ticket = 1;
 };
 
@@ -472,18 +450,6 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
             ++p.n;
         }
         p.ntiles = ntiles;
-        if (dsize(b->dtype) == 2 && (b->tiles_dirty || !b->use_params)) {  // 16-bit: tile records, rebuilt with the live set or the shape
-            std::vector<TileP> tl;
-            tl.reserve((size_t)ntiles);
-            for (int k = 0; k < p.n; ++k) {
-                const int end = k + 1 < p.n ? p.start[k + 1] : ntiles;
-                for (int j = 0; j < end - p.start[k]; ++j) tl.push_back(TileP{k, (unsigned)j});
-            }
-            lbm_status st = grow_table(b, (void **)&b->ptiles_d, &b->ptiles_cap, tl.size(), sizeof(TileP), 1024,
-                                       "batch: tile table");
-            if (st == LBM_OK) st = upload_async(b, b->ptiles_d, tl.data(), tl.size() * sizeof(TileP), "batch: upload tiles");
-            if (st != LBM_OK) return st;
-        }
         b->ntiles = ntiles;
         b->use_params = true;
         b->dirty = false;
@@ -541,9 +507,9 @@ cudaError_t launch_v(lbm_batch *b, int step, int reverse) {
     dim3 grid((unsigned)b->ntiles);
     if (b->use_params) {
         if constexpr (sizeof(S) == 2 && V == 4)
-            batch_step_kernel_p_occ<S, V><<<grid, block, 0, b->stream>>>(b->params, b->ptiles_d, step, reverse);
+            batch_step_kernel_p_occ<S, V><<<grid, block, 0, b->stream>>>(b->params, step, reverse);
         else if constexpr (sizeof(S) <= 4)
-            batch_step_kernel_p<S, V><<<grid, block, 0, b->stream>>>(b->params, b->ptiles_d, step, reverse);
+            batch_step_kernel_p<S, V><<<grid, block, 0, b->stream>>>(b->params, step, reverse);
         return cudaGetLastError();
     }
     if constexpr (sizeof(S) == 2 && V == 4)
@@ -720,7 +686,6 @@ LBM_API lbm_status lbm_batch_destroy(lbm_batch *b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     cudaFree(b->desc_d);
     cudaFree(b->tiles_d);
-    cudaFree(b->ptiles_d);
     cudaFree(b->staging);
     cudaFree(b->result_d);
     for (PinnedBlock &pb : b->pinned) {

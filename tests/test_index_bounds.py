@@ -287,12 +287,11 @@ def test_bulk_protocol_simulation_catches_a_missing_release():
 # each; then pitch x ny uint16 link words; then flags and the fluid count).  Tiles are flat: tile j
 # of a slot covers the tx * ty * V consecutive cells from j * tx * ty * V of the slot's padded cell
 # array, thread k of the block the vector at j * tx * ty * V + k * V (d2q9_vec.cuh: step_vec_flat).
-# 16-bit blocks read (slot, tile) from a tile record, FP32 blocks binary-search the slots' first
-# tiles.
+# A block finds its slot by a binary search over the slots' first tiles.
 
 
 def batch_tiles(shapes, V, tx, ty):
-    """The tile list of rebuild(): (slot, tile within the slot) per tile, and the slots' first tiles."""
+    """Every tile of a launch as (slot, tile within the slot), and the slots' first tiles (rebuild())."""
     tiles, start = [], []
     per_tile = tx * ty * V
     for k, (nx, ny) in enumerate(shapes):
@@ -386,7 +385,7 @@ def test_batch_parameter_path_tiles_and_addresses(seed):
     shapes += [(1, 1), (32, 1), (33, 3), (64, 5)]
     for elem, V, tx, ty in ((2, 4, 32, 4), (2, 8, 32, 2), (2, 2, 64, 1), (4, 4, 32, 2), (4, 2, 128, 2), (2, 8, 256, 1)):
         tiles, start = batch_tiles(shapes, V, tx, ty)
-        # the binary search (FP32) finds every tile's record (16-bit)
+        # the binary search finds every tile's slot and index within the slot
         for t, rec in enumerate(tiles):
             assert search_tile(start, t) == rec
         for k, (nx, ny) in enumerate(shapes):
