@@ -188,7 +188,7 @@ LBM_API lbm_status lbm_apply(lbm_ctx *ctx, int32_t op);
  *                                 the step)
  *   LBM_EQ_FP32                   the same expression in FP32 (a few ulps from the FP64 value; the
  *                                 populations stay within 1e-5 relative of the reference's), for
- *                                 speed.  Cells next to reflecting cells keep the FP64 expression. */
+ *                                 speed. */
 enum { LBM_EQ_FLOAT_FLOAT = 0, LBM_EQ_FP64 = 1, LBM_EQ_FP32 = 2 };
 LBM_API lbm_status lbm_set_equilibrium_evaluation(lbm_ctx *ctx, int32_t mode);
 /* Diagnostic: both evaluations on `samples` pseudo-random (rho, u) draws (|u| up to 2) x the 27

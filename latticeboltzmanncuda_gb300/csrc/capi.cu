@@ -135,6 +135,10 @@ lbm_status d3_prepare(lbm_ctx *ctx) {
     dfree(ctx, ctx->tgt_cells_d, ctx->ntgt * sizeof(int32_t));
     dfree(ctx, ctx->tgt_off_d, (ctx->ntgt + 1) * sizeof(int32_t));
     dfree(ctx, ctx->entries_d, ctx->nent * sizeof(GatherEntry));
+    dfree(ctx, ctx->gathered_d, ctx->ntgt * 27 * sizeof(float));
+    dfree(ctx, ctx->tgt_index_d, ctx->ntgt ? (size_t)ctx->cells * sizeof(int32_t) : 0);
+    ctx->gathered_d = nullptr;
+    ctx->tgt_index_d = nullptr;
     ctx->tgt_cells_d = nullptr;
     ctx->tgt_off_d = nullptr;
     ctx->entries_d = nullptr;
@@ -148,7 +152,15 @@ lbm_status d3_prepare(lbm_ctx *ctx) {
         CUDA_TRY(ctx, cudaMemcpy(ctx->tgt_cells_d, tgt.data(), tgt.size() * sizeof(int32_t), cudaMemcpyHostToDevice), "upload gather targets");
         CUDA_TRY(ctx, cudaMemcpy(ctx->tgt_off_d, off.data(), off.size() * sizeof(int32_t), cudaMemcpyHostToDevice), "upload gather offsets");
         CUDA_TRY(ctx, cudaMemcpy(ctx->entries_d, flat.data(), flat.size() * sizeof(GatherEntry), cudaMemcpyHostToDevice), "upload gather entries");
-        const size_t nblocks = (size_t)((ctx->ntgt + 127) / 128);
+        if ((s = dalloc(ctx, (void **)&ctx->gathered_d, tgt.size() * 27 * sizeof(float), "gathered populations")) != LBM_OK)
+            return s;
+        if ((s = dalloc(ctx, (void **)&ctx->tgt_index_d, (size_t)ctx->cells * sizeof(int32_t), "target index")) != LBM_OK)
+            return s;
+        std::vector<int32_t> index((size_t)ctx->cells, -1);
+        for (size_t k = 0; k < tgt.size(); ++k) index[(size_t)tgt[k]] = (int32_t)k;
+        CUDA_TRY(ctx, cudaMemcpy(ctx->tgt_index_d, index.data(), index.size() * sizeof(int32_t), cudaMemcpyHostToDevice),
+                 "upload target index");
+        const size_t nblocks = d3q27_gather_blocks(ctx->ntgt);
         if ((s = ensure_scratch(ctx, std::max<size_t>(nblocks * 3, 512 * 4))) != LBM_OK) return s;
     }
     CUDA_TRY(ctx, cudaMemcpy(ctx->flags_d, fl.data(), fl.size(), cudaMemcpyHostToDevice), "upload flags");
@@ -300,6 +312,8 @@ LBM_API lbm_status lbm_destroy(lbm_ctx *ctx) {
     cudaFree(ctx->tgt_cells_d);
     cudaFree(ctx->tgt_off_d);
     cudaFree(ctx->entries_d);
+    cudaFree(ctx->gathered_d);
+    cudaFree(ctx->tgt_index_d);
     cudaFree(ctx->induced_d);
     cudaFree(ctx->force_acc_d);
     cudaFree(ctx->scratch.partials);
@@ -538,7 +552,7 @@ LBM_API lbm_status lbm_set_force(lbm_ctx *ctx, const float in[3], int32_t enable
     double h[4] = {in ? in[0] : 0.0, in ? in[1] : 0.0, in ? in[2] : 0.0, 0.0};
     CUDA_TRY(ctx, cudaMemcpyAsync(ctx->force_acc_d, h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream), "upload force");
     ctx->force_on = enabled != 0;
-    if (ctx->force_on && (st = ensure_scratch(ctx, std::max<size_t>((size_t)((ctx->ntgt + 127) / 128) * 3, 512 * 4))) != LBM_OK)
+    if (ctx->force_on && (st = ensure_scratch(ctx, std::max<size_t>(d3q27_gather_blocks(ctx->ntgt) * 3, 512 * 4))) != LBM_OK)
         return st;
     return sync(ctx, "upload force");
 }
@@ -549,7 +563,7 @@ LBM_API lbm_status lbm_set_force_accumulation(lbm_ctx *ctx, int32_t enabled) {
     lbm_status st = use_device(ctx);
     if (st != LBM_OK) return st;
     ctx->force_on = enabled != 0;
-    if (ctx->force_on && (st = ensure_scratch(ctx, std::max<size_t>((size_t)((ctx->ntgt + 127) / 128) * 3, 512 * 4))) != LBM_OK)
+    if (ctx->force_on && (st = ensure_scratch(ctx, std::max<size_t>(d3q27_gather_blocks(ctx->ntgt) * 3, 512 * 4))) != LBM_OK)
         return st;
     return LBM_OK;
 }

@@ -8,16 +8,31 @@ namespace lbm {
 namespace {
 thread_local std::string g_thread_error;
 
-// out[k] (+)= sum over b of partials[b*ncomp + k], one thread per component, in block order
-__global__ void finalize_kernel(const double *__restrict__ partials, int nblocks, int ncomp, double *out,
-                                int accumulate, double *also) {
-    const int k = threadIdx.x;
-    if (k >= ncomp) return;
-    double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += partials[(int64_t)b * ncomp + k];
-    const double v = accumulate ? out[k] + s : s;
-    out[k] = v;
-    if (also) also[k] = v;
+// out[k] (+)= sum over b of partials[b*ncomp + k] (ncomp <= FIN_MAX): thread t sums the blocks t,
+// t + FIN_THREADS, ... in that order, then a fixed tree over the threads -- the same order on every
+// run, with the loads of many blocks in flight at once.
+constexpr int FIN_THREADS = 1024, FIN_MAX = 4;
+
+__global__ void __launch_bounds__(FIN_THREADS) finalize_kernel(const double *__restrict__ partials, int nblocks,
+                                                               int ncomp, double *out, int accumulate, double *also) {
+    __shared__ double sm[FIN_MAX][FIN_THREADS];
+    const int t = threadIdx.x;
+    for (int k = 0; k < ncomp; ++k) {
+        double s = 0.0;
+        for (int b = t; b < nblocks; b += FIN_THREADS) s += partials[(int64_t)b * ncomp + k];
+        sm[k][t] = s;
+    }
+    __syncthreads();
+    for (int h = FIN_THREADS / 2; h > 0; h >>= 1) {
+        if (t < h)
+            for (int k = 0; k < ncomp; ++k) sm[k][t] += sm[k][t + h];
+        __syncthreads();
+    }
+    if (t < ncomp) {
+        const double v = accumulate ? out[t] + sm[t][0] : sm[t][0];
+        out[t] = v;
+        if (also) also[t] = v;
+    }
 }
 }  // namespace
 
@@ -75,7 +90,8 @@ lbm_status ensure_scratch(lbm_ctx *ctx, size_t n) {
 
 cudaError_t finalize_sums(cudaStream_t s, const double *partials, int nblocks, int ncomp, double *out,
                           bool accumulate, double *also) {
-    finalize_kernel<<<1, 32, 0, s>>>(partials, nblocks, ncomp, out, accumulate ? 1 : 0, also);
+    if (ncomp < 1 || ncomp > FIN_MAX) return cudaErrorInvalidValue;
+    finalize_kernel<<<1, FIN_THREADS, 0, s>>>(partials, nblocks, ncomp, out, accumulate ? 1 : 0, also);
     return cudaGetLastError();
 }
 

@@ -545,15 +545,24 @@ struct StepArgs {
     const uint8_t *flags;
     Dims d;
     Tau tau;
-    const float *induced;  // nullptr: no flow
-    int cli;               // 1: stream, reflect, collide, flow; 0: stream, collide
+    const float *induced;    // nullptr: no flow
+    int cli;                 // 1: stream, reflect, collide, flow; 0: stream, collide
+    const float *gathered;   // CLI order: the gather targets' populations (27 per target), or nullptr
+    const int32_t *tgt_index;  // per cell: its row of `gathered`
 };
 
-// one cell of the fused step: pull, zero internal cells, collide, flow source, store
+// one cell of the fused step: pull (or, for a target of the gather lists, its gathered populations),
+// zero internal cells, collide, flow source, store
 template <int EQ>
 __device__ __forceinline__ bool fused_cell(const StepArgs &a, int64_t c, int x, int y, int z, uint8_t fl) {
     float v[27];
-    pull(a.src, a.d, c, x, y, z, v);
+    if (a.cli && (fl & F_GATHER)) {
+        const float *g = a.gathered + (int64_t)__ldg(a.tgt_index + c) * 27;
+#pragma unroll
+        for (int j = 0; j < 27; ++j) v[j] = __ldg(g + j);
+    } else {
+        pull(a.src, a.d, c, x, y, z, v);
+    }
     if (a.cli && (fl & F_INTERNAL)) {
 #pragma unroll
         for (int j = 0; j < 27; ++j) v[j] = 0.0f;
@@ -586,7 +595,6 @@ __global__ void __launch_bounds__(FUSED_THREADS, fused_min_blocks(EQ)) fused_ker
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= a.d.n) return;
     const uint8_t fl = a.flags[c];
-    if (a.cli && (fl & F_GATHER)) return;  // written by gather_kernel
     int x, y, z;
     decode(a.d, c, x, y, z);
     if (!fused_cell<EQ>(a, c, x, y, z, fl)) fused_cell_fp64(a, c, x, y, z, fl);
@@ -599,63 +607,98 @@ struct GatherArgs {
     int64_t ntgt;
     double *partials;  // 3 per block, or nullptr when no force is accumulated
     int force_mode;
+    float *gathered;   // mode 0: the targets' populations out (27 per target)
 };
 
-// force contribution m * (c_d SPLIT[d] - c_k SPLIT[k]) (SimCalcFuncs.cu:181-183)
-__device__ __forceinline__ void force_term(float m, const GatherEntry &e, int mode, double acc[3]) {
+// force contribution m * (c_d SPLIT[d] - c_k SPLIT[k]) (SimCalcFuncs.cu:181-183); cs[j][a] = c_ja SPLIT_j
+// (exact products), read from shared memory: the lanes of a warp index it with different directions,
+// which the constant cache would serve one address at a time
+__device__ __forceinline__ void force_term(float m, const GatherEntry &e, int mode, const float (*cs)[3],
+                                           double acc[3]) {
     const int k = mode == LBM_FORCE_MOMENTUM_EXCHANGE ? e.slot / 3 : e.slot;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const float kin = k < 27 ? (float)c_dir[k][a] * c_split[k] : 0.0f;
-        const float coef = ((float)c_dir[e.dst_pop][a] * c_split[e.dst_pop]) - kin;
-        acc[a] += (double)(m * coef);
+        const float kin = k < 27 ? cs[k][a] : 0.0f;
+        const float coef = __fsub_rn(cs[e.dst_pop][a], kin);
+        acc[a] += (double)__fmul_rn(m, coef);
     }
 }
 
-// mode 0: fused step (values of the reflecting cells are their streamed populations);
-// mode 1: the reference's separate reflection pass (values read in place, no collision).
-// The cells next to reflecting cells (a thin layer) evaluate the equilibrium in FP64 directly.
+// The gather lists, one warp per target cell: lane j (< 27) holds population j of the cell -- pulled
+// from its neighbour with zero fill (mode 0: the fused step, whose reflecting cells contribute their
+// streamed populations) or read in place (mode 1: the reference's separate reflection pass) -- and
+// the lanes read up to 32 of the cell's entries at once: each computes its contribution m = val * w
+// and the warp walks them in list order, lane dst_pop adding each one that targets it, so every
+// population takes its adds in the order of the sequential scatter (one rounded add of the rounded
+// product per contribution, as the reference's atomicAdd at SimCalcFuncs.cu:177).  The force terms
+// are summed in FP64 per lane, then over the block in a fixed tree.  Internal cells are zeroed.
+// Mode 0 writes the result to the target's row of g.gathered, from which the fused kernel, launched
+// next, collides the cell with all the others; mode 1 writes it to the destination lattice.
+__device__ __forceinline__ float pull_one(const float *__restrict__ src, const Dims &d, int64_t c, int x, int y,
+                                          int z, int j, const int (*dir)[3]) {
+    const int sx = x - dir[j][0], sy = y - dir[j][1], sz = z - dir[j][2];
+    if (sx < 0 || sy < 0 || sz < 0 || sx >= d.X || sy >= d.Y || sz >= d.Z) return 0.0f;
+    return __ldg(src + (int64_t)j * d.n + sz + (int64_t)d.Z * (sy + (int64_t)d.Y * sx));
+}
+
+constexpr int GATHER_THREADS = 128;  // four target cells per block
+
 template <int MODE>
-__global__ void __launch_bounds__(128) gather_kernel(StepArgs a, GatherArgs g) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(GATHER_THREADS) gather_kernel(StepArgs a, GatherArgs g) {
+    // the direction tables in shared memory: each lane indexes them with its own direction
+    __shared__ int s_dir[27][3];
+    __shared__ float s_cs[27][3];
+    if (threadIdx.x < 27) {
+        for (int q = 0; q < 3; ++q) {
+            s_dir[threadIdx.x][q] = c_dir[threadIdx.x][q];
+            s_cs[threadIdx.x][q] = (float)c_dir[threadIdx.x][q] * c_split[threadIdx.x];
+        }
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;  // target of this warp
     double facc[3] = {0.0, 0.0, 0.0};
-    if (i < g.ntgt) {
+    if (i < g.ntgt) {  // uniform per warp
         const int64_t c = g.tgt[i];
         const uint8_t fl = a.flags[c];
-        float v[27];
-        if (MODE == 0) {
-            int x, y, z;
-            decode(a.d, c, x, y, z);
-            pull(a.src, a.d, c, x, y, z, v);
-        } else {
+        int x = 0, y = 0, z = 0;
+        if (MODE == 0) decode(a.d, c, x, y, z);
+        float v = 0.0f;  // population `lane` of the cell
+        if (lane < 27)
+            v = MODE == 0 ? pull_one(a.src, a.d, c, x, y, z, lane, s_dir) : __ldg(a.src + (int64_t)lane * a.d.n + c);
+        const int k0 = g.off[i], k1 = g.off[i + 1];
+        for (int base = k0; base < k1; base += 32) {
+            const int k = base + lane;
+            float m = 0.0f;
+            int dst = 0;
+            double fc[3] = {0.0, 0.0, 0.0};
+            if (k < k1) {
+                const GatherEntry e = g.ent[k];
+                const int64_t s = MODE == 0 ? (int64_t)e.src_stream : (int64_t)e.src_cell;
+                const float val = s >= 0 ? __ldg(a.src + (int64_t)e.src_pop * a.d.n + s) : 0.0f;
+                m = __fmul_rn(val, e.w);
+                dst = e.dst_pop;
+                if (g.partials) force_term(m, e, g.force_mode, s_cs, fc);
+            }
+            // each lane keeps its own entries' force terms; block_sum below adds them in a fixed tree
+            // (GB300 issues an FP64 instruction per warp at a small fraction of the FP32 rate, so the
+            // additions are spread over the lanes rather than made one after another in one lane)
 #pragma unroll
-            for (int j = 0; j < 27; ++j) v[j] = __ldg(a.src + (int64_t)j * a.d.n + c);
-        }
-        for (int k = g.off[i]; k < g.off[i + 1]; ++k) {
-            const GatherEntry e = g.ent[k];
-            const int64_t s = MODE == 0 ? (int64_t)e.src_stream : (int64_t)e.src_cell;
-            const float val = s >= 0 ? __ldg(a.src + (int64_t)e.src_pop * a.d.n + s) : 0.0f;
-            const float m = __fmul_rn(val, e.w);
-            // v[e.dst_pop] += m, one rounded add of the rounded product per contribution as the
-            // reference's atomicAdd (SimCalcFuncs.cu:177), selected over the register-resident array
-#pragma unroll
-            for (int j = 1; j < 27; ++j)
-                if (j == e.dst_pop) v[j] = __fadd_rn(v[j], m);
-            if (g.partials) force_term(m, e, g.force_mode, facc);
-        }
-        if (fl & F_INTERNAL) {
-#pragma unroll
-            for (int j = 0; j < 27; ++j) v[j] = 0.0f;
-        }
-        if (MODE == 0) {
-            collide<true>(v, a.tau);
-            if (a.induced && (fl & F_SOURCE)) {
-#pragma unroll
-                for (int j = 0; j < 27; ++j) v[j] = v[j] + __ldg(a.induced + j);
+            for (int q = 0; q < 3; ++q) facc[q] += fc[q];
+            const int cnt = min(32, k1 - base);
+            for (int j = 0; j < cnt; ++j) {
+                const float mj = __shfl_sync(0xffffffffu, m, j);
+                const int dj = __shfl_sync(0xffffffffu, dst, j);
+                if (lane == dj) v = __fadd_rn(v, mj);
             }
         }
-#pragma unroll
-        for (int j = 0; j < 27; ++j) a.dst[(int64_t)j * a.d.n + c] = v[j];
+        if (fl & F_INTERNAL) v = 0.0f;
+        if (lane < 27) {
+            if (MODE == 0)
+                g.gathered[i * 27 + lane] = v;
+            else
+                a.dst[(int64_t)lane * a.d.n + c] = v;
+        }
     }
     if (g.partials) block_sum<3>(facc, g.partials + 3 * blockIdx.x);
 }
@@ -855,18 +898,20 @@ GatherArgs gather_args(lbm_ctx *ctx) {
     g.ntgt = ctx->ntgt;
     g.partials = ctx->force_on ? ctx->scratch.partials : nullptr;
     g.force_mode = ctx->desc.force_mode;
+    g.gathered = ctx->gathered_d;
     return g;
 }
 
 cudaError_t launch_gather(lbm_ctx *ctx, const StepArgs &a, int mode, double *force_copy = nullptr) {
     if (ctx->ntgt == 0) return cudaSuccess;
     GatherArgs g = gather_args(ctx);
-    const int threads = 128;
-    const unsigned nb = blocks_for(ctx->ntgt, threads);
-    if (mode == 0)
-        gather_kernel<0><<<nb, threads, 0, ctx->stream>>>(a, g);
-    else
+    const int threads = GATHER_THREADS;
+    const unsigned nb = (unsigned)d3q27_gather_blocks(ctx->ntgt);  // one warp per target cell
+    static_assert(GATHER_THREADS == 4 * 32, "d3q27_gather_blocks assumes four warps per block");
+    if (mode != 0)
         gather_kernel<1><<<nb, threads, 0, ctx->stream>>>(a, g);
+    else
+        gather_kernel<0><<<nb, threads, 0, ctx->stream>>>(a, g);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !g.partials) return e;
     return finalize_sums(ctx->stream, g.partials, (int)nb, 3, ctx->force_acc_d, true, force_copy);
@@ -969,20 +1014,23 @@ cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps, double *series_d) {
         a.tau = tau;
         a.cli = ctx->desc.order == LBM_ORDER_CLI;
         a.induced = (a.cli && ctx->flow_on) ? ctx->induced_d : nullptr;
+        a.gathered = ctx->gathered_d;
+        a.tgt_index = ctx->tgt_index_d;
+        cudaError_t e = cudaSuccess;
+        double *copy = series_d ? series_d + 3 * (int64_t)s : nullptr;
+        const bool reduced = a.cli && ctx->ntgt > 0 && ctx->force_on;  // the force changes this step
+        if (a.cli) {  // the targets of the gather lists first: the fused kernel collides them
+            e = launch_gather(ctx, a, 0, copy);
+            if (e != cudaSuccess) return e;
+        }
         if (ctx->eq_mode == EQ_F64)
             fused_kernel<EQ_F64><<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
         else if (ctx->eq_mode == EQ_F32)
             fused_kernel<EQ_F32><<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
         else
             fused_kernel<EQ_FF><<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
-        cudaError_t e = cudaGetLastError();
+        e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        double *copy = series_d ? series_d + 3 * (int64_t)s : nullptr;
-        const bool reduced = a.cli && ctx->ntgt > 0 && ctx->force_on;  // the force changes this step
-        if (a.cli) {
-            e = launch_gather(ctx, a, 0, copy);
-            if (e != cudaSuccess) return e;
-        }
         if (copy && !reduced) {
             e = cudaMemcpyAsync(copy, ctx->force_acc_d, 3 * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
             if (e != cudaSuccess) return e;
@@ -1015,6 +1063,8 @@ cudaError_t d3q27_apply(lbm_ctx *ctx, int op) {
             a.tau = tau_of(ctx);
             a.induced = nullptr;
             a.cli = 1;
+            a.gathered = nullptr;
+            a.tgt_index = nullptr;
             e = launch_gather(ctx, a, 1);
             ctx->cur ^= 1;
             break;

@@ -96,6 +96,8 @@ struct lbm_ctx {
     int32_t *tgt_cells_d = nullptr;  // target cells of the gather lists
     int32_t *tgt_off_d = nullptr;    // CSR offsets (ntgt + 1)
     lbm::GatherEntry *entries_d = nullptr;
+    float *gathered_d = nullptr;     // ntgt x 27: the targets' populations after the gather, before collision
+    int32_t *tgt_index_d = nullptr;  // per cell: its index in the target list, or -1
     int64_t ntgt = 0, nent = 0;
     float *induced_d = nullptr;      // 27 floats
     bool flow_on = false;
@@ -166,6 +168,9 @@ cudaError_t d3q27_moments(lbm_ctx *ctx, float *rho_d, float *ux_d, float *uy_d, 
 cudaError_t d3q27_conservation(lbm_ctx *ctx, double *out_d);
 cudaError_t d3q27_load(lbm_ctx *ctx, const void *src_d, int src_dtype, int aos);
 cudaError_t d3q27_store(lbm_ctx *ctx, void *dst_d, int dst_dtype, int aos);
+
+// blocks of the D3Q27_REF gather kernel: one warp per target cell, four per block (d3q27.cu)
+inline size_t d3q27_gather_blocks(int64_t ntgt) { return (size_t)((ntgt + 3) / 4); }
 
 // reduction finaliser (common.cu): out[k] (+)= sum_b partials[b*ncomp + k], fixed order
 // out[k] (+)= sum over blocks of partials[b][k]; the result is also written to also[k] if given
