@@ -11,7 +11,7 @@ thread_local std::string g_thread_error;
 // out[k] (+)= sum over b of partials[b*ncomp + k] (ncomp <= FIN_MAX): thread t sums the blocks t,
 // t + FIN_THREADS, ... in that order, then a fixed tree over the threads -- the same order on every
 // run, with the loads of many blocks in flight at once.
-constexpr int FIN_THREADS = 1024, FIN_MAX = 4;
+constexpr int FIN_THREADS = 256, FIN_MAX = 4;
 
 __global__ void __launch_bounds__(FIN_THREADS) finalize_kernel(const double *__restrict__ partials, int nblocks,
                                                                int ncomp, double *out, int accumulate, double *also) {

@@ -641,7 +641,8 @@ __device__ __forceinline__ float pull_one(const float *__restrict__ src, const D
     return __ldg(src + (int64_t)j * d.n + sz + (int64_t)d.Z * (sy + (int64_t)d.Y * sx));
 }
 
-constexpr int GATHER_THREADS = 128;  // four target cells per block
+// sixteen target cells per block: fewer per-block force partials for the FP64 finaliser
+constexpr int GATHER_THREADS = 512;
 
 template <int MODE>
 __global__ void __launch_bounds__(GATHER_THREADS) gather_kernel(StepArgs a, GatherArgs g) {
@@ -907,7 +908,7 @@ cudaError_t launch_gather(lbm_ctx *ctx, const StepArgs &a, int mode, double *for
     GatherArgs g = gather_args(ctx);
     const int threads = GATHER_THREADS;
     const unsigned nb = (unsigned)d3q27_gather_blocks(ctx->ntgt);  // one warp per target cell
-    static_assert(GATHER_THREADS == 4 * 32, "d3q27_gather_blocks assumes four warps per block");
+    static_assert(GATHER_THREADS == 16 * 32, "d3q27_gather_blocks assumes sixteen warps per block");
     if (mode != 0)
         gather_kernel<1><<<nb, threads, 0, ctx->stream>>>(a, g);
     else

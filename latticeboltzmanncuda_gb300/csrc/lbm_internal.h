@@ -169,8 +169,8 @@ cudaError_t d3q27_conservation(lbm_ctx *ctx, double *out_d);
 cudaError_t d3q27_load(lbm_ctx *ctx, const void *src_d, int src_dtype, int aos);
 cudaError_t d3q27_store(lbm_ctx *ctx, void *dst_d, int dst_dtype, int aos);
 
-// blocks of the D3Q27_REF gather kernel: one warp per target cell, four per block (d3q27.cu)
-inline size_t d3q27_gather_blocks(int64_t ntgt) { return (size_t)((ntgt + 3) / 4); }
+// blocks of the D3Q27_REF gather kernel: one warp per target cell, sixteen per block (d3q27.cu)
+inline size_t d3q27_gather_blocks(int64_t ntgt) { return (size_t)((ntgt + 15) / 16); }
 
 // reduction finaliser (common.cu): out[k] (+)= sum_b partials[b*ncomp + k], fixed order
 // out[k] (+)= sum over blocks of partials[b][k]; the result is also written to also[k] if given
