@@ -614,13 +614,13 @@ struct GatherArgs {
 // (exact products), read from shared memory: the lanes of a warp index it with different directions,
 // which the constant cache would serve one address at a time
 __device__ __forceinline__ void force_term(float m, const GatherEntry &e, int mode, const float (*cs)[3],
-                                           double acc[3]) {
+                                           float acc[3]) {
     const int k = mode == LBM_FORCE_MOMENTUM_EXCHANGE ? e.slot / 3 : e.slot;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const float kin = k < 27 ? cs[k][a] : 0.0f;
         const float coef = __fsub_rn(cs[e.dst_pop][a], kin);
-        acc[a] += (double)__fmul_rn(m, coef);
+        acc[a] = __fadd_rn(acc[a], __fmul_rn(m, coef));
     }
 }
 
@@ -630,8 +630,11 @@ __device__ __forceinline__ void force_term(float m, const GatherEntry &e, int mo
 // the lanes read up to 32 of the cell's entries at once: each computes its contribution m = val * w
 // and the warp walks them in list order, lane dst_pop adding each one that targets it, so every
 // population takes its adds in the order of the sequential scatter (one rounded add of the rounded
-// product per contribution, as the reference's atomicAdd at SimCalcFuncs.cu:177).  The force terms
-// are summed in FP64 per lane, then over the block in a fixed tree.  Internal cells are zeroed.
+// product per contribution, as the reference's atomicAdd at SimCalcFuncs.cu:177).  The force terms of
+// a target are summed in FP32 by a fixed shuffle tree (the reference accumulates them with FP32
+// atomics), the targets of a block in FP64 in warp order -- few FP64 instructions, which GB300 issues
+// at a small fraction of its FP32 rate -- and the blocks by the FP64 finaliser.  Internal cells are
+// zeroed.
 // Mode 0 writes the result to the target's row of g.gathered, from which the fused kernel, launched
 // next, collides the cell with all the others; mode 1 writes it to the destination lattice.
 __device__ __forceinline__ float pull_one(const float *__restrict__ src, const Dims &d, int64_t c, int x, int y,
@@ -656,9 +659,10 @@ __global__ void __launch_bounds__(GATHER_THREADS) gather_kernel(StepArgs a, Gath
         }
     }
     __syncthreads();
-    const int lane = threadIdx.x & 31;
+    __shared__ double s_force[GATHER_THREADS / 32][3];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;  // target of this warp
-    double facc[3] = {0.0, 0.0, 0.0};
+    float facc[3] = {0.0f, 0.0f, 0.0f};
     if (i < g.ntgt) {  // uniform per warp
         const int64_t c = g.tgt[i];
         const uint8_t fl = a.flags[c];
@@ -672,20 +676,14 @@ __global__ void __launch_bounds__(GATHER_THREADS) gather_kernel(StepArgs a, Gath
             const int k = base + lane;
             float m = 0.0f;
             int dst = 0;
-            double fc[3] = {0.0, 0.0, 0.0};
             if (k < k1) {
                 const GatherEntry e = g.ent[k];
                 const int64_t s = MODE == 0 ? (int64_t)e.src_stream : (int64_t)e.src_cell;
                 const float val = s >= 0 ? __ldg(a.src + (int64_t)e.src_pop * a.d.n + s) : 0.0f;
                 m = __fmul_rn(val, e.w);
                 dst = e.dst_pop;
-                if (g.partials) force_term(m, e, g.force_mode, s_cs, fc);
+                if (g.partials) force_term(m, e, g.force_mode, s_cs, facc);
             }
-            // each lane keeps its own entries' force terms; block_sum below adds them in a fixed tree
-            // (GB300 issues an FP64 instruction per warp at a small fraction of the FP32 rate, so the
-            // additions are spread over the lanes rather than made one after another in one lane)
-#pragma unroll
-            for (int q = 0; q < 3; ++q) facc[q] += fc[q];
             const int cnt = min(32, k1 - base);
             for (int j = 0; j < cnt; ++j) {
                 const float mj = __shfl_sync(0xffffffffu, m, j);
@@ -701,7 +699,20 @@ __global__ void __launch_bounds__(GATHER_THREADS) gather_kernel(StepArgs a, Gath
                 a.dst[(int64_t)lane * a.d.n + c] = v;
         }
     }
-    if (g.partials) block_sum<3>(facc, g.partials + 3 * blockIdx.x);
+    if (g.partials) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) facc[q] = __fadd_rn(facc[q], __shfl_xor_sync(0xffffffffu, facc[q], o));
+            if (lane == 0) s_force[warp][q] = (double)facc[q];
+        }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            double t = 0.0;
+            for (int w = 0; w < GATHER_THREADS / 32; ++w) t += s_force[w][threadIdx.x];
+            g.partials[3 * blockIdx.x + threadIdx.x] = t;
+        }
+    }
 }
 
 // ------------------------------------------------------------------------- separate passes
