@@ -839,6 +839,7 @@ LBM_API lbm_status lbm_batch_step(lbm_batch *b, int32_t nsteps) {
     if (!b) return lbm::set_thread_error(LBM_ERR_INVALID, "null batch");
     if (nsteps < 0) return bfail(b, LBM_ERR_INVALID, "nsteps must be >= 0");
     if (nsteps == 0) return LBM_OK;
+    NvtxRange range("lbm_batch_step");
     BCUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
     // Tuning on a handful of small slots would fix the shape for the mix that follows: the batch
     // keeps the default shape until it holds TUNE_CELLS cells, tunes then, and once more if it

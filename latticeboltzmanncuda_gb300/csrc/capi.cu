@@ -587,6 +587,7 @@ LBM_API lbm_status lbm_step(lbm_ctx *ctx, int32_t nsteps) {
     CHECK_CTX(ctx);
     if (nsteps < 0) return fail(ctx, LBM_ERR_INVALID, "nsteps must be >= 0");
     if (nsteps == 0) return LBM_OK;
+    NvtxRange range(ctx->desc.mode == LBM_D2Q9 ? "lbm_step d2q9" : "lbm_step d3q27_ref");
     lbm_status st = use_device(ctx);
     if (st != LBM_OK) return st;
     if (ctx->desc.mode == LBM_D2Q9) {
@@ -717,6 +718,7 @@ LBM_API lbm_status lbm_set_pipeline_wait(lbm_ctx *ctx, int64_t wait_ns, int32_t 
 
 LBM_API lbm_status lbm_apply(lbm_ctx *ctx, int32_t op) {
     CHECK_CTX(ctx);
+    NvtxRange range("lbm_apply");
     if (ctx->desc.mode != LBM_D3Q27_REF) return fail(ctx, LBM_ERR_UNSUPPORTED, "lbm_apply is D3Q27_REF only");
     if (op != LBM_OP_STREAM && op != LBM_OP_REFLECT && op != LBM_OP_COLLIDE && op != LBM_OP_FLOW)
         return fail(ctx, LBM_ERR_INVALID, "op must be one LBM_OP_* flag");

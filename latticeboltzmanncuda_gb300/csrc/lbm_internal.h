@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <string>
@@ -10,6 +11,15 @@
 #include "lbm_capi.h"
 
 namespace lbm {
+
+// NVTX range for the duration of a scope (steps, batch rounds, server rounds): visible in Nsight
+// Systems / Compute timelines, a no-op without a tool attached
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // D3Q27 directions in the reference's population order (SimCalcFuncs.cu:12, Constants.cpp:6),
 // host copy; the inverse of direction q is the q' with c_q' = -c_q (Constants.cpp:7).

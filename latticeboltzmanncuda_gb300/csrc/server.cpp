@@ -33,6 +33,7 @@
 #include <vector>
 
 #include <cuda_runtime_api.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "lbm_capi.h"
 
@@ -102,6 +103,10 @@ LBM_API const char *lbm_server_last_error(const lbm_server *s) { return s ? s->e
 
 LBM_API lbm_status lbm_server_run(lbm_server *s, const lbm_request *reqs, int64_t n, lbm_request_result *results,
                                   lbm_server_stats *stats) {
+    nvtxRangePushA("lbm_server_run");
+    struct PopRange {
+        ~PopRange() { nvtxRangePop(); }
+    } pop_range;
     if (!s || (n > 0 && (!reqs || !results)))
         return lbm::set_thread_error(LBM_ERR_INVALID, "lbm_server_run: null argument");
     const lbm_server_config &cfg = s->cfg;
