@@ -137,6 +137,8 @@ lbm_status d3_prepare(lbm_ctx *ctx) {
     dfree(ctx, ctx->entries_d, ctx->nent * sizeof(GatherEntry));
     dfree(ctx, ctx->gathered_d, ctx->ntgt * 27 * sizeof(float));
     dfree(ctx, ctx->tgt_index_d, ctx->ntgt ? (size_t)ctx->cells * sizeof(int32_t) : 0);
+    dfree(ctx, ctx->gather_done_d, ctx->ntgt ? 16 : 0);
+    ctx->gather_done_d = nullptr;
     ctx->gathered_d = nullptr;
     ctx->tgt_index_d = nullptr;
     ctx->tgt_cells_d = nullptr;
@@ -156,6 +158,8 @@ lbm_status d3_prepare(lbm_ctx *ctx) {
             return s;
         if ((s = dalloc(ctx, (void **)&ctx->tgt_index_d, (size_t)ctx->cells * sizeof(int32_t), "target index")) != LBM_OK)
             return s;
+        if ((s = dalloc(ctx, (void **)&ctx->gather_done_d, 16, "gather block counter")) != LBM_OK) return s;
+        CUDA_TRY(ctx, cudaMemset(ctx->gather_done_d, 0, 16), "clear gather block counter");
         std::vector<int32_t> index((size_t)ctx->cells, -1);
         for (size_t k = 0; k < tgt.size(); ++k) index[(size_t)tgt[k]] = (int32_t)k;
         CUDA_TRY(ctx, cudaMemcpy(ctx->tgt_index_d, index.data(), index.size() * sizeof(int32_t), cudaMemcpyHostToDevice),
@@ -314,6 +318,7 @@ LBM_API lbm_status lbm_destroy(lbm_ctx *ctx) {
     cudaFree(ctx->entries_d);
     cudaFree(ctx->gathered_d);
     cudaFree(ctx->tgt_index_d);
+    cudaFree(ctx->gather_done_d);
     cudaFree(ctx->induced_d);
     cudaFree(ctx->force_acc_d);
     cudaFree(ctx->scratch.partials);

@@ -608,6 +608,9 @@ struct GatherArgs {
     double *partials;  // 3 per block, or nullptr when no force is accumulated
     int force_mode;
     float *gathered;   // mode 0: the targets' populations out (27 per target)
+    unsigned *done;    // blocks that have written their force partial (the last one finalises; 0 between launches)
+    double *force;     // running force sum (3 doubles), the step's force added by the last block
+    double *force_copy;  // if not null: the running sum after this launch also goes here
 };
 
 // force contribution m * (c_d SPLIT[d] - c_k SPLIT[k]) (SimCalcFuncs.cu:181-183); cs[j][a] = c_ja SPLIT_j
@@ -711,6 +714,34 @@ __global__ void __launch_bounds__(GATHER_THREADS) gather_kernel(StepArgs a, Gath
             double t = 0.0;
             for (int w = 0; w < GATHER_THREADS / 32; ++w) t += s_force[w][threadIdx.x];
             g.partials[3 * blockIdx.x + threadIdx.x] = t;
+            __threadfence();  // the partial is visible device-wide before this block is counted
+        }
+        // the last block to finish adds the partials of all blocks, in a fixed order whichever block
+        // that is: thread t the blocks t, t + GATHER_THREADS, ..., then a tree over the threads
+        __shared__ bool s_last;
+        __shared__ double s_sum[3][GATHER_THREADS];
+        __syncthreads();
+        if (threadIdx.x == 0) s_last = atomicAdd(g.done, 1u) == gridDim.x - 1;
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            for (int q = 0; q < 3; ++q) {
+                double t = 0.0;
+                for (unsigned b = threadIdx.x; b < gridDim.x; b += GATHER_THREADS) t += __ldcg(g.partials + 3 * b + q);
+                s_sum[q][threadIdx.x] = t;
+            }
+            __syncthreads();
+            for (int h = GATHER_THREADS / 2; h > 0; h >>= 1) {
+                if ((int)threadIdx.x < h)
+                    for (int q = 0; q < 3; ++q) s_sum[q][threadIdx.x] += s_sum[q][threadIdx.x + h];
+                __syncthreads();
+            }
+            if (threadIdx.x < 3) {
+                const double v = g.force[threadIdx.x] + s_sum[threadIdx.x][0];
+                g.force[threadIdx.x] = v;
+                if (g.force_copy) g.force_copy[threadIdx.x] = v;
+            }
+            if (threadIdx.x == 0) *g.done = 0;  // ready for the next launch (stream-ordered)
         }
     }
 }
@@ -911,12 +942,16 @@ GatherArgs gather_args(lbm_ctx *ctx) {
     g.partials = ctx->force_on ? ctx->scratch.partials : nullptr;
     g.force_mode = ctx->desc.force_mode;
     g.gathered = ctx->gathered_d;
+    g.done = ctx->gather_done_d;
+    g.force = ctx->force_acc_d;
+    g.force_copy = nullptr;
     return g;
 }
 
 cudaError_t launch_gather(lbm_ctx *ctx, const StepArgs &a, int mode, double *force_copy = nullptr) {
     if (ctx->ntgt == 0) return cudaSuccess;
     GatherArgs g = gather_args(ctx);
+    g.force_copy = force_copy;
     const int threads = GATHER_THREADS;
     const unsigned nb = (unsigned)d3q27_gather_blocks(ctx->ntgt);  // one warp per target cell
     static_assert(GATHER_THREADS == 16 * 32, "d3q27_gather_blocks assumes sixteen warps per block");
@@ -924,9 +959,7 @@ cudaError_t launch_gather(lbm_ctx *ctx, const StepArgs &a, int mode, double *for
         gather_kernel<1><<<nb, threads, 0, ctx->stream>>>(a, g);
     else
         gather_kernel<0><<<nb, threads, 0, ctx->stream>>>(a, g);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess || !g.partials) return e;
-    return finalize_sums(ctx->stream, g.partials, (int)nb, 3, ctx->force_acc_d, true, force_copy);
+    return cudaGetLastError();  // the force, when accumulated, was added by the kernel's last block
 }
 
 // Both equilibrium evaluations on n pseudo-random (rho, u) samples, all directions: counts the

@@ -108,6 +108,7 @@ struct lbm_ctx {
     lbm::GatherEntry *entries_d = nullptr;
     float *gathered_d = nullptr;     // ntgt x 27: the targets' populations after the gather, before collision
     int32_t *tgt_index_d = nullptr;  // per cell: its index in the target list, or -1
+    unsigned *gather_done_d = nullptr;  // blocks of the gather kernel that have written their force partial
     int64_t ntgt = 0, nent = 0;
     float *induced_d = nullptr;      // 27 floats
     bool flow_on = false;
