@@ -142,7 +142,8 @@ struct SlotDescP {  // 56 bytes; pitch, plane, buffers and link words follow fro
     int bits;    // periodic (bits 0-1), force (bit 2), current buffer at the sequence start (bit 3),
                  // shift of the division by the pitch (bits 8-12)
     int stop;    // steps this slot takes in the launch sequence
-    unsigned magic;  // multiplier of the division by the pitch (Granlund-Montgomery)
+    unsigned magic;  // flat tiles: multiplier of the division by the pitch (Granlund-Montgomery)
+    int chunks;      // row-band tiles: column chunks per row band
     float omega, fx, fy, uwx, uwy;
 };
 
@@ -155,14 +156,21 @@ struct BatchParams {
 
 static_assert(sizeof(BatchParams) <= 32764, "kernel parameter block limit");
 
-// Parameter-block tiles are flat: tile j of a slot is the run of blockDim.x * blockDim.y * V
-// consecutive cells starting at j * blockDim.x * blockDim.y * V of the slot's padded cell array
-// [0, pitch * ny), row after row (step_vec_flat), so a row costs at most its 31 padding cells of
-// idle lanes instead of the rest of a column chunk, and only a slot's last tile is ragged.
-// A block finds its slot by a binary search over the slots' first tiles in the parameter block: the
-// loop and its loads are uniform, so the descriptor fields come from the constant bank into uniform
-// registers.  (An 8-byte tile record per block read from global memory instead measured 1-4 %
-// slower with the flat tiles on the serve and batch domains.)
+// Parameter-block tiles.  16-bit storage: flat -- tile j of a slot is the run of blockDim.x *
+// blockDim.y * V consecutive cells starting at j * blockDim.x * blockDim.y * V of the slot's padded
+// cell array [0, pitch * ny), row after row (step_vec_flat), so a row costs at most its 31 padding
+// cells of idle lanes instead of the rest of a column chunk, and only a slot's last tile is ragged.
+// FP32: row bands -- tile j is the column chunk j % chunks of the band of blockDim.y rows j / chunks,
+// each warp one row (step_vec).  Measured on the 512-domain batch: FP16 104.0k against 102.3k MLUPS
+// with row bands, FP32 81.8k against 85.6k with flat tiles.  Either way a block finds its slot by a
+// binary search over the slots' first tiles in the parameter block: the loop and its loads are
+// uniform, so the descriptor fields come from the constant bank.  (An 8-byte tile record per block
+// read from global memory instead measured 1-4 % slower with the flat tiles.)
+template <class S>
+constexpr bool flat_tiles() {
+    return sizeof(S) == 2;
+}
+
 template <class S, int V>
 __device__ __forceinline__ void batch_tile_p(const BatchParams &p, int step, int reverse) {
     const int t = reverse ? p.ntiles - 1 - (int)blockIdx.x : (int)blockIdx.x;
@@ -175,16 +183,25 @@ __device__ __forceinline__ void batch_tile_p(const BatchParams &p, int step, int
     const SlotDescP &D = p.d[slot];
     if (step >= D.stop) return;  // the slot has used its step budget
     const int pitch = (D.nx + 31) & ~31, plane = pitch * D.ny;
-    const int k = (int)threadIdx.y * (int)blockDim.x + (int)threadIdx.x;
-    const int first = tile * (int)(blockDim.x * blockDim.y) * V;
-    if (first + (k & ~31) * V >= plane) return;  // the warp lies past the slot's last cell (uniform)
-    int i = first + k * V;
-    const bool active = i < plane;
-    if (!active) i = plane - V;  // in bounds; shuffles only, no store
-    // i / pitch by multiply-high (pitch >= 32, so the pre-shift is 1)
-    const uint32_t th = __umulhi(D.magic, (uint32_t)i);
-    const int y = (int)((th + (((uint32_t)i - th) >> 1)) >> ((D.bits >> 8) & 31));
-    const int x0 = i - y * pitch;
+    int x0, y;
+    bool active = true;
+    if constexpr (flat_tiles<S>()) {
+        const int k = (int)threadIdx.y * (int)blockDim.x + (int)threadIdx.x;
+        const int first = tile * (int)(blockDim.x * blockDim.y) * V;
+        if (first + (k & ~31) * V >= plane) return;  // the warp lies past the slot's last cell (uniform)
+        int i = first + k * V;
+        active = i < plane;
+        if (!active) i = plane - V;  // in bounds; shuffles only, no store
+        // i / pitch by multiply-high (pitch >= 32, so the pre-shift is 1)
+        const uint32_t th = __umulhi(D.magic, (uint32_t)i);
+        y = (int)((th + (((uint32_t)i - th) >> 1)) >> ((D.bits >> 8) & 31));
+        x0 = i - y * pitch;
+    } else {
+        const int band = tile / D.chunks, xchunk = tile - band * D.chunks;
+        y = band * (int)blockDim.y + (int)threadIdx.y;
+        if (y >= D.ny) return;  // uniform per warp
+        x0 = (xchunk * (int)blockDim.x + (int)threadIdx.x) * V;
+    }
     const int cur = ((D.bits >> 3) + step) & 1;
     S *const a = static_cast<S *>(D.base);
     const S *src = a + (size_t)cur * 9 * plane;
@@ -198,10 +215,17 @@ __device__ __forceinline__ void batch_tile_p(const BatchParams &p, int step, int
     prm.uwy = D.uwy;
     prm.omega_d = prm.fx_d = prm.fy_d = prm.uwx_d = prm.uwy_d = 0.0;  // FP64 storage uses the table path
     const int periodic = D.bits & 3;
-    if (D.bits & 4)
-        d2q9::step_vec_flat<S, V, true, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm, active);
-    else
-        d2q9::step_vec_flat<S, V, false, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm, active);
+    if constexpr (flat_tiles<S>()) {
+        if (D.bits & 4)
+            d2q9::step_vec_flat<S, V, true, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm, active);
+        else
+            d2q9::step_vec_flat<S, V, false, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm, active);
+    } else {
+        if (D.bits & 4)
+            d2q9::step_vec<S, V, true, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm);
+        else
+            d2q9::step_vec<S, V, false, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm);
+    }
 }
 
 // registers held to what the table kernel uses (2-wide 64, 4-wide 85, 8-wide 128): the descriptor
@@ -438,7 +462,9 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
             d.magic = (unsigned)((((uint64_t)1 << 32) * (((uint64_t)1 << l) - (uint64_t)s.pitch)) / (uint64_t)s.pitch + 1);
             d.bits = (s.desc.periodic & 3) | (force ? 4 : 0) | (s.cur ? 8 : 0) | ((l - 1) << 8);
             const int per_tile = b->tx * b->ty * b->v;
-            const int ntile_slot = (int)((s.plane + per_tile - 1) / per_tile);
+            d.chunks = (s.pitch / b->v + b->tx - 1) / b->tx;
+            const int ntile_slot = dsize(b->dtype) == 2 ? (int)((s.plane + per_tile - 1) / per_tile)
+                                                        : d.chunks * ((s.desc.ny + b->ty - 1) / b->ty);
             const D2Q9Params prm = d2q9_params(s.desc);
             d.omega = prm.omega;
             d.fx = prm.fx;

@@ -284,10 +284,11 @@ def test_bulk_protocol_simulation_catches_a_missing_release():
 
 # ------------------------------------------------------------------ batch parameter-block path
 # csrc/batch.cu: slots are one allocation each (buffer A, buffer B: 9 planes of pitch x ny elements
-# each; then pitch x ny uint16 link words; then flags and the fluid count).  Tiles are flat: tile j
-# of a slot covers the tx * ty * V consecutive cells from j * tx * ty * V of the slot's padded cell
-# array, thread k of the block the vector at j * tx * ty * V + k * V (d2q9_vec.cuh: step_vec_flat).
-# A block finds its slot by a binary search over the slots' first tiles.
+# each; then pitch x ny uint16 link words; then flags and the fluid count).  16-bit storage: flat
+# tiles -- tile j of a slot covers the tx * ty * V consecutive cells from j * tx * ty * V of the slot's
+# padded cell array, thread k of the block the vector at j * tx * ty * V + k * V (d2q9_vec.cuh:
+# step_vec_flat).  FP32: row-band tiles -- (slot, band of ty rows, column chunk of tx * V cells).  A
+# block finds its slot by a binary search over the slots' first tiles.
 
 
 def batch_tiles(shapes, V, tx, ty):
@@ -383,7 +384,7 @@ def test_batch_parameter_path_tiles_and_addresses(seed):
     n = int(rng.integers(1, 30))
     shapes = [(int(rng.integers(1, 700)), int(rng.integers(1, 300))) for _ in range(n)]
     shapes += [(1, 1), (32, 1), (33, 3), (64, 5)]
-    for elem, V, tx, ty in ((2, 4, 32, 4), (2, 8, 32, 2), (2, 2, 64, 1), (4, 4, 32, 2), (4, 2, 128, 2), (2, 8, 256, 1)):
+    for elem, V, tx, ty in ((2, 4, 32, 4), (2, 8, 32, 2), (2, 2, 64, 1), (2, 4, 32, 1), (2, 8, 256, 1)):
         tiles, start = batch_tiles(shapes, V, tx, ty)
         # the binary search finds every tile's slot and index within the slot
         for t, rec in enumerate(tiles):
@@ -427,6 +428,71 @@ def test_flat_lane_edges_take_their_own_neighbours():
                     assert lane[a - 1] == lane[a] - 1 and y[a - 1] == y[a] and x0[a - 1] == x0[a] - V
                 if not right[a] and active[a]:
                     assert lane[a + 1] == lane[a] + 1 and y[a + 1] == y[a] and x0[a + 1] == x0[a] + V
+
+
+def band_tiles(shapes, V, tx, ty):
+    """FP32 row-band tiles of rebuild(): (slot, band, xchunk) per tile, and the slots' first tiles."""
+    tiles, start = [], []
+    for k, (nx, ny) in enumerate(shapes):
+        pitch = (nx + 31) // 32 * 32
+        chunks = (pitch // V + tx - 1) // tx
+        start.append(len(tiles))
+        for band in range((ny + ty - 1) // ty):
+            for xc in range(chunks):
+                tiles.append((k, band, xc))
+    return tiles, start
+
+
+def search_band_tile(start, t, chunks):
+    """batch_tile_p's binary search and division for a row-band tile t."""
+    lo, hi = 0, len(start) - 1
+    while lo < hi:
+        mid = (lo + hi + 1) >> 1
+        if start[mid] <= t:
+            lo = mid
+        else:
+            hi = mid - 1
+    i = t - start[lo]
+    return lo, i // chunks[lo], i - (i // chunks[lo]) * chunks[lo]
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_batch_parameter_path_row_bands_fp32(seed):
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(1, 30))
+    shapes = [(int(rng.integers(1, 700)), int(rng.integers(1, 300))) for _ in range(n)]
+    for elem, V, tx, ty in ((4, 4, 32, 2), (4, 2, 128, 2), (4, 4, 64, 1), (4, 2, 32, 8)):
+        tiles, start = band_tiles(shapes, V, tx, ty)
+        chunks = [((nx + 31) // 32 * 32 // V + tx - 1) // tx for nx, _ in shapes]
+        # the binary search finds every tile's slot, band and column chunk
+        for t, rec in enumerate(tiles):
+            assert search_band_tile(start, t, chunks) == rec
+        # every cell of every slot is covered by exactly one (tile, thread row, lane, element)
+        for k, (nx, ny) in enumerate(shapes):
+            pitch = (nx + 31) // 32 * 32
+            plane = pitch * ny
+            pop = 9 * plane * elem
+            alloc = 2 * pop + plane * 2 + ((nx * ny + 7) // 8 * 8 + 8)
+            seen = np.zeros((ny, pitch), int)
+            for (kk, band, xc) in (r for r in tiles if r[0] == k):
+                for ti in range(ty):
+                    y = band * ty + ti
+                    if y >= ny:
+                        continue
+                    x0 = (xc * tx + np.arange(tx)) * V
+                    xa = np.minimum(x0, pitch - V)
+                    for cur in (0, 1):
+                        src = cur * 9 * plane  # elements from the base
+                        dst = (cur ^ 1) * 9 * plane
+                        for base in (src, dst):
+                            offs = base + 8 * plane + y * pitch + xa + V - 1  # the highest plane and element
+                            assert offs.max() * elem < pop * (2 if base else 1)
+                    links = 18 * plane * elem  # byte offset of the link words
+                    assert links == 2 * pop and links + (y * pitch + xa.max() + V) * 2 <= alloc
+                    act = x0 < nx
+                    for x in x0[act]:
+                        seen[y, x:x + V] += 1
+            assert (seen[:, :nx] == 1).all()
 
 
 def test_invariant_division_formula():
