@@ -252,6 +252,10 @@ LBM_API lbm_status lbm_load(lbm_ctx *ctx, const char *path) {
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpy(ctx->f[ctx->cur], pops.get(), pop_bytes, cudaMemcpyHostToDevice);
+    // into the other buffer as well: the D2Q9 step never writes solid cells, so both buffers must
+    // agree there (its fluid cells are overwritten by the next step)
+    if (e == cudaSuccess && ctx->f[ctx->cur ^ 1])
+        e = cudaMemcpy(ctx->f[ctx->cur ^ 1], pops.get(), pop_bytes, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "lbm_load: populations");
     ctx->steps_done = h.steps_done;
     return LBM_OK;

@@ -51,14 +51,29 @@ namespace {
 // ------------------------------------------------------------------------------------------------
 // link words: one pass over the flag bytes
 // ------------------------------------------------------------------------------------------------
+// The step kernels never write a solid cell, so both population buffers must hold the same values
+// there: a solid cell's populations are copied from the current buffer into the other one.
+template <class W>
+__device__ __forceinline__ void copy_cell(const void *cur, void *other, int64_t c, int64_t plane) {
+    const W *a = static_cast<const W *>(cur);
+    W *b = static_cast<W *>(other);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) b[q * plane + c] = a[q * plane + c];
+}
+
 __global__ void build_links_kernel(const uint8_t *__restrict__ flags, uint16_t *__restrict__ links,
-                                   int nx, int ny, int64_t pitch, int periodic) {
+                                   int nx, int ny, int64_t pitch, int periodic, const void *cur, void *other,
+                                   int elem) {
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y;
     if (x >= nx) return;
     int64_t c = (int64_t)y * pitch + x;
     if (flags[(int64_t)y * nx + x] != 0) {
         links[c] = LINK_SOLID;
+        const int64_t plane = pitch * ny;
+        if (elem == 2) copy_cell<uint16_t>(cur, other, c, plane);
+        else if (elem == 4) copy_cell<uint32_t>(cur, other, c, plane);
+        else copy_cell<uint64_t>(cur, other, c, plane);
         return;
     }
     uint16_t L = 0;
@@ -586,7 +601,8 @@ inline dim3 row_grid(const lbm_ctx *ctx, int threads) {
 cudaError_t d2q9_build_links_async(lbm_ctx *ctx, unsigned long long *count_d) {
     const lbm_desc &d = ctx->desc;
     build_links_kernel<<<row_grid(ctx, 256), 256, 0, ctx->stream>>>(ctx->flags_d, ctx->links_d, d.nx, d.ny,
-                                                                    ctx->pitch, d.periodic);
+                                                                    ctx->pitch, d.periodic, ctx->f[ctx->cur],
+                                                                    ctx->f[ctx->cur ^ 1], (int)ctx->elem);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemsetAsync(count_d, 0, sizeof(unsigned long long), ctx->stream);
     if (e != cudaSuccess) return e;
@@ -597,7 +613,8 @@ cudaError_t d2q9_build_links_async(lbm_ctx *ctx, unsigned long long *count_d) {
 cudaError_t d2q9_build_links(lbm_ctx *ctx) {
     const lbm_desc &d = ctx->desc;
     build_links_kernel<<<row_grid(ctx, 256), 256, 0, ctx->stream>>>(ctx->flags_d, ctx->links_d, d.nx, d.ny,
-                                                                    ctx->pitch, d.periodic);
+                                                                    ctx->pitch, d.periodic, ctx->f[ctx->cur],
+                                                                    ctx->f[ctx->cur ^ 1], (int)ctx->elem);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     unsigned long long *cnt = reinterpret_cast<unsigned long long *>(ctx->result_d);

@@ -15,8 +15,8 @@
 // aligned and a multiple of 16 bytes) - and the row's link words, so every population is read from
 // HBM once.  In a row periodic in x, lane 1 reads the wrapped columns (x = nx - 1 for the first
 // strip, x = 0 for the strip holding the last column) into a small per-slot area with plain loads.
-// Bounce-back and solid cells take their own populations 0, 1, 3 from the slot (plane rows of row
-// y) and the others from global memory.
+// Bounce-back takes the cells' own populations 1 and 3 from the slot (plane rows of row y) and
+// the others from global memory; solid cells are not written.
 //
 // Per cell the inputs are those of gather() (d2q9_core.cuh) and the update is finish_row()
 // (d2q9_vec.cuh), so the results are bit-identical to the other D2Q9 kernels.  Plane elements that
@@ -232,14 +232,13 @@ __device__ __forceinline__ void update(const uint16_t *sl, const S *__restrict__
     ld.w[0] = raw_s<S>(wr[3]);  // used by the vector holding the last column of a periodic row only
     ld.w[1] = raw_s<S>(wr[4]);
     ld.w[2] = raw_s<S>(wr[5]);
-    // own populations of row y: planes 0, 1, 3 are staged from row y, the others are read from
-    // global memory at the clamped vector (a vector beyond the row stores nothing)
+    // own populations of row y (raw): planes 0, 1, 3 are staged from row y, the others are read
+    // from global memory at the clamped vector (a vector beyond the row stores nothing)
+    using T = typename RawPack<2 * V>::T;
     const S *mine = src + (int64_t)y * pitch + min(x0, pitch - V);
-    auto own = [&](int q, R (&out)[V]) {
-        if (q == 0 || q == 1 || q == 3)
-            unpack<S, V>(ldsv<V>(sl + q * SEG + lx), out);
-        else
-            ld_pack<S, V>(mine + (int64_t)q * plane, out);
+    auto own = [&](int q) -> T {
+        if (q == 0 || q == 1 || q == 3) return ldsv<V>(sl + q * SEG + lx);
+        return __ldg(reinterpret_cast<const T *>(mine + (int64_t)q * plane));
     };
     finish_row<S, V, FORCE, int, 0>(ld, own, dst, x0, nx, plane, periodic, prm, 0, ld.e, ld.e, lane == 0, lane == 31,
                                     true);

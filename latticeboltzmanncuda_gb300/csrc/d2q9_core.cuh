@@ -270,6 +270,14 @@ __device__ __forceinline__ void ld_pack_pol(const S *__restrict__ p, typename St
     }
 }
 
+template <class T, int POL>
+__device__ __forceinline__ void st_raw_pol(T *__restrict__ p, const T &raw, uint64_t pol) {
+    if constexpr (POL != 1)
+        *p = raw;
+    else
+        st_hint(p, raw, pol);
+}
+
 template <class S, int V, int POL>
 __device__ __forceinline__ void st_pack_pol(S *__restrict__ p, const typename Store<S>::R (&in)[V], uint64_t pol) {
     if constexpr (POL != 1) {

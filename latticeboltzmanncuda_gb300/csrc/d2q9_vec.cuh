@@ -4,9 +4,9 @@
 // lane 0 loads its left neighbour itself (wrapped at x = 0 in a periodic row) and lane 31 its right
 // one.  In a periodic row, the vector holding the last column patches that cell's three values from
 // x = 0.  Cells with bounce-back links take their own opposite population (one extra wide load per
-// population that bounces somewhere in the vector); solid cells copy their own populations, so both
-// A/B buffers keep identical values there.  Elements beyond the last column compute garbage that is
-// stored only into the row padding, which no cell ever reads.
+// population that bounces somewhere in the vector, none for populations 1 and 3, whose own values
+// are loaded for the pull); solid cells are not written (both buffers agree there).  Elements beyond
+// the last column compute garbage that is stored only into the row padding, which no cell ever reads.
 //
 // All 32 lanes of a warp must call step_vec for the same row with consecutive vectors, lane 0
 // holding a vector that starts on a multiple of 32 * V (the shuffles use the full mask): blockDim.x
@@ -112,103 +112,288 @@ __device__ __forceinline__ void load_row(RowLoad<S, V, I> &ld, const S *__restri
     }
 }
 
-// Update the vector of ld and store it to dst.  own(q, out) yields the vector's own population q
-// (bounce-back takes the opposite population of the cell itself; solid cells keep their own).
+// Words of a raw pack: 16-bit storage holds two cells per 32-bit word (cell 2j in the low half).
+template <int NW, class T>
+__device__ __forceinline__ void words(const T &raw, uint32_t (&w)[NW]) {
+    static_assert(sizeof(T) == 4 * NW, "pack size");
+    memcpy(w, &raw, sizeof(w));
+}
+template <class S>
+__device__ __forceinline__ uint32_t raw16(S v) {
+    uint16_t u;
+    memcpy(&u, &v, sizeof(u));
+    return u;
+}
+// (high half of a, low half of b): a pair shifted by one cell across two adjacent words
+__device__ __forceinline__ uint32_t hi_lo(uint32_t a, uint32_t b) { return __byte_perm(a, b, 0x5432); }
+// 0xFFFF in each 16-bit half of a link word whose bit q - 1 is set: the bit is moved to the sign
+// position of byte 0 (byte 2 for the high half) and prmt replicates each sign over its half
+__device__ __forceinline__ uint32_t link_halves(uint32_t lw, int q) {
+    uint32_t m;
+    asm("prmt.b32 %0, %1, 0, 0xAA88;" : "=r"(m) : "r"(lw << (8 - q)));
+    return m;
+}
+// 16-bit storage: bit k of the result is set when cell k of the vector is solid
+template <int NW>
+__device__ __forceinline__ uint32_t solid_cells(const uint32_t (&lw)[NW]) {
+    uint32_t s = 0;
+#pragma unroll
+    for (int j = 0; j < NW; ++j)
+        s |= ((lw[j] & 0xFFFFu) == LINK_SOLID ? 1u : 0u) << (2 * j) | ((lw[j] >> 16) == LINK_SOLID ? 1u : 0u) << (2 * j + 1);
+    return s;
+}
+
+// Update the vector of ld and store it to dst.  own(q) returns the raw pack of the vector's own
+// population q (bounce-back takes the opposite population of the cell itself).  Solid cells are
+// not written: no fluid cell reads their values (a pull from a solid cell is replaced by
+// bounce-back), and both buffers hold the same values there from the initialisation on, so a
+// vector without solid cells is stored whole, a mixed vector cell by cell, an all-solid one not
+// at all.
+//
+// 16-bit storage assembles the pulled populations and applies the bounce-back on the raw pairs:
+// the x-shifted vectors are byte permutes of adjacent words, and a bounce-back is one select per
+// pair under a mask built from the link word.  The arithmetic values are then those of the float
+// path (a raw select followed by the conversion is the conversion followed by the select).
 template <class S, int V, bool FORCE, class I, int POL, class Own>
 __device__ __forceinline__ void finish_row(const RowLoad<S, V, I> &ld, Own own, S *__restrict__ dst, int x0, int nx,
                                            I plane, int periodic, const D2Q9Params &prm, uint64_t pol_st,
                                            const S (&el)[3], const S (&er)[3], bool left_own, bool right_own,
                                            bool active) {
     using R = typename Store<S>::R;
+    using T = typename RowLoad<S, V, I>::T;
     const I r0 = ld.r0;
+    constexpr bool RAW = sizeof(S) == 2 && V % 2 == 0;  // 16-bit storage: the raw-pair path
     R f[9][V];
-    R a1[V], a5[V], a8[V], b3[V], b6[V], b7[V];
-    unpack<S, V>(ld.q0, f[0]);
-    unpack<S, V>(ld.q2, f[2]);
-    unpack<S, V>(ld.q4, f[4]);
-    unpack<S, V>(ld.a1, a1);
-    unpack<S, V>(ld.a5, a5);
-    unpack<S, V>(ld.a8, a8);
-    unpack<S, V>(ld.b3, b3);
-    unpack<S, V>(ld.b6, b6);
-    unpack<S, V>(ld.b7, b7);
-    uint32_t L[V];
-    if constexpr (V == 1) {
-        L[0] = ld.links;
-    } else {
-        uint16_t e[V];
-        memcpy(e, &ld.links, sizeof(e));
+    uint32_t solid = 0;
+    const int kl = nx - 1 - x0;  // the vector's element holding the last column, if in [0, V)
+    if constexpr (RAW) {
+        constexpr int NW = V / 2;
+        uint32_t P[9][NW], A1[NW], A5[NW], A8[NW], B3[NW], B6[NW], B7[NW], LW[NW];
+        words<NW>(ld.q0, P[0]);
+        words<NW>(ld.q2, P[2]);
+        words<NW>(ld.q4, P[4]);
+        words<NW>(ld.a1, A1);
+        words<NW>(ld.a5, A5);
+        words<NW>(ld.a8, A8);
+        words<NW>(ld.b3, B3);
+        words<NW>(ld.b6, B6);
+        words<NW>(ld.b7, B7);
+        words<NW>(ld.links, LW);
+        // +x populations from x - 1: the previous lane's last cell (high half of its last word);
+        // -x populations from x + V: the next lane's first cell (low half of its first word)
+        uint32_t p1 = __shfl_up_sync(0xffffffffu, A1[NW - 1], 1);
+        uint32_t p5 = __shfl_up_sync(0xffffffffu, A5[NW - 1], 1);
+        uint32_t p8 = __shfl_up_sync(0xffffffffu, A8[NW - 1], 1);
+        uint32_t n3 = __shfl_down_sync(0xffffffffu, B3[0], 1);
+        uint32_t n6 = __shfl_down_sync(0xffffffffu, B6[0], 1);
+        uint32_t n7 = __shfl_down_sync(0xffffffffu, B7[0], 1);
+        if (left_own) {
+            p1 = raw16(el[0]) << 16;
+            p5 = raw16(el[1]) << 16;
+            p8 = raw16(el[2]) << 16;
+        }
+        if (right_own) {
+            n3 = raw16(er[0]);
+            n6 = raw16(er[1]);
+            n7 = raw16(er[2]);
+        }
 #pragma unroll
-        for (int k = 0; k < V; ++k) L[k] = e[k];
-    }
-
-    // populations moving +x come from x-1: the previous lane's last element
-    R p1 = __shfl_up_sync(0xffffffffu, a1[V - 1], 1);
-    R p5 = __shfl_up_sync(0xffffffffu, a5[V - 1], 1);
-    R p8 = __shfl_up_sync(0xffffffffu, a8[V - 1], 1);
-    // populations moving -x come from x+V: the next lane's first element
-    R n3 = __shfl_down_sync(0xffffffffu, b3[0], 1);
-    R n6 = __shfl_down_sync(0xffffffffu, b6[0], 1);
-    R n7 = __shfl_down_sync(0xffffffffu, b7[0], 1);
-    if (left_own) {
-        p1 = Store<S>::to(el[0]);
-        p5 = Store<S>::to(el[1]);
-        p8 = Store<S>::to(el[2]);
-    }
-    if (right_own) {
-        n3 = Store<S>::to(er[0]);
-        n6 = Store<S>::to(er[1]);
-        n7 = Store<S>::to(er[2]);
-    }
+        for (int j = 0; j < NW; ++j) {
+            P[1][j] = hi_lo(j == 0 ? p1 : A1[j - 1], A1[j]);
+            P[5][j] = hi_lo(j == 0 ? p5 : A5[j - 1], A5[j]);
+            P[8][j] = hi_lo(j == 0 ? p8 : A8[j - 1], A8[j]);
+            P[3][j] = hi_lo(B3[j], j + 1 < NW ? B3[j + 1] : n3);
+            P[6][j] = hi_lo(B6[j], j + 1 < NW ? B6[j + 1] : n6);
+            P[7][j] = hi_lo(B7[j], j + 1 < NW ? B7[j + 1] : n7);
+        }
+        // periodic row: the last column pulls q = 3, 6, 7 from x = 0
+        if ((periodic & 1) && kl >= 0 && kl < V) {
+            const uint32_t w3 = raw16(ld.w[0]), w6 = raw16(ld.w[1]), w7 = raw16(ld.w[2]);
+            const bool hi = kl & 1;
+            const uint32_t keep = hi ? 0x0000FFFFu : 0xFFFF0000u;
 #pragma unroll
-    for (int k = 0; k < V; ++k) {
-        f[1][k] = k == 0 ? p1 : a1[k - 1];
-        f[5][k] = k == 0 ? p5 : a5[k - 1];
-        f[8][k] = k == 0 ? p8 : a8[k - 1];
-        f[3][k] = k == V - 1 ? n3 : b3[k + 1];
-        f[6][k] = k == V - 1 ? n6 : b6[k + 1];
-        f[7][k] = k == V - 1 ? n7 : b7[k + 1];
-    }
-    // periodic row: the last column pulls q = 3, 6, 7 from x = 0
-    const int kl = nx - 1 - x0;
-    if ((periodic & 1) && kl >= 0 && kl < V) {
-        const R w3 = Store<S>::to(ld.w[0]), w6 = Store<S>::to(ld.w[1]), w7 = Store<S>::to(ld.w[2]);
+            for (int j = 0; j < NW; ++j)
+                if ((kl >> 1) == j) {
+                    P[3][j] = (P[3][j] & keep) | (hi ? w3 << 16 : w3);
+                    P[6][j] = (P[6][j] & keep) | (hi ? w6 << 16 : w6);
+                    P[7][j] = (P[7][j] & keep) | (hi ? w7 << 16 : w7);
+                }
+        }
+        // bounce-back (link bits 0-7 and 16-23 of a word; solid cells have none)
+        uint32_t links = 0;
 #pragma unroll
-        for (int k = 0; k < V; ++k)
-            if (k == kl) {
-                f[3][k] = w3;
-                f[6][k] = w6;
-                f[7][k] = w7;
-            }
-    }
-
-    uint32_t any = 0;
+        for (int j = 0; j < NW; ++j) links |= LW[j];
+        if (links & 0x00FF00FFu) {
 #pragma unroll
-    for (int k = 0; k < V; ++k) any |= L[k];
-    bool solid_any = false;
-    if (any) {
-        const Vec2<R> uw = wall_u<R>(prm);
+            for (int q = 1; q < 9; ++q) {
+                if (links & (0x00010001u << (q - 1))) {
+                    uint32_t O[NW];
+                    // own populations 1 and 3 are the values loaded for the pull (row y)
+                    if (opp(q) == 1) {
 #pragma unroll
-        for (int q = 1; q < 9; ++q) {
-            uint32_t hit = 0;
+                        for (int j = 0; j < NW; ++j) O[j] = A1[j];
+                    } else if (opp(q) == 3) {
 #pragma unroll
-            for (int k = 0; k < V; ++k) hit |= L[k] != LINK_SOLID ? (L[k] >> (q - 1)) & 1u : 0u;
-            if (hit) {
-                R mine[V];
-                own(opp(q), mine);
+                        for (int j = 0; j < NW; ++j) O[j] = B3[j];
+                    } else {
+                        words<NW>(own(opp(q)), O);
+                    }
 #pragma unroll
-                for (int k = 0; k < V; ++k) {
-                    if (L[k] != LINK_SOLID && ((L[k] >> (q - 1)) & 1u)) {
-                        R v = mine[k];
-                        if ((L[k] >> (q + 7)) & 1u) v = add_(v, wall_term<S, R>(q, uw));
-                        f[q][k] = v;
+                    for (int j = 0; j < NW; ++j) {
+                        const uint32_t m = link_halves(LW[j], q);
+                        P[q][j] = (P[q][j] & ~m) | (O[j] & m);
                     }
                 }
             }
         }
+        // moving walls: the wall term on the bounced populations (bit q + 7 with bit q - 1)
+        uint32_t wall = 0;
 #pragma unroll
-        for (int k = 0; k < V; ++k) solid_any |= L[k] == LINK_SOLID;
+        for (int j = 0; j < NW; ++j) wall |= LW[j] & (LW[j] << 8);
+        wall &= 0xFF00FF00u;
+        // collide pair by pair (cells 2j, 2j + 1 on the packed FP32 pipe), the results packed back
+        // into P: at most one pair of cells is held in FP32 at a time
+#pragma unroll
+        for (int j = 0; j < NW; ++j) {
+            float2 h[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                typename Pair<S>::P h2;
+                memcpy(&h2, &P[q][j], sizeof(h2));
+                h[q] = Pair<S>::to(h2);
+            }
+            if (wall) {
+                const Vec2<R> uw = wall_u<R>(prm);
+#pragma unroll
+                for (int q = 1; q < 9; ++q) {
+                    if (wall & (0x01000100u << (q - 1))) {
+                        const R wt = wall_term<S, R>(q, uw);
+                        const uint32_t lw = LW[j];
+                        if ((lw >> (q - 1)) & (lw >> (q + 7)) & 1u) h[q].x = add_(h[q].x, wt);
+                        if ((lw >> (q + 15)) & (lw >> (q + 23)) & 1u) h[q].y = add_(h[q].y, wt);
+                    }
+                }
+            }
+            collide_t<S, float2, FORCE>(h, omega<R>(prm), force<R>(prm));
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                const typename Pair<S>::P h2 = Pair<S>::from(h[q].x, h[q].y);
+                memcpy(&P[q][j], &h2, sizeof(h2));
+            }
+        }
+        if (!active || x0 >= nx) return;  // vector in the row padding (or past the end of a flat tile)
+        solid = solid_cells<NW>(LW);
+        if (solid == 0) {
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                T raw;
+                memcpy(&raw, P[q], sizeof(raw));
+                st_raw_pol<T, POL>(reinterpret_cast<T *>(dst + q * plane + r0 + x0), raw, pol_st);
+            }
+        } else if (solid != (1u << V) - 1) {
+            // mixed vector: the fluid cells one by one
+            uint16_t *d16 = reinterpret_cast<uint16_t *>(dst + r0 + x0);
+#pragma unroll
+            for (int q = 0; q < 9; ++q)
+#pragma unroll
+                for (int k = 0; k < V; ++k)
+                    if (!((solid >> k) & 1u)) d16[q * plane + k] = (uint16_t)(P[q][k >> 1] >> (16 * (k & 1)));
+        }
+        return;
+    } else {
+        R a1[V], a5[V], a8[V], b3[V], b6[V], b7[V];
+        unpack<S, V>(ld.q0, f[0]);
+        unpack<S, V>(ld.q2, f[2]);
+        unpack<S, V>(ld.q4, f[4]);
+        unpack<S, V>(ld.a1, a1);
+        unpack<S, V>(ld.a5, a5);
+        unpack<S, V>(ld.a8, a8);
+        unpack<S, V>(ld.b3, b3);
+        unpack<S, V>(ld.b6, b6);
+        unpack<S, V>(ld.b7, b7);
+        uint32_t L[V];
+        if constexpr (V == 1) {
+            L[0] = ld.links;
+        } else {
+            uint16_t e[V];
+            memcpy(e, &ld.links, sizeof(e));
+#pragma unroll
+            for (int k = 0; k < V; ++k) L[k] = e[k];
+        }
+
+        // populations moving +x come from x-1: the previous lane's last element
+        R p1 = __shfl_up_sync(0xffffffffu, a1[V - 1], 1);
+        R p5 = __shfl_up_sync(0xffffffffu, a5[V - 1], 1);
+        R p8 = __shfl_up_sync(0xffffffffu, a8[V - 1], 1);
+        // populations moving -x come from x+V: the next lane's first element
+        R n3 = __shfl_down_sync(0xffffffffu, b3[0], 1);
+        R n6 = __shfl_down_sync(0xffffffffu, b6[0], 1);
+        R n7 = __shfl_down_sync(0xffffffffu, b7[0], 1);
+        if (left_own) {
+            p1 = Store<S>::to(el[0]);
+            p5 = Store<S>::to(el[1]);
+            p8 = Store<S>::to(el[2]);
+        }
+        if (right_own) {
+            n3 = Store<S>::to(er[0]);
+            n6 = Store<S>::to(er[1]);
+            n7 = Store<S>::to(er[2]);
+        }
+#pragma unroll
+        for (int k = 0; k < V; ++k) {
+            f[1][k] = k == 0 ? p1 : a1[k - 1];
+            f[5][k] = k == 0 ? p5 : a5[k - 1];
+            f[8][k] = k == 0 ? p8 : a8[k - 1];
+            f[3][k] = k == V - 1 ? n3 : b3[k + 1];
+            f[6][k] = k == V - 1 ? n6 : b6[k + 1];
+            f[7][k] = k == V - 1 ? n7 : b7[k + 1];
+        }
+        // periodic row: the last column pulls q = 3, 6, 7 from x = 0
+        if ((periodic & 1) && kl >= 0 && kl < V) {
+            const R w3 = Store<S>::to(ld.w[0]), w6 = Store<S>::to(ld.w[1]), w7 = Store<S>::to(ld.w[2]);
+#pragma unroll
+            for (int k = 0; k < V; ++k)
+                if (k == kl) {
+                    f[3][k] = w3;
+                    f[6][k] = w6;
+                    f[7][k] = w7;
+                }
+        }
+
+        uint32_t any = 0;  // bounce-back bits 0-7 (solid cells have none)
+#pragma unroll
+        for (int k = 0; k < V; ++k) {
+            solid |= (L[k] == LINK_SOLID ? 1u : 0u) << k;
+            any |= L[k];
+        }
+        if (any & 0xFFu) {
+            const Vec2<R> uw = wall_u<R>(prm);
+#pragma unroll
+            for (int q = 1; q < 9; ++q) {
+                if ((any >> (q - 1)) & 1u) {
+                    R mine[V];
+                    if (opp(q) == 1) {
+#pragma unroll
+                        for (int k = 0; k < V; ++k) mine[k] = a1[k];
+                    } else if (opp(q) == 3) {
+#pragma unroll
+                        for (int k = 0; k < V; ++k) mine[k] = b3[k];
+                    } else {
+                        unpack<S, V>(own(opp(q)), mine);
+                    }
+#pragma unroll
+                    for (int k = 0; k < V; ++k) {
+                        if ((L[k] >> (q - 1)) & 1u) {
+                            R v = mine[k];
+                            if ((L[k] >> (q + 7)) & 1u) v = add_(v, wall_term<S, R>(q, uw));
+                            f[q][k] = v;
+                        }
+                    }
+                }
+            }
+        }
     }
+    if constexpr (RAW) return;  // collided and stored above
 
     if constexpr (std::is_same<R, float>::value && V % 2 == 0) {
         // FP32 arithmetic: cells k and k + 1 collide together on the packed FP32 pipe
@@ -237,16 +422,21 @@ __device__ __forceinline__ void finish_row(const RowLoad<S, V, I> &ld, Own own, 
     }
 
     if (!active || x0 >= nx) return;  // vector entirely in the row padding (or past the end of a flat tile)
+    if (solid == 0) {
 #pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        if (solid_any) {
-            R mine[V];
-            own(q, mine);
+        for (int q = 0; q < 9; ++q) st_pack_pol<S, V, POL>(dst + q * plane + r0 + x0, f[q], pol_st);
+    } else if (solid != (1u << V) - 1) {
+        // mixed vector: the fluid cells one by one
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            T raw;
+            pack<S, V>(f[q], raw);
+            S e[V];
+            memcpy(e, &raw, sizeof(e));
 #pragma unroll
             for (int k = 0; k < V; ++k)
-                if (L[k] == LINK_SOLID) f[q][k] = mine[k];
+                if (!((solid >> k) & 1u)) dst[q * plane + r0 + x0 + k] = e[k];
         }
-        st_pack_pol<S, V, POL>(dst + q * plane + r0 + x0, f[q], pol_st);
     }
 }
 
@@ -260,7 +450,8 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
     load_row<S, V, I, POL>(ld, src, links, x0, y, nx, ny, pitch, plane, periodic, pol_ld);
     // own populations at the clamped xa (equal to x0 for every vector that is stored)
     const S *mine = src + ld.r0 + ld.xa;
-    auto own = [&](int q, typename Store<S>::R (&out)[V]) { ld_pack<S, V>(mine + q * plane, out); };
+    using T = typename RowLoad<S, V, I>::T;
+    auto own = [&](int q) { return __ldg(reinterpret_cast<const T *>(mine + q * plane)); };
     const int lane = threadIdx.x & 31;
     finish_row<S, V, FORCE, I, POL>(ld, own, dst, x0, nx, plane, periodic, prm, pol_st, ld.e, ld.e, lane == 0,
                                     lane == 31, true);
@@ -334,7 +525,8 @@ __device__ __forceinline__ void step_vec_flat(const S *__restrict__ src, S *__re
     RowLoad<S, V, I> ld;
     load_row_flat<S, V, I>(ld, src, links, x0, y, nx, ny, pitch, plane, periodic, left_own, right_own);
     const S *mine = src + ld.r0 + x0;
-    auto own = [&](int q, typename Store<S>::R (&out)[V]) { ld_pack<S, V>(mine + q * plane, out); };
+    using T = typename RowLoad<S, V, I>::T;
+    auto own = [&](int q) { return __ldg(reinterpret_cast<const T *>(mine + q * plane)); };
     finish_row<S, V, FORCE, I, 0>(ld, own, dst, x0, nx, plane, periodic, prm, 0, ld.e, ld.er, left_own, right_own,
                                   active);
 }

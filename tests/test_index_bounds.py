@@ -47,7 +47,7 @@ def thread_offsets(nx, ny, pitch, V, x0, y, lane, periodic):
     for q in range(9):
         for k in range(V):
             pop.append(q * plane + r0 + xa + k)
-    # solid copies and stores, only for vectors that start inside the row
+    # stores (fluid cells), only for vectors that start inside the row
     act = x0 < nx
     for q in range(9):
         for k in range(V):
@@ -338,7 +338,7 @@ def flat_thread_offsets(nx, ny, pitch, V, x0, y, lane, periodic, active):
     for q, r in {0: r0, 2: rm, 4: rp, 1: r0, 5: rm, 8: rp, 3: r0, 6: rm, 7: rp}.items():
         for k in range(V):
             pop.append(q * plane + r + x0 + k)
-            pop.append(q * plane + r0 + x0 + k)  # own populations (bounce-back, solid copies)
+            pop.append(q * plane + r0 + x0 + k)  # own populations (bounce-back)
     for k in range(V):
         lnk.append(r0 + x0 + k)
     left = (lane == 0) | (x0 == 0)
@@ -409,7 +409,7 @@ def test_batch_parameter_path_tiles_and_addresses(seed):
                 st = active & (x0 < nx)
                 for e in range(V):
                     np.add.at(seen, (y[st], x0[st] + e), 1)
-            # every cell of every slot is stored by exactly one lane
+            # every cell of every slot belongs to exactly one storing lane (which skips solid cells)
             assert (seen[:, :nx] == 1).all(), (nx, ny, V, tx, ty)
 
 
