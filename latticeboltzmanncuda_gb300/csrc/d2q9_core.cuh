@@ -59,7 +59,9 @@ __device__ __forceinline__ float2 fma_(float2 a, float2 b, float2 c) { return __
 __device__ __forceinline__ float2 mul_(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 add_(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 neg_(float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ float2 sub_(float2 a, float2 b) { return __fadd2_rn(a, neg_(b)); }
+// a - b as a + b * (-1): the product is exact, so the one rounding gives a - b (a packed negation
+// would cost an instruction of its own)
+__device__ __forceinline__ float2 sub_(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
 
 // lane type of an arithmetic type, and a uniform value broadcast to every lane
 template <class T>
@@ -475,30 +477,32 @@ __device__ __forceinline__ void collide_t(T h[9], typename Lane<T>::R om, Vec2<t
         ux = mul_(mx, inv);
         uy = mul_(my, inv);
     }
-    const T usq = mul_(B((R)1.5), fma_(ux, ux, mul_(uy, uy)));
+    // -1.5 u^2 (negated products are exact, so every expression below equals the one with the
+    // negation written out)
+    const T nusq = mul_(B((R)-1.5), fma_(ux, ux, mul_(uy, uy)));
     const T om1 = B(sub_((R)1, om));
     const T omv = B(om);
     const T om_s_drho = mul_(omv, mul_(B(s), drho));
     const T om_s_rho = mul_(omv, mul_(B(s), rho));
     const T om_s_rho3 = mul_(B((R)3), om_s_rho);
     R pre = 0, pre3 = 0;
-    T uF3 = B((R)0);
+    T nuF3 = B((R)0);  // -3 u.F
     if (FORCE) {
         pre = mul_(s, fma_((R)-0.5, om, (R)1));
         pre3 = mul_((R)3, pre);
-        uF3 = mul_(B((R)3), fma_(ux, B(F.x), mul_(uy, B(F.y))));
+        nuF3 = mul_(B((R)-3), fma_(ux, B(F.x), mul_(uy, B(F.y))));
     }
     // rest population: h0eq = s (drho - rho usq), forcing s (1 - om/2) (-3 u.F)
     {
-        T a = fma_(neg_(om_s_rho), usq, om_s_drho);
-        if (FORCE) a = fma_(B(-pre), uF3, a);
+        T a = fma_(om_s_rho, nusq, om_s_drho);
+        if (FORCE) a = fma_(B(pre), nuF3, a);
         h[0] = fma_(om1, h[0], a);
     }
     auto pair = [&](int q, int qb, T cu, R cF) {
-        T a = fma_(om_s_rho, fma_(mul_(B((R)4.5), cu), cu, neg_(usq)), om_s_drho);
+        T a = fma_(om_s_rho, fma_(mul_(B((R)4.5), cu), cu, nusq), om_s_drho);
         T b = mul_(om_s_rho3, cu);
         if (FORCE) {
-            a = fma_(B(pre), fma_(mul_(B((R)9), cu), B(cF), neg_(uF3)), a);
+            a = fma_(B(pre), fma_(mul_(B((R)9), cu), B(cF), nuF3), a);
             b = fma_(B(pre3), B(cF), b);
         }
         h[q] = fma_(om1, h[q], add_(a, b));
