@@ -422,13 +422,17 @@ struct is_half_store<__nv_bfloat16> : std::true_type {};
 // (h = s f / w, w_0 = 16 w_d, w_axis = 4 w_d) is  h_d += 4 r_0 + 2 (r_a + r_b)  with a, b the axis
 // populations with c_a + c_b = c_d.  What remains is the diagonals' own rounding, whose absolute
 // resolution is 4x (momentum) and 16x (mass) finer.
+// With `packed` (float2 only), the stored pairs of populations 0-4 are also returned: packing the
+// rounded values again would give the same words.
 template <class S, class T>
-__device__ __forceinline__ void conserve_rounding(T h[9]) {
+__device__ __forceinline__ void conserve_rounding(T h[9], uint32_t *packed = nullptr) {
     T r[5];
     if constexpr (std::is_same<T, float2>::value) {
 #pragma unroll
         for (int q = 0; q < 5; ++q) {  // the two cells' values of population q round-trip together
-            const float2 hr = Pair<S>::to(Pair<S>::from(h[q].x, h[q].y));
+            const typename Pair<S>::P p = Pair<S>::from(h[q].x, h[q].y);
+            if (packed) memcpy(&packed[q], &p, sizeof(p));
+            const float2 hr = Pair<S>::to(p);
             r[q] = sub_(h[q], hr);
             h[q] = hr;
         }
@@ -461,7 +465,8 @@ __device__ __forceinline__ void conserve_rounding(T h[9]) {
 // the force and what depends only on them -- are computed in R and broadcast, which gives every
 // lane the scalar path's values).
 template <class S, class T, bool FORCE>
-__device__ __forceinline__ void collide_t(T h[9], typename Lane<T>::R om, Vec2<typename Lane<T>::R> F) {
+__device__ __forceinline__ void collide_t(T h[9], typename Lane<T>::R om, Vec2<typename Lane<T>::R> F,
+                                          uint32_t *packed = nullptr) {
     using R = typename Lane<T>::R;
     auto B = [](R c) { return Lane<T>::bc(c); };
     constexpr R s = hscale<S, R>();
@@ -512,7 +517,7 @@ __device__ __forceinline__ void collide_t(T h[9], typename Lane<T>::R om, Vec2<t
     pair(2, 4, uy, F.y);
     pair(5, 7, add_(ux, uy), add_(F.x, F.y));
     pair(8, 6, sub_(ux, uy), sub_(F.x, F.y));
-    if constexpr (is_half_store<S>::value) conserve_rounding<S, T>(h);
+    if constexpr (is_half_store<S>::value) conserve_rounding<S, T>(h, packed);
 }
 
 template <class S, class R, bool FORCE>

@@ -274,9 +274,12 @@ __device__ __forceinline__ void finish_row(const RowLoad<S, V, I> &ld, Own own, 
                     }
                 }
             }
-            collide_t<S, float2, FORCE>(h, omega<R>(prm), force<R>(prm));
+            uint32_t rounded[5];  // populations 0-4 come back packed from the conservative rounding
+            collide_t<S, float2, FORCE>(h, omega<R>(prm), force<R>(prm), rounded);
 #pragma unroll
-            for (int q = 0; q < 9; ++q) {
+            for (int q = 0; q < 5; ++q) P[q][j] = rounded[q];
+#pragma unroll
+            for (int q = 5; q < 9; ++q) {
                 const typename Pair<S>::P h2 = Pair<S>::from(h[q].x, h[q].y);
                 memcpy(&P[q][j], &h2, sizeof(h2));
             }
