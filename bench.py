@@ -66,7 +66,7 @@ def parse():
     ap.add_argument("--d3-steps", type=int, default=100)
     ap.add_argument("--d3-modes", default="float_float,fp64,fp32",
                     help="equilibrium evaluations timed by --workload d3q27 (comma separated)")
-    ap.add_argument("--workload", default="channel", choices=["channel", "batch", "serve", "tgv", "d3q27"],
+    ap.add_argument("--workload", default="channel", choices=["channel", "batch", "serve", "tgv", "d3q27", "persistent"],
                     help="channel: the headline single-domain solve; batch: 512 uneven domains; "
                          "serve: Poisson request streams through the continuous-batching server; "
                          "tgv: Taylor-Green precision runs per storage type")
@@ -880,6 +880,44 @@ def run_d3q27_reference(args):
     return 0
 
 
+def run_persistent(args):
+    """Small batches (1 to 64 domains of 64^2 to 256^2 cells, FP16-shifted storage), where launching
+    every step costs more than the step: step sequences of --round-steps steps as one launch per
+    step against one persistent launch per sequence, time per step and aggregate MLUPS of each."""
+    import torch
+    import latticeboltzmanncuda_gb300 as lbm
+    from latticeboltzmanncuda_gb300 import workloads
+
+    stream = torch.cuda.Stream()
+    seq = args.round_steps
+    rows = []
+    for count in (1, 4, 16, 64):
+        doms = workloads.small_batch(count, SEED)
+        cells = sum(d.nx * d.ny for d in doms)
+        row = {"slots": count, "cells": cells}
+        for mode, name in ((0, "launch_per_step"), (2, "persistent")):
+            with lbm.Batch("f16s", stream=stream.cuda_stream) as B:
+                B.set_persistent(mode)
+                for d in doms:
+                    B.add(d.nx, d.ny, d.tau, d.flags, d.periodic, d.body_force, d.wall_velocity)
+                for _ in range(max(args.warmup, 1)):
+                    B.step(seq)
+                B.synchronize()
+                nseq = max(1, int(round(4000 / seq)))
+                t = _timed(stream, lambda: [B.step(seq) for _ in range(nseq)])
+                B.synchronize()
+            steps = nseq * seq
+            row[name] = {"us_per_step": round(1e6 * t / steps, 3), "mlups": round(cells * steps / t / 1e6, 1)}
+        row["speedup"] = round(row["persistent"]["mlups"] / row["launch_per_step"]["mlups"], 3)
+        rows.append(row)
+    print(json.dumps({"metric": "aggregate MLUPS, persistent vs one launch per step", "workload": "persistent",
+                      "unit": "MLUPS", "higher_is_better": True, "data": "synthetic", "dtype": "f16s",
+                      "config": {"workload": f"small D2Q9 batches (area log-uniform in [64^2, 256^2], seed {SEED}), "
+                                             f"sequences of {seq} steps", "steps": 4000},
+                      "value": rows[-1]["persistent"]["mlups"], "rows": rows}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference" and args.workload == "d3q27":
@@ -894,6 +932,8 @@ def main():
         return run_tgv(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "persistent":
+        return run_persistent(args)
     return run_mine(args)
 
 

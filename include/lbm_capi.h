@@ -265,7 +265,8 @@ LBM_API lbm_status lbm_checkpoint_desc(const char *path, lbm_desc *out);
 
 /* ---------------------------------------------------------------- batched domains */
 /* Many independent D2Q9 domains ("slots": own size, tau, force, wall velocity, periodicity and
- * flags) advanced together, one kernel launch per time step for all live slots.  No counterpart
+ * flags) advanced together, one kernel launch per time step for all live slots (small batches: one
+ * persistent launch per step sequence, see lbm_batch_set_persistent).  No counterpart
  * in the reference, which runs one lattice per process; each slot computes exactly what a
  * single-domain context with the same descriptor computes (bit-identical populations).  Slots
  * are added (allocated, flags set, equilibrium rho = 1, u = 0) and removed between steps;
@@ -295,7 +296,18 @@ LBM_API lbm_status lbm_batch_autotune(lbm_batch *b);
 LBM_API lbm_status lbm_batch_tunings(lbm_batch *b, int32_t *count);
 LBM_API lbm_status lbm_batch_set_launch(lbm_batch *b, int32_t cells_per_thread, int32_t block_threads,
                                         int32_t rows_per_block);
+/* Waits for the batch stream; LBM_ERR_TIMEOUT when a persistent launch (below) gave up waiting for
+ * its blocks since the last call (the slots' populations are then not valid). */
 LBM_API lbm_status lbm_batch_synchronize(lbm_batch *b);
+/* Persistent launches: a step sequence of lbm_batch_step (two steps or more) runs as one
+ * cooperative launch whose blocks meet after each step, instead of one launch per step.  With
+ * 4-wide tiles (the default shape of batches below the tuning threshold), for FP32 and 16-bit
+ * storage.  mode 0: never; 1 (default): batches of at most 2^21 live cells, where a launch per step
+ * costs more than the step; 2: whenever the shape allows.  Each meeting waits at most wait_ns
+ * (default 1e9) for the other blocks, then the launch ends and lbm_batch_synchronize reports
+ * LBM_ERR_TIMEOUT.  skip_block >= 0 is a diagnostic: that block does not arrive at the first
+ * meeting, so the wait runs out (no counterpart in the reference). */
+LBM_API lbm_status lbm_batch_set_persistent(lbm_batch *b, int32_t mode, int64_t wait_ns, int32_t skip_block);
 LBM_API lbm_status lbm_batch_get_stream(lbm_batch *b, void **stream);
 /* out: live slots, cells, fluid cells, device bytes of the slots, cells per thread, block width,
  * rows per block, tiles per step */

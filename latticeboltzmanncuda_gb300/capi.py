@@ -146,6 +146,7 @@ SIGNATURES = [
     ("lbm_batch_tunings", _S, [_P, _P]),
     ("lbm_batch_set_launch", _S, [_P, _I32, _I32, _I32]),
     ("lbm_batch_synchronize", _S, [_P]),
+    ("lbm_batch_set_persistent", _S, [_P, _I32, _I64, _I32]),
     ("lbm_batch_get_stream", _S, [_P, _P]),
     ("lbm_batch_info", _S, [_P, _P]),
     ("lbm_batch_slot_steps", _S, [_P, _I32, _P]),

@@ -171,9 +171,10 @@ constexpr bool flat_tiles() {
     return sizeof(S) == 2;
 }
 
-template <class S, int V>
-__device__ __forceinline__ void batch_tile_p(const BatchParams &p, int step, int reverse) {
-    const int t = reverse ? p.ntiles - 1 - (int)blockIdx.x : (int)blockIdx.x;
+// Tile t of the launch sequence's step `step` (POL 3: the loads at L2, coherent with the stores of
+// the previous step in the same launch).
+template <class S, int V, int POL = 0>
+__device__ __forceinline__ void batch_tile_p(const BatchParams &p, int t, int step) {
     int lo = 0, hi = p.n - 1;
     while (lo < hi) {  // the last slot whose first tile is at or before t (uniform per block)
         const int mid = (lo + hi + 1) >> 1;
@@ -217,14 +218,16 @@ __device__ __forceinline__ void batch_tile_p(const BatchParams &p, int step, int
     const int periodic = D.bits & 3;
     if constexpr (flat_tiles<S>()) {
         if (D.bits & 4)
-            d2q9::step_vec_flat<S, V, true, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm, active);
+            d2q9::step_vec_flat<S, V, true, int, POL>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm,
+                                                      active);
         else
-            d2q9::step_vec_flat<S, V, false, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm, active);
+            d2q9::step_vec_flat<S, V, false, int, POL>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm,
+                                                       active);
     } else {
         if (D.bits & 4)
-            d2q9::step_vec<S, V, true, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm);
+            d2q9::step_vec<S, V, true, int, POL>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm);
         else
-            d2q9::step_vec<S, V, false, int>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm);
+            d2q9::step_vec<S, V, false, int, POL>(src, dst, links, x0, y, D.nx, D.ny, pitch, plane, periodic, prm);
     }
 }
 
@@ -232,16 +235,83 @@ __device__ __forceinline__ void batch_tile_p(const BatchParams &p, int step, int
 // fields read from the parameter block otherwise stay in registers and cost occupancy
 __host__ __device__ constexpr int batch_min_blocks(int v) { return v == 8 ? 2 : (v == 4 ? 3 : 4); }
 
+__device__ __forceinline__ int launch_tile(int ntiles, int reverse) {
+    return reverse ? ntiles - 1 - (int)blockIdx.x : (int)blockIdx.x;
+}
+
 template <class S, int V>
 __global__ void __launch_bounds__(256, batch_min_blocks(V)) batch_step_kernel_p(const __grid_constant__ BatchParams p,
                                                                                int step, int reverse) {
-    batch_tile_p<S, V>(p, step, reverse);
+    batch_tile_p<S, V>(p, launch_tile(p.ntiles, reverse), step);
 }
 
 template <class S, int V>
 __global__ void __launch_bounds__(256, 4) batch_step_kernel_p_occ(const __grid_constant__ BatchParams p, int step,
                                                                   int reverse) {
-    batch_tile_p<S, V>(p, step, reverse);
+    batch_tile_p<S, V>(p, launch_tile(p.ntiles, reverse), step);
+}
+
+// Persistent launch: one cooperative launch runs a whole step sequence.  Its blocks (no more than
+// fit on the GPU at once) take the step's tiles b, b + gridDim.x, ... and then meet all other
+// blocks before the next step, whose loads go to L2 (the previous step's stores of other SMs are
+// there, while this SM's L1 may hold lines of the buffer from two steps ago).  For batches of few
+// cells, where one launch per step costs more than the step itself.
+struct GridSync {
+    unsigned int arrived;  // block arrivals since the launch began
+    unsigned int status;   // nonzero: a block gave up waiting for the others
+};
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Every block of the launch arrives; the first thread of each then waits until `target` arrivals
+// are counted, at most limit_ns (then it records the failure in g->status, and every block that
+// sees it ends its launch).  `skip`: the block does not arrive (a diagnostic of the wait limit).
+// Returns false when the sequence must stop.
+__device__ bool grid_meet(GridSync *g, unsigned target, int64_t limit_ns, bool skip) {
+    __shared__ int ok;  // the first thread's verdict, the same for the whole block
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        __threadfence();  // this block's stores before its arrival
+        if (!skip) atomicAdd(&g->arrived, 1u);
+        const uint64_t t0 = global_ns();
+        volatile unsigned *arrived = &g->arrived, *status = &g->status;
+        while (*arrived < target && *status == 0) {
+            if ((int64_t)(global_ns() - t0) > limit_ns) {
+                atomicOr(&g->status, 1u);
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();  // the other blocks' stores before this block's next loads
+        ok = *status == 0;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// registers held to 128 (the step-loop state comes on top of the tile's; a batch that runs
+// persistent is small, so occupancy counts less than spills)
+template <class S>
+constexpr int persist_min_blocks() {
+    return 2;
+}
+
+template <class S>
+__global__ void __launch_bounds__(256, persist_min_blocks<S>())
+    batch_persistent_kernel(const __grid_constant__ BatchParams p, int nsteps, int sweep0, GridSync *g,
+                            int64_t limit_ns, int skip_block) {
+    for (int s = 0; s < nsteps; ++s) {
+        const int reverse = (sweep0 + s) & 1;
+        for (int b = (int)blockIdx.x; b < p.ntiles; b += (int)gridDim.x)
+            batch_tile_p<S, 4, 3>(p, reverse ? p.ntiles - 1 - b : b, s);
+        if (s + 1 < nsteps &&
+            !grid_meet(g, (unsigned)(s + 1) * gridDim.x, limit_ns, s == 0 && (int)blockIdx.x == skip_block))
+            return;
+    }
 }
 
 size_t dsize(int dtype) { return dtype == LBM_F64 ? 8 : (dtype == LBM_F32 ? 4 : 2); }
@@ -287,6 +357,14 @@ struct lbm_batch {
     bool use_params = false;             // the launch takes the descriptors in its parameter block
     BatchParams params{};
     int64_t next_ticket = 1;
+    // persistent launches: mode (0 never, 1 batches of at most PERSIST_CELLS live cells, 2 whenever
+    // the launch allows it), the limit of their waits, a block that does not arrive (diagnostic)
+    int persist = 1;
+    int64_t persist_wait_ns = 1000000000;
+    int persist_skip = -1;
+    GridSync *sync_d = nullptr;
+    bool sync_d_init = false;
+    int persist_launches = 0;  // persistent launches so far (lbm_batch_info)
 };
 
 namespace {
@@ -545,6 +623,55 @@ cudaError_t launch_v(lbm_batch *b, int step, int reverse) {
     return cudaGetLastError();
 }
 
+// batches of at most this many live cells run a step sequence as one persistent launch
+constexpr int64_t PERSIST_CELLS = (int64_t)1 << 21;
+
+bool persistent_ok(const lbm_batch *b, int nsteps) {
+    if (!b->use_params || b->v != 4 || nsteps < 2 || b->persist == 0) return false;
+    return b->persist == 2 || b->live_cells <= PERSIST_CELLS;
+}
+
+template <class S>
+cudaError_t launch_persistent_t(lbm_batch *b, int nsteps) {
+    if constexpr (sizeof(S) > 4) {
+        return cudaErrorInvalidValue;
+    } else {
+        const dim3 block(b->tx, b->ty);
+        int per_sm = 0, sms = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_persistent_kernel<S>,
+                                                                      (int)(block.x * block.y), 0);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) return cudaErrorInvalidConfiguration;
+        const int grid = std::min(b->ntiles, per_sm * sms);  // every block resident at once
+        // arrivals from zero; the status word keeps a failure until lbm_batch_synchronize reads it
+        e = cudaMemsetAsync(&b->sync_d->arrived, 0, sizeof(unsigned int), b->stream);
+        if (e != cudaSuccess) return e;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = block;
+        cfg.stream = b->stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, batch_persistent_kernel<S>, b->params, nsteps, (int)(b->sweep & 1u), b->sync_d,
+                               b->persist_wait_ns, b->persist_skip);
+        if (e == cudaSuccess) ++b->persist_launches;
+        return e;
+    }
+}
+
+cudaError_t launch_persistent(lbm_batch *b, int nsteps) {
+    switch (b->dtype) {
+        case LBM_F32: return launch_persistent_t<float>(b, nsteps);
+        case LBM_F16S: return launch_persistent_t<__half>(b, nsteps);
+        case LBM_BF16S: return launch_persistent_t<__nv_bfloat16>(b, nsteps);
+    }
+    return cudaErrorInvalidValue;
+}
+
 template <class S>
 cudaError_t launch(lbm_batch *b, int step, int reverse) {
     if constexpr (vec_ok<S>(2)) {
@@ -712,6 +839,7 @@ LBM_API lbm_status lbm_batch_destroy(lbm_batch *b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     cudaFree(b->desc_d);
     cudaFree(b->tiles_d);
+    cudaFree(b->sync_d);
     cudaFree(b->staging);
     cudaFree(b->result_d);
     for (PinnedBlock &pb : b->pinned) {
@@ -880,7 +1008,17 @@ LBM_API lbm_status lbm_batch_step(lbm_batch *b, int32_t nsteps) {
     lbm_status st = rebuild(b, nsteps);
     if (st != LBM_OK) return st;
     if (b->ntiles > 0) {
-        for (int s = 0; s < nsteps; ++s) {
+        bool done = false;
+        if (persistent_ok(b, nsteps)) {
+            if (!b->sync_d) BCUDA(b, cudaMalloc(&b->sync_d, sizeof(GridSync)), "batch: grid sync word");
+            if (!b->sync_d_init) {
+                BCUDA(b, cudaMemsetAsync(b->sync_d, 0, sizeof(GridSync), b->stream), "batch: grid sync word");
+                b->sync_d_init = true;
+            }
+            BCUDA(b, launch_persistent(b, nsteps), "batch persistent launch");
+            done = true;
+        }
+        for (int s = 0; !done && s < nsteps; ++s) {
             BCUDA(b, launch_any(b, s, (int)((b->sweep + s) & 1)), "batch step");
         }
     }
@@ -908,6 +1046,26 @@ LBM_API lbm_status lbm_batch_set_slot_steps(lbm_batch *b, int32_t slot, int64_t 
 LBM_API lbm_status lbm_batch_synchronize(lbm_batch *b) {
     if (!b) return lbm::set_thread_error(LBM_ERR_INVALID, "null batch");
     BCUDA(b, cudaStreamSynchronize(b->stream), "batch synchronize");
+    if (b->sync_d) {
+        unsigned int status = 0;
+        BCUDA(b, cudaMemcpy(&status, &b->sync_d->status, sizeof(status), cudaMemcpyDeviceToHost), "batch synchronize");
+        if (status) {
+            BCUDA(b, cudaMemset(&b->sync_d->status, 0, sizeof(status)), "batch synchronize");
+            return bfail(b, LBM_ERR_TIMEOUT,
+                         "batch: a persistent launch gave up waiting for its blocks; the slots' populations are "
+                         "not valid");
+        }
+    }
+    return LBM_OK;
+}
+
+LBM_API lbm_status lbm_batch_set_persistent(lbm_batch *b, int32_t mode, int64_t wait_ns, int32_t skip_block) {
+    if (!b) return lbm::set_thread_error(LBM_ERR_INVALID, "null batch");
+    if (mode < 0 || mode > 2) return bfail(b, LBM_ERR_INVALID, "lbm_batch_set_persistent: mode must be 0, 1 or 2");
+    if (wait_ns <= 0) return bfail(b, LBM_ERR_INVALID, "lbm_batch_set_persistent: wait_ns must be > 0");
+    b->persist = mode;
+    b->persist_wait_ns = wait_ns;
+    b->persist_skip = skip_block;
     return LBM_OK;
 }
 

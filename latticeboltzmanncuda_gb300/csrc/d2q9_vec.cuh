@@ -53,12 +53,24 @@ struct RowLoad {
     int xa;
 };
 
+// POL 0: read-only path; 1, 2: read-only path with an L2 eviction hint; 3: loads at L2 (`.cg`),
+// coherent with the stores of other blocks earlier in the same kernel (the persistent batch
+// kernel, whose steps follow one another inside one launch)
 template <class T, int POL>
 __device__ __forceinline__ T ld_raw(const T *p, uint64_t pol) {
     if constexpr (POL == 0)
         return __ldg(p);
+    else if constexpr (POL == 3)
+        return __ldcg(p);
     else
         return ld_hint<T>(p, pol);
+}
+template <int POL, class T>
+__device__ __forceinline__ T ld_one(const T *p) {
+    if constexpr (POL == 3)
+        return __ldcg(p);
+    else
+        return __ldg(p);
 }
 
 template <class S, int V, class I, int POL>
@@ -95,20 +107,20 @@ __device__ __forceinline__ void load_row(RowLoad<S, V, I> &ld, const S *__restri
         // from the clamped xa: a warp lying wholly beyond the row must not address past it
         int xm = xa - 1;
         if (xm < 0) xm = (periodic & 1) ? nx - 1 : 0;  // unused (bounce-back) when not periodic
-        ld.e[0] = __ldg(src + 1 * plane + r0 + xm);
-        ld.e[1] = __ldg(src + 5 * plane + rm + xm);
-        ld.e[2] = __ldg(src + 8 * plane + rp + xm);
+        ld.e[0] = ld_one<POL>(src + 1 * plane + r0 + xm);
+        ld.e[1] = ld_one<POL>(src + 5 * plane + rm + xm);
+        ld.e[2] = ld_one<POL>(src + 8 * plane + rp + xm);
     } else if (lane == 31) {
         const int xq = min(x0 + V, (int)pitch - 1);
-        ld.e[0] = __ldg(src + 3 * plane + r0 + xq);
-        ld.e[1] = __ldg(src + 6 * plane + rm + xq);
-        ld.e[2] = __ldg(src + 7 * plane + rp + xq);
+        ld.e[0] = ld_one<POL>(src + 3 * plane + r0 + xq);
+        ld.e[1] = ld_one<POL>(src + 6 * plane + rm + xq);
+        ld.e[2] = ld_one<POL>(src + 7 * plane + rp + xq);
     }
     const int kl = nx - 1 - x0;
     if ((periodic & 1) && kl >= 0 && kl < V) {
-        ld.w[0] = __ldg(src + 3 * plane + r0);
-        ld.w[1] = __ldg(src + 6 * plane + rm);
-        ld.w[2] = __ldg(src + 7 * plane + rp);
+        ld.w[0] = ld_one<POL>(src + 3 * plane + r0);
+        ld.w[1] = ld_one<POL>(src + 6 * plane + rm);
+        ld.w[2] = ld_one<POL>(src + 7 * plane + rp);
     }
 }
 
@@ -447,14 +459,14 @@ template <class S, int V, bool FORCE, class I, int POL = 0>
 __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restrict__ dst,
                                          const uint16_t *__restrict__ links, int x0, int y, int nx, int ny,
                                          I pitch, I plane, int periodic, const D2Q9Params &prm) {
-    const uint64_t pol_ld = POL ? policy_evict_first() : 0;
+    const uint64_t pol_ld = POL == 1 || POL == 2 ? policy_evict_first() : 0;
     const uint64_t pol_st = POL == 1 ? policy_evict_last() : 0;
     RowLoad<S, V, I> ld;
     load_row<S, V, I, POL>(ld, src, links, x0, y, nx, ny, pitch, plane, periodic, pol_ld);
     // own populations at the clamped xa (equal to x0 for every vector that is stored)
     const S *mine = src + ld.r0 + ld.xa;
     using T = typename RowLoad<S, V, I>::T;
-    auto own = [&](int q) { return __ldg(reinterpret_cast<const T *>(mine + q * plane)); };
+    auto own = [&](int q) { return ld_one<POL>(reinterpret_cast<const T *>(mine + q * plane)); };
     const int lane = threadIdx.x & 31;
     finish_row<S, V, FORCE, I, POL>(ld, own, dst, x0, nx, plane, periodic, prm, pol_st, ld.e, ld.e, lane == 0,
                                     lane == 31, true);
@@ -469,7 +481,7 @@ __device__ __forceinline__ void step_vec(const S *__restrict__ src, S *__restric
 // the slot's last vector are given that vector and active = false: they load in bounds, take part
 // in the shuffles and store nothing.  Per cell the arithmetic is that of step_vec, so the results
 // are bit-identical to the row mapping and to the single-domain kernel.
-template <class S, int V, class I>
+template <class S, int V, class I, int POL = 0>
 __device__ __forceinline__ void load_row_flat(RowLoad<S, V, I> &ld, const S *__restrict__ src,
                                               const uint16_t *__restrict__ links, int x0, int y, int nx, int ny,
                                               I pitch, I plane, int periodic, bool left_own, bool right_own) {
@@ -484,15 +496,15 @@ __device__ __forceinline__ void load_row_flat(RowLoad<S, V, I> &ld, const S *__r
     ld.rp = rp;
     ld.xa = x0;
     auto at = [&](int q, I r) { return reinterpret_cast<const T *>(src + q * plane + r + x0); };
-    ld.q0 = __ldg(at(0, r0));
-    ld.q2 = __ldg(at(2, rm));
-    ld.q4 = __ldg(at(4, rp));
-    ld.a1 = __ldg(at(1, r0));
-    ld.a5 = __ldg(at(5, rm));
-    ld.a8 = __ldg(at(8, rp));
-    ld.b3 = __ldg(at(3, r0));
-    ld.b6 = __ldg(at(6, rm));
-    ld.b7 = __ldg(at(7, rp));
+    ld.q0 = ld_one<POL>(at(0, r0));
+    ld.q2 = ld_one<POL>(at(2, rm));
+    ld.q4 = ld_one<POL>(at(4, rp));
+    ld.a1 = ld_one<POL>(at(1, r0));
+    ld.a5 = ld_one<POL>(at(5, rm));
+    ld.a8 = ld_one<POL>(at(8, rp));
+    ld.b3 = ld_one<POL>(at(3, r0));
+    ld.b6 = ld_one<POL>(at(6, rm));
+    ld.b7 = ld_one<POL>(at(7, rp));
     if constexpr (V == 1)
         ld.links = __ldg(links + r0 + x0);
     else
@@ -500,25 +512,25 @@ __device__ __forceinline__ void load_row_flat(RowLoad<S, V, I> &ld, const S *__r
     if (left_own) {
         int xm = x0 - 1;
         if (xm < 0) xm = (periodic & 1) ? nx - 1 : 0;  // unused (bounce-back) when not periodic
-        ld.e[0] = __ldg(src + 1 * plane + r0 + xm);
-        ld.e[1] = __ldg(src + 5 * plane + rm + xm);
-        ld.e[2] = __ldg(src + 8 * plane + rp + xm);
+        ld.e[0] = ld_one<POL>(src + 1 * plane + r0 + xm);
+        ld.e[1] = ld_one<POL>(src + 5 * plane + rm + xm);
+        ld.e[2] = ld_one<POL>(src + 8 * plane + rp + xm);
     }
     if (right_own) {
         const int xq = min(x0 + V, (int)pitch - 1);
-        ld.er[0] = __ldg(src + 3 * plane + r0 + xq);
-        ld.er[1] = __ldg(src + 6 * plane + rm + xq);
-        ld.er[2] = __ldg(src + 7 * plane + rp + xq);
+        ld.er[0] = ld_one<POL>(src + 3 * plane + r0 + xq);
+        ld.er[1] = ld_one<POL>(src + 6 * plane + rm + xq);
+        ld.er[2] = ld_one<POL>(src + 7 * plane + rp + xq);
     }
     const int kl = nx - 1 - x0;
     if ((periodic & 1) && kl >= 0 && kl < V) {
-        ld.w[0] = __ldg(src + 3 * plane + r0);
-        ld.w[1] = __ldg(src + 6 * plane + rm);
-        ld.w[2] = __ldg(src + 7 * plane + rp);
+        ld.w[0] = ld_one<POL>(src + 3 * plane + r0);
+        ld.w[1] = ld_one<POL>(src + 6 * plane + rm);
+        ld.w[2] = ld_one<POL>(src + 7 * plane + rp);
     }
 }
 
-template <class S, int V, bool FORCE, class I>
+template <class S, int V, bool FORCE, class I, int POL = 0>
 __device__ __forceinline__ void step_vec_flat(const S *__restrict__ src, S *__restrict__ dst,
                                               const uint16_t *__restrict__ links, int x0, int y, int nx, int ny,
                                               I pitch, I plane, int periodic, const D2Q9Params &prm, bool active) {
@@ -526,11 +538,11 @@ __device__ __forceinline__ void step_vec_flat(const S *__restrict__ src, S *__re
     const bool left_own = lane == 0 || x0 == 0;
     const bool right_own = lane == 31 || x0 + V == (int)pitch;
     RowLoad<S, V, I> ld;
-    load_row_flat<S, V, I>(ld, src, links, x0, y, nx, ny, pitch, plane, periodic, left_own, right_own);
+    load_row_flat<S, V, I, POL>(ld, src, links, x0, y, nx, ny, pitch, plane, periodic, left_own, right_own);
     const S *mine = src + ld.r0 + x0;
     using T = typename RowLoad<S, V, I>::T;
-    auto own = [&](int q) { return __ldg(reinterpret_cast<const T *>(mine + q * plane)); };
-    finish_row<S, V, FORCE, I, 0>(ld, own, dst, x0, nx, plane, periodic, prm, 0, ld.e, ld.er, left_own, right_own,
+    auto own = [&](int q) { return ld_one<POL>(reinterpret_cast<const T *>(mine + q * plane)); };
+    finish_row<S, V, FORCE, I, POL>(ld, own, dst, x0, nx, plane, periodic, prm, 0, ld.e, ld.er, left_own, right_own,
                                   active);
 }
 

@@ -91,6 +91,13 @@ def batch(count=512, seed=DEFAULT_SEED, steps=2000):
     return out
 
 
+def small_batch(count, seed=DEFAULT_SEED):
+    """`count` small independent domains (area log-uniform in [64^2, 256^2], otherwise as batch()):
+    a batch whose step is short enough for the launch of each step to matter."""
+    rng = np.random.default_rng(seed + 11)
+    return [_random_domain(rng, seed * 31 + i, 64 * 64, 256 * 256, 4.0, 0.52, 1.2, 0.30) for i in range(count)]
+
+
 def requests(rate, duration, seed=DEFAULT_SEED, side_lo=128, side_hi=2048, steps_lo=1000, steps_hi=50000):
     """Poisson arrivals at `rate` per second for `duration` seconds.  Side length log-uniform in
     [side_lo, side_hi] (area = side^2, aspect as in batch()), solid 0-30 %, tau 0.52-1.2, steps

@@ -233,3 +233,53 @@ def test_many_slots_table_path_and_back(dtype):
     for i, got in list(late.items())[::7]:
         assert np.array_equal(got, single(kinds[i], init_state(kinds[i][0], kinds[i][1], 1000 + i), first + second,
                                           dtype)), i
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f16s", "bf16s"])
+def test_persistent_launch_equals_one_launch_per_step(dtype):
+    """A step sequence run as one persistent (cooperative) launch, its blocks meeting after each
+    step, gives the populations of one launch per step, bit for bit, with step budgets that stop
+    slots inside the sequence."""
+    sp = specs()
+    budgets = [5, -1, 9, 0, -1, 3]
+    out = {}
+    for mode in (0, 2):
+        with lbm.Batch(dtype) as B:
+            B.set_persistent(mode)
+            slots = []
+            for i, s in enumerate(sp):
+                slot = B.add(*s[:4], s[4], s[5], s[6])
+                B.load_populations(slot, init_state(s[0], s[1], 60 + i))
+                B.set_slot_steps(slot, budgets[i])
+                slots.append(slot)
+            B.step(7)
+            B.step(6)
+            B.synchronize()
+            out[mode] = [(B.steps_done(sl), B.retrieve_populations(sl, np.float64)) for sl in slots]
+    for i, ((n0, g0), (n2, g2)) in enumerate(zip(out[0], out[2])):
+        assert n0 == n2 == (13 if budgets[i] < 0 else min(13, budgets[i]))
+        assert np.array_equal(g0, g2), (dtype, i)
+
+
+def test_persistent_launch_wait_gives_up_and_reports():
+    """The persistent launch's bounded meeting, exercised without any fault: with a 1 ms limit and
+    block 0 kept from arriving, the other blocks' wait runs out, every block ends the launch, and the
+    next lbm_batch_synchronize returns LBM_ERR_TIMEOUT; a new batch afterwards steps as usual."""
+    sp = specs()
+    with lbm.Batch("f16s") as B:
+        B.set_persistent(2, wait_ns=1_000_000, skip_block=0)
+        for i, s in enumerate(sp):
+            slot = B.add(*s[:4], s[4], s[5], s[6])
+            B.load_populations(slot, init_state(s[0], s[1], i))
+        B.step(3)
+        with pytest.raises(lbm.LBMError) as err:
+            B.synchronize()
+        assert err.value.status == lbm.capi.ERR_TIMEOUT and "persistent launch" in str(err.value)
+        B.synchronize()  # the status was taken: nothing left to report
+    s = sp[0]
+    with lbm.Batch("f16s") as B:
+        slot = B.add(*s[:4], s[4], s[5], s[6])
+        B.load_populations(slot, init_state(s[0], s[1], 0))
+        B.step(11)
+        got = B.retrieve_populations(slot, np.float64)
+    assert np.array_equal(got, single(s, init_state(s[0], s[1], 0), 11, "f16s"))
