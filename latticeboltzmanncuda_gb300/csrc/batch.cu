@@ -171,10 +171,24 @@ constexpr bool flat_tiles() {
     return sizeof(S) == 2;
 }
 
+// L2 prefetch of the flat tiles that start soon: the block's first thread asks L2 for the ten
+// segments (nine planes, with the row shift of their pull, and the link words) of the tile
+// PREFETCH_CELLS cells further along its slot in the sweep's direction (`cp.async.bulk.prefetch`,
+// no registers held and nothing to wait for), so those tiles' loads find their lines in L2.
+// Measured on the 512-domain batch and the serve mix (FP16): 118.0k -> 124.7k and 127.6k ->
+// 136.4k MLUPS; 8k to 64k cells ahead all within 2 %; on the single-domain kernel the same
+// prefetch measured slower.
+constexpr int PREFETCH_CELLS = 32768;
+
+__device__ __forceinline__ void prefetch_l2(const void *ptr, unsigned bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(ptr), "r"(bytes) : "memory");
+}
+
 // Tile t of the launch sequence's step `step` (POL 3: the loads at L2, coherent with the stores of
-// the previous step in the same launch).
+// the previous step in the same launch); dir +1 / -1: the sweep's direction for the L2 prefetch of
+// flat tiles (0: none).
 template <class S, int V, int POL = 0>
-__device__ __forceinline__ void batch_tile_p(const BatchParams &p, int t, int step) {
+__device__ __forceinline__ void batch_tile_p(const BatchParams &p, int t, int step, int dir = 0) {
     int lo = 0, hi = p.n - 1;
     while (lo < hi) {  // the last slot whose first tile is at or before t (uniform per block)
         const int mid = (lo + hi + 1) >> 1;
@@ -208,6 +222,24 @@ __device__ __forceinline__ void batch_tile_p(const BatchParams &p, int t, int st
     const S *src = a + (size_t)cur * 9 * plane;
     S *dst = a + (size_t)(cur ^ 1) * 9 * plane;
     const uint16_t *links = reinterpret_cast<const uint16_t *>(a + (size_t)18 * plane);
+    if constexpr (flat_tiles<S>()) {
+        if (dir != 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+            // segments of per cells, every offset a multiple of 32 cells (16-byte aligned) and
+            // clamped into the slot's planes
+            const int per = (int)(blockDim.x * blockDim.y) * V;
+            const int tf = tile + dir * (PREFETCH_CELLS / per);
+            if (plane >= per && tf >= 0 && (int64_t)tf * per < (int64_t)plane) {
+                const int first = min(tf * per, plane - per);
+#pragma unroll
+                for (int q = 0; q < 9; ++q) {
+                    const int dy = d2q9::cy(q);  // the pull of population q reads row y - c_y(q)
+                    const int o = max(0, min(first - dy * pitch, plane - per));
+                    prefetch_l2(src + (size_t)q * plane + o, (unsigned)(per * sizeof(S)));
+                }
+                prefetch_l2(links + first, (unsigned)(per * sizeof(uint16_t)));
+            }
+        }
+    }
     D2Q9Params prm;
     prm.omega = D.omega;
     prm.fx = D.fx;
@@ -242,13 +274,13 @@ __device__ __forceinline__ int launch_tile(int ntiles, int reverse) {
 template <class S, int V>
 __global__ void __launch_bounds__(256, batch_min_blocks(V)) batch_step_kernel_p(const __grid_constant__ BatchParams p,
                                                                                int step, int reverse) {
-    batch_tile_p<S, V>(p, launch_tile(p.ntiles, reverse), step);
+    batch_tile_p<S, V>(p, launch_tile(p.ntiles, reverse), step, reverse ? -1 : 1);
 }
 
 template <class S, int V>
 __global__ void __launch_bounds__(256, 4) batch_step_kernel_p_occ(const __grid_constant__ BatchParams p, int step,
                                                                   int reverse) {
-    batch_tile_p<S, V>(p, launch_tile(p.ntiles, reverse), step);
+    batch_tile_p<S, V>(p, launch_tile(p.ntiles, reverse), step, reverse ? -1 : 1);
 }
 
 // Persistent launch: one cooperative launch runs a whole step sequence.  Its blocks (no more than

@@ -6,6 +6,7 @@ must lie in [0, 9 * plane) and every link-word offset in [0, plane).  The kernel
 device-side bounds checks, so this replay is where their indexing is checked; keep it in step
 with the kernels."""
 import itertools
+import os
 
 import numpy as np
 import pytest
@@ -302,6 +303,17 @@ def batch_tiles(shapes, V, tx, ty):
     return tiles, start
 
 
+PREFETCH_CELLS = 32768  # batch.cu: PREFETCH_CELLS
+CY = [0, 0, 1, 0, -1, 1, 1, -1, -1]  # c_y of the D2Q9 populations
+
+
+def test_prefetch_distance_matches_the_kernel_source():
+    src = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                       "latticeboltzmanncuda_gb300", "csrc", "batch.cu")
+    with open(src) as fh:
+        assert f"constexpr int PREFETCH_CELLS = {PREFETCH_CELLS};" in fh.read()
+
+
 def search_tile(start, t):
     """batch_tile_p's binary search for tile t: (slot, tile within the slot)."""
     lo, hi = 0, len(start) - 1
@@ -409,6 +421,19 @@ def test_batch_parameter_path_tiles_and_addresses(seed):
                 st = active & (x0 < nx)
                 for e in range(V):
                     np.add.at(seen, (y[st], x0[st] + e), 1)
+            # the L2 prefetch of the tile PREFETCH_CELLS further along (16-bit flat tiles) stays in
+            # the slot's planes, 16-byte aligned
+            per = tx * ty * V
+            for j in range(len(js)):
+                for d in (1, -1):
+                    tf = j + d * (PREFETCH_CELLS // per)
+                    if plane < per or tf < 0 or tf * per >= plane:
+                        continue
+                    first = min(tf * per, plane - per)
+                    for q in range(9):
+                        o = max(0, min(first - CY[q] * pitch, plane - per))
+                        assert 0 <= o and o + per <= plane and (o * elem) % 16 == 0 and (per * elem) % 16 == 0
+                    assert first + per <= plane and (first * 2) % 16 == 0
             # every cell of every slot belongs to exactly one storing lane (which skips solid cells)
             assert (seen[:, :nx] == 1).all(), (nx, ny, V, tx, ty)
 
