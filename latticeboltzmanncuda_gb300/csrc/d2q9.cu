@@ -525,22 +525,34 @@ cudaError_t tune(lbm_ctx *ctx) {
         ms = t;
         return cudaSuccess;
     };
+    const std::vector<Shape> cands = candidates<S>(ctx);
+    // bring the clocks up before anything is compared: about 20 ms of launches of the first shape
+    if (!cands.empty()) {
+        float ms = -1.0f;
+        err = time_shape(cands[0], 8, ms);
+        if (err == cudaSuccess && ms > 0.0f) {
+            const int n = (int)std::min(2000.0f, 20.0f / (ms / 8.0f));
+            if (n > 8) err = time_shape(cands[0], n, ms);
+        }
+    }
     std::vector<std::pair<float, Shape>> timed;
-    for (const Shape &sh : candidates<S>(ctx)) {
+    for (size_t i = 0; i < cands.size() && err == cudaSuccess; ++i) {
         float ms;
-        if ((err = time_shape(sh, reps, ms)) != cudaSuccess) break;
-        if (ms >= 0.0f) timed.push_back({ms, sh});
+        if ((err = time_shape(cands[i], reps, ms)) != cudaSuccess) break;
+        if (ms >= 0.0f) timed.push_back({ms, cands[i]});
     }
     Shape pick = {1, 256, 1, 0};
     if (err == cudaSuccess && !timed.empty()) {
         std::stable_sort(timed.begin(), timed.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+        // the four fastest again, four interleaved passes in alternating order with eight times the
+        // launches (shapes a few per cent apart were otherwise picked by timing noise)
         const size_t top = std::min<size_t>(4, timed.size());
         std::vector<float> total(top, 0.0f);
-        for (int pass = 0; pass < 2 && err == cudaSuccess; ++pass)
+        for (int pass = 0; pass < 4 && err == cudaSuccess; ++pass)
             for (size_t k = 0; k < top && err == cudaSuccess; ++k) {
-                const size_t c = pass ? top - 1 - k : k;
+                const size_t c = (pass & 1) ? top - 1 - k : k;
                 float ms;
-                err = time_shape(timed[c].second, 4 * reps, ms);
+                err = time_shape(timed[c].second, 8 * reps, ms);
                 total[c] = (ms < 0.0f || total[c] < 0.0f) ? -1.0f : total[c] + ms;
             }
         float best = 1e30f;
