@@ -180,14 +180,6 @@ constexpr bool flat_tiles() {
 // prefetch measured slower.
 constexpr int PREFETCH_CELLS = 32768;
 
-// c_y(q) + 1 of the nine populations, two bits each
-constexpr unsigned cy_plus_one_bits() {
-    unsigned b = 0;
-    for (int q = 0; q < 9; ++q) b |= (unsigned)(d2q9::cy(q) + 1) << (2 * q);
-    return b;
-}
-constexpr unsigned CY_PLUS_ONE = cy_plus_one_bits();
-
 __device__ __forceinline__ void prefetch_l2(const void *ptr, unsigned bytes) {
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(ptr), "r"(bytes) : "memory");
 }
@@ -231,22 +223,20 @@ __device__ __forceinline__ void batch_tile_p(const BatchParams &p, int t, int st
     S *dst = a + (size_t)(cur ^ 1) * 9 * plane;
     const uint16_t *links = reinterpret_cast<const uint16_t *>(a + (size_t)18 * plane);
     if constexpr (flat_tiles<S>()) {
-        // lanes 0-8 of the block's first warp prefetch plane q = lane, lane 9 the link words: one
-        // warp instruction for the ten segments.  Segments of per cells (per * 2 bytes), every
-        // offset a multiple of 32 cells (16-byte aligned) and clamped into the slot's planes.
-        const int lane = (int)threadIdx.x;
-        if (dir != 0 && threadIdx.y == 0 && lane < 10) {
+        if (dir != 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+            // segments of per cells, every offset a multiple of 32 cells (16-byte aligned) and
+            // clamped into the slot's planes
             const int per = (int)(blockDim.x * blockDim.y) * V;
             const int tf = tile + dir * (PREFETCH_CELLS / per);
             if (plane >= per && tf >= 0 && (int64_t)tf * per < (int64_t)plane) {
                 const int first = min(tf * per, plane - per);
-                const void *seg = links + first;
-                if (lane < 9) {
-                    const int dy = (int)((CY_PLUS_ONE >> (2 * lane)) & 3u) - 1;  // the pull reads row y - c_y(q)
+#pragma unroll
+                for (int q = 0; q < 9; ++q) {
+                    const int dy = d2q9::cy(q);  // the pull of population q reads row y - c_y(q)
                     const int o = max(0, min(first - dy * pitch, plane - per));
-                    seg = src + (size_t)lane * plane + o;
+                    prefetch_l2(src + (size_t)q * plane + o, (unsigned)(per * sizeof(S)));
                 }
-                prefetch_l2(seg, (unsigned)(per * sizeof(S)));
+                prefetch_l2(links + first, (unsigned)(per * sizeof(uint16_t)));
             }
         }
     }
