@@ -153,15 +153,21 @@ __device__ __forceinline__ void decode(const Dims &d, int64_t c, int &x, int &y,
 // pull streaming with zero fill (SimCalcFuncs.cu:79-96): v[j] = f_j(x - c_j), 0 outside
 __device__ __forceinline__ void pull(const float *__restrict__ src, const Dims &d, int64_t c, int x, int y, int z,
                                      float v[27]) {
-    if (x > 0 && y > 0 && z > 0 && x < d.X - 1 && y < d.Y - 1 && z < d.Z - 1) {
-        // interior cell: every neighbour exists
+    if (x > 0 && y > 0 && x < d.X - 1 && y < d.Y - 1) {
+        // every x and y neighbour exists (uniform over a block when Z is a multiple of the block
+        // size: its cells are then one column of z); a neighbour beyond the first or last z is
+        // zero, its load predicated off, so a warp holding z = 0 or z = Z - 1 does not diverge
         const int64_t sy = d.Z, sx = (int64_t)d.Z * d.Y;
+        const bool zlo = z > 0, zhi = z < d.Z - 1;
         Unroll<27>::run([&](auto jj) {
             constexpr int j = decltype(jj)::value;
             int64_t s = c - kd(j, 2);
             if (kd(j, 1)) s = kd(j, 1) > 0 ? s - sy : s + sy;
             if (kd(j, 0)) s = kd(j, 0) > 0 ? s - sx : s + sx;
-            v[j] = __ldg(src + (int64_t)j * d.n + s);
+            if constexpr (kd(j, 2) == 0)
+                v[j] = __ldg(src + (int64_t)j * d.n + s);
+            else
+                v[j] = (kd(j, 2) > 0 ? zlo : zhi) ? __ldg(src + (int64_t)j * d.n + s) : 0.0f;
         });
         return;
     }
