@@ -596,8 +596,34 @@ __device__ __noinline__ void fused_cell_fp64(StepArgs a, int64_t c, int x, int y
 constexpr int FUSED_THREADS = 128;
 __host__ __device__ constexpr int fused_min_blocks(int eq) { return eq == EQ_F32 ? 8 : 5; }
 
+// FP32-equilibrium step: the first thread of a block prefetches into L2 the 27 pulled segments of
+// the block D3_PREFETCH_BLOCKS further on (`cp.async.bulk.prefetch.L2`, nothing held or awaited).
+// A segment is rounded out to 16-byte boundaries of the population buffer (one allocation of 27
+// planes) and clamped into it.  Measured on the 128^3 sphere model: 23.7k -> 24.3k MLUPS (32 to 256
+// blocks ahead within 0.3 %); the float-float kernel measured slower with it (13.7k -> 10.9k), so it
+// has none.
+constexpr int D3_PREFETCH_BLOCKS = 128;
+
+__device__ __forceinline__ void prefetch_block_ahead(const StepArgs &a) {
+    if (threadIdx.x != 0) return;
+    const int64_t first = ((int64_t)blockIdx.x + D3_PREFETCH_BLOCKS) * blockDim.x;
+    const int64_t len = (int64_t)blockDim.x + 4;  // cells: the segment and a one-cell shift either way
+    const int64_t total = 27 * a.d.n;             // elements of the buffer
+    if (first + (int64_t)blockDim.x > a.d.n || total < len) return;
+    Unroll<27>::run([&](auto jj) {
+        constexpr int j = decltype(jj)::value;
+        const int64_t off = (int64_t)kd(j, 2) + (int64_t)a.d.Z * ((int64_t)kd(j, 1) + (int64_t)a.d.Y * kd(j, 0));
+        int64_t e = (int64_t)j * a.d.n + first - off;
+        e = e < 0 ? 0 : (e > total - len ? total - len : e);
+        e &= ~(int64_t)3;  // 16-byte aligned (the buffer itself is)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a.src + e), "r"((unsigned)(len * 4))
+                     : "memory");
+    });
+}
+
 template <int EQ>
 __global__ void __launch_bounds__(FUSED_THREADS, fused_min_blocks(EQ)) fused_kernel(StepArgs a) {
+    if constexpr (EQ == EQ_F32) prefetch_block_ahead(a);
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= a.d.n) return;
     const uint8_t fl = a.flags[c];

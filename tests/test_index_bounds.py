@@ -540,3 +540,46 @@ def test_invariant_division_formula():
     for d in divisors:
         for n in [0, 1, d - 1, d, d + 1, 2 * d - 1, 2 ** 31 - 1, 2 ** 32 - 1] + [rng.randrange(2 ** 32) for _ in range(50)]:
             assert fastdiv(n, d) == n // d, (n, d)
+
+
+D3_PREFETCH_BLOCKS = 128  # d3q27.cu: D3_PREFETCH_BLOCKS
+KD27 = None
+
+
+def _kd27():
+    """the D3Q27 direction table of d3q27.cu's kd(j, a), read from the source"""
+    global KD27
+    if KD27 is None:
+        import re
+        src = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                           "latticeboltzmanncuda_gb300", "csrc", "d3q27.cu")
+        with open(src) as fh:
+            text = fh.read()
+        assert f"constexpr int D3_PREFETCH_BLOCKS = {D3_PREFETCH_BLOCKS};" in text
+        body = text[text.index("constexpr int kd(int j, int a)"):]
+        body = body[body.index("{", body.index("t[27][3]")):body.index("};")]
+        vals = [int(v) for v in re.findall(r"-?\d+", body)]
+        KD27 = np.array(vals[:81]).reshape(27, 3)
+    return KD27
+
+
+@pytest.mark.parametrize("dims", [(128, 128, 128), (5, 7, 3), (33, 17, 50), (1, 1, 130), (64, 3, 129)])
+def test_d3q27_prefetch_stays_in_the_population_buffer(dims):
+    """fused_kernel<FP32>'s L2 prefetch: for every block, each of the 27 segments lies inside the
+    27-plane buffer and starts on a 16-byte boundary."""
+    X, Y, Z = dims
+    n = X * Y * Z
+    kd = _kd27()
+    threads = 128
+    length = threads + 4
+    total = 27 * n
+    for b in range((n + threads - 1) // threads):
+        first = (b + D3_PREFETCH_BLOCKS) * threads
+        if first + threads > n or total < length:
+            continue
+        for j in range(27):
+            off = kd[j, 2] + Z * (kd[j, 1] + Y * kd[j, 0])
+            e = j * n + first - off
+            e = 0 if e < 0 else (total - length if e > total - length else e)
+            e &= ~3
+            assert 0 <= e and e + length <= total and (e * 4) % 16 == 0
