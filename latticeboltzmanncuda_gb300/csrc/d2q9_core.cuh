@@ -48,17 +48,13 @@ __device__ __forceinline__ double fma_(double a, double b, double c) { return __
 __device__ __forceinline__ double mul_(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double add_(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub_(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ float neg_(float a) { return -a; }
-__device__ __forceinline__ double neg_(double a) { return -a; }
 
 // Two cells at once on the packed FP32 pipe of sm_100+ (FFMA2 / FADD2 / FMUL2): every lane gets the
 // same IEEE round-to-nearest result as the scalar intrinsic, so a packed update is bit-identical to
-// two scalar ones while issuing half the arithmetic instructions.  a - b is computed as a + (-b),
-// which is the same IEEE value.
+// two scalar ones while issuing half the arithmetic instructions.
 __device__ __forceinline__ float2 fma_(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 mul_(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 add_(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 neg_(float2 a) { return make_float2(-a.x, -a.y); }
 // a - b as a + b * (-1): the product is exact, so the one rounding gives a - b (a packed negation
 // would cost an instruction of its own)
 __device__ __forceinline__ float2 sub_(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
@@ -197,13 +193,6 @@ __device__ __forceinline__ void pack(const typename Store<S>::R (&in)[V], T &raw
 }
 
 template <class S, int V>
-__device__ __forceinline__ void ld_pack(const S *__restrict__ p, typename Store<S>::R (&out)[V]) {
-    using T = typename RawPack<sizeof(S) * V>::T;
-    const T raw = __ldg(reinterpret_cast<const T *>(p));
-    unpack<S, V>(raw, out);
-}
-
-template <class S, int V>
 __device__ __forceinline__ void st_pack(S *__restrict__ p, const typename Store<S>::R (&in)[V]) {
     using T = typename RawPack<sizeof(S) * V>::T;
     T raw;
@@ -259,17 +248,6 @@ __device__ __forceinline__ void st_hint(uint2 *p, uint2 v, uint64_t pol) {
 }
 __device__ __forceinline__ void st_hint(unsigned int *p, unsigned int v, uint64_t pol) {
     asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
-}
-
-template <class S, int V, int POL>
-__device__ __forceinline__ void ld_pack_pol(const S *__restrict__ p, typename Store<S>::R (&out)[V], uint64_t pol) {
-    if constexpr (POL == 0) {
-        ld_pack<S, V>(p, out);
-    } else {
-        using T = typename RawPack<sizeof(S) * V>::T;
-        const T raw = ld_hint<T>(reinterpret_cast<const T *>(p), pol);
-        unpack<S, V>(raw, out);
-    }
 }
 
 template <class T, int POL>
