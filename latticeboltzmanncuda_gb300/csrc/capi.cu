@@ -167,11 +167,7 @@ lbm_status d3_prepare(lbm_ctx *ctx) {
         const size_t nblocks = d3q27_gather_blocks(ctx->ntgt);
         if ((s = ensure_scratch(ctx, std::max<size_t>(nblocks * 3, 512 * 4))) != LBM_OK) return s;
         if (!ctx->side_stream) {
-            // the highest priority: its blocks are dispatched ahead of the fused kernel's
-            int least = 0, greatest = 0;
-            CUDA_TRY(ctx, cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
-            CUDA_TRY(ctx, cudaStreamCreateWithPriority(&ctx->side_stream, cudaStreamNonBlocking, greatest),
-                     "gather stream");
+            CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking), "gather stream");
             CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming), "gather fork event");
             CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming), "gather join event");
         }

@@ -561,9 +561,6 @@ struct StepArgs {
 // one cell of the fused step: pull (or, for a target of the gather lists, its gathered populations),
 // zero internal cells, collide, flow source, store
 template <int EQ>
-__device__ __forceinline__ bool finish_cell(const StepArgs &a, int64_t c, uint8_t fl, float v[27]);
-
-template <int EQ>
 __device__ __forceinline__ bool fused_cell(const StepArgs &a, int64_t c, int x, int y, int z, uint8_t fl) {
     float v[27];
     if (a.cli && (fl & F_GATHER)) {
@@ -573,13 +570,6 @@ __device__ __forceinline__ bool fused_cell(const StepArgs &a, int64_t c, int x, 
     } else {
         pull(a.src, a.d, c, x, y, z, v);
     }
-    return finish_cell<EQ>(a, c, fl, v);
-}
-
-// the cell's update from its streamed (or gathered) populations v: zeroing of internal cells,
-// collision, flow source, store; false when the float-float equilibrium must be redone in FP64
-template <int EQ>
-__device__ __forceinline__ bool finish_cell(const StepArgs &a, int64_t c, uint8_t fl, float v[27]) {
     if (a.cli && (fl & F_INTERNAL)) {
 #pragma unroll
         for (int j = 0; j < 27; ++j) v[j] = 0.0f;
@@ -646,26 +636,16 @@ __global__ void __launch_bounds__(FUSED_THREADS, fused_min_blocks(EQ)) fused_ker
 
 // The gather targets' update when the gather ran beside the fused kernel: the same fused_cell, from
 // each target's gathered row, one thread per target.
-// The block's rows are read into shared memory with consecutive threads on consecutive words
-// (a row is 27 floats) and each thread's row is taken from there.
 template <int EQ>
 __global__ void __launch_bounds__(FUSED_THREADS, fused_min_blocks(EQ))
     targets_kernel(StepArgs a, const int32_t *__restrict__ tgt, int64_t ntgt) {
-    __shared__ float rows[FUSED_THREADS * 27];
-    const int64_t i0 = blockIdx.x * (int64_t)blockDim.x;
-    const int64_t nrow = min((int64_t)blockDim.x, ntgt - i0);
-    for (int k = threadIdx.x; k < nrow * 27; k += blockDim.x) rows[k] = __ldg(a.gathered + i0 * 27 + k);
-    __syncthreads();
-    const int64_t i = i0 + threadIdx.x;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= ntgt) return;
     const int64_t c = tgt[i];
     const uint8_t fl = a.flags[c];
     int x, y, z;
     decode(a.d, c, x, y, z);
-    float v[27];
-#pragma unroll
-    for (int j = 0; j < 27; ++j) v[j] = rows[threadIdx.x * 27 + j];
-    if (!finish_cell<EQ>(a, c, fl, v)) fused_cell_fp64(a, c, x, y, z, fl);
+    if (!fused_cell<EQ>(a, c, x, y, z, fl)) fused_cell_fp64(a, c, x, y, z, fl);
 }
 
 struct GatherArgs {
