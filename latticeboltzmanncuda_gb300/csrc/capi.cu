@@ -166,11 +166,6 @@ lbm_status d3_prepare(lbm_ctx *ctx) {
                  "upload target index");
         const size_t nblocks = d3q27_gather_blocks(ctx->ntgt);
         if ((s = ensure_scratch(ctx, std::max<size_t>(nblocks * 3, 512 * 4))) != LBM_OK) return s;
-        if (!ctx->side_stream) {
-            CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking), "gather stream");
-            CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming), "gather fork event");
-            CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming), "gather join event");
-        }
     }
     CUDA_TRY(ctx, cudaMemcpy(ctx->flags_d, fl.data(), fl.size(), cudaMemcpyHostToDevice), "upload flags");
     ctx->d3_dirty = false;
@@ -329,12 +324,6 @@ LBM_API lbm_status lbm_destroy(lbm_ctx *ctx) {
     cudaFree(ctx->scratch.partials);
     cudaFree(ctx->result_d);
     cudaFree(ctx->staging);
-    if (ctx->side_stream) {
-        cudaStreamSynchronize(ctx->side_stream);
-        cudaStreamDestroy(ctx->side_stream);
-        cudaEventDestroy(ctx->ev_fork);
-        cudaEventDestroy(ctx->ev_join);
-    }
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return LBM_OK;

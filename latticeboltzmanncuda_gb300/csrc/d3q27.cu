@@ -555,7 +555,6 @@ struct StepArgs {
     int cli;                 // 1: stream, reflect, collide, flow; 0: stream, collide
     const float *gathered;   // CLI order: the gather targets' populations (27 per target), or nullptr
     const int32_t *tgt_index;  // per cell: its row of `gathered`
-    int skip_targets = 0;    // 1: the fused kernel leaves the gather targets to targets_kernel
 };
 
 // one cell of the fused step: pull (or, for a target of the gather lists, its gathered populations),
@@ -627,21 +626,6 @@ __global__ void __launch_bounds__(FUSED_THREADS, fused_min_blocks(EQ)) fused_ker
     if constexpr (EQ == EQ_F32) prefetch_block_ahead(a);
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= a.d.n) return;
-    const uint8_t fl = a.flags[c];
-    if (a.skip_targets && a.cli && (fl & F_GATHER)) return;  // collided by targets_kernel after the gather
-    int x, y, z;
-    decode(a.d, c, x, y, z);
-    if (!fused_cell<EQ>(a, c, x, y, z, fl)) fused_cell_fp64(a, c, x, y, z, fl);
-}
-
-// The gather targets' update when the gather ran beside the fused kernel: the same fused_cell, from
-// each target's gathered row, one thread per target.
-template <int EQ>
-__global__ void __launch_bounds__(FUSED_THREADS, fused_min_blocks(EQ))
-    targets_kernel(StepArgs a, const int32_t *__restrict__ tgt, int64_t ntgt) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= ntgt) return;
-    const int64_t c = tgt[i];
     const uint8_t fl = a.flags[c];
     int x, y, z;
     decode(a.d, c, x, y, z);
@@ -996,19 +980,17 @@ GatherArgs gather_args(lbm_ctx *ctx) {
     return g;
 }
 
-cudaError_t launch_gather(lbm_ctx *ctx, const StepArgs &a, int mode, double *force_copy = nullptr,
-                          cudaStream_t stream = nullptr) {
+cudaError_t launch_gather(lbm_ctx *ctx, const StepArgs &a, int mode, double *force_copy = nullptr) {
     if (ctx->ntgt == 0) return cudaSuccess;
-    if (!stream) stream = ctx->stream;
     GatherArgs g = gather_args(ctx);
     g.force_copy = force_copy;
     const int threads = GATHER_THREADS;
     const unsigned nb = (unsigned)d3q27_gather_blocks(ctx->ntgt);  // one warp per target cell
     static_assert(GATHER_THREADS == 16 * 32, "d3q27_gather_blocks assumes sixteen warps per block");
     if (mode != 0)
-        gather_kernel<1><<<nb, threads, 0, stream>>>(a, g);
+        gather_kernel<1><<<nb, threads, 0, ctx->stream>>>(a, g);
     else
-        gather_kernel<0><<<nb, threads, 0, stream>>>(a, g);
+        gather_kernel<0><<<nb, threads, 0, ctx->stream>>>(a, g);
     return cudaGetLastError();  // the force, when accumulated, was added by the kernel's last block
 }
 
@@ -1114,17 +1096,7 @@ cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps, double *series_d) {
         cudaError_t e = cudaSuccess;
         double *copy = series_d ? series_d + 3 * (int64_t)s : nullptr;
         const bool reduced = a.cli && ctx->ntgt > 0 && ctx->force_on;  // the force changes this step
-        // CLI order with gather targets: the gather runs on the side stream while the fused kernel
-        // updates every other cell (both only read the source buffer), then the targets are
-        // collided from their gathered rows
-        const bool fork = a.cli && ctx->ntgt > 0 && ctx->side_stream;
-        a.skip_targets = fork ? 1 : 0;
-        if (fork) {
-            if ((e = cudaEventRecord(ctx->ev_fork, ctx->stream)) != cudaSuccess) return e;
-            if ((e = cudaStreamWaitEvent(ctx->side_stream, ctx->ev_fork, 0)) != cudaSuccess) return e;
-            if ((e = launch_gather(ctx, a, 0, copy, ctx->side_stream)) != cudaSuccess) return e;
-            if ((e = cudaEventRecord(ctx->ev_join, ctx->side_stream)) != cudaSuccess) return e;
-        } else if (a.cli) {  // the targets of the gather lists first: the fused kernel collides them
+        if (a.cli) {  // the targets of the gather lists first: the fused kernel collides them
             e = launch_gather(ctx, a, 0, copy);
             if (e != cudaSuccess) return e;
         }
@@ -1136,17 +1108,6 @@ cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps, double *series_d) {
             fused_kernel<EQ_FF><<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        if (fork) {
-            if ((e = cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0)) != cudaSuccess) return e;
-            const unsigned nt = blocks_for(ctx->ntgt, threads);
-            if (ctx->eq_mode == EQ_F64)
-                targets_kernel<EQ_F64><<<nt, threads, 0, ctx->stream>>>(a, ctx->tgt_cells_d, ctx->ntgt);
-            else if (ctx->eq_mode == EQ_F32)
-                targets_kernel<EQ_F32><<<nt, threads, 0, ctx->stream>>>(a, ctx->tgt_cells_d, ctx->ntgt);
-            else
-                targets_kernel<EQ_FF><<<nt, threads, 0, ctx->stream>>>(a, ctx->tgt_cells_d, ctx->ntgt);
-            if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        }
         if (copy && !reduced) {
             e = cudaMemcpyAsync(copy, ctx->force_acc_d, 3 * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
             if (e != cudaSuccess) return e;

@@ -110,9 +110,6 @@ struct lbm_ctx {
     int32_t *tgt_index_d = nullptr;  // per cell: its index in the target list, or -1
     unsigned *gather_done_d = nullptr;  // blocks of the gather kernel that have written their force partial
     int64_t ntgt = 0, nent = 0;
-    // the gather kernel runs on a stream of its own beside the fused kernel (fork and join events)
-    cudaStream_t side_stream = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     float *induced_d = nullptr;      // 27 floats
     bool flow_on = false;
     double *force_acc_d = nullptr;   // running force sum (3 doubles)
