@@ -401,3 +401,37 @@ def test_pipeline_wait_arguments_checked():
             L.set_pipeline_wait(10)  # below 1 microsecond
         with pytest.raises(lbm.LBMError):
             L.set_pipeline_wait(1_000_000, skip_task=-2)
+
+
+@pytest.mark.parametrize("shape", [(1, 256, 1, 0), (2, 64, 1, 0), (2, 32, 4, 0)])
+def test_solid_cells_stay_frozen_across_flag_changes(shape):
+    """The step kernels never write a solid cell; both population buffers hold its values (the link
+    build copies solid cells into the other buffer, so flags can change between steps).  FP64 against
+    the oracle, which copies solid cells forward, on every cell -- solid ones included -- after 5
+    steps with one set of flags and 7 (an odd count: the other buffer is current) with another that
+    adds a disk and frees part of an old one."""
+    nx, ny = 97, 41
+    a = np.zeros((ny, nx), np.uint8)
+    a[0, :] = a[-1, :] = 1
+    yy, xx = np.mgrid[0:ny, 0:nx]
+    a[(xx - 30) ** 2 + (yy - 20) ** 2 <= 36] = 1
+    b = a.copy()
+    b[(xx - 70) ** 2 + (yy - 18) ** 2 <= 25] = 1       # a new disk
+    b[(xx - 30) ** 2 + (yy - 20) ** 2 <= 36] = 0
+    b[(xx - 30) ** 2 + (yy - 20) ** 2 <= 9] = 1        # the old disk shrinks
+    f0 = random_state(nx, ny, 4242)
+    tau, force = 0.7, (2e-6, 0.0)
+    ref = oracle.d2q9_run(f0, a, tau, 5, periodic=1, force=force)
+    ref = oracle.d2q9_run(ref, b, tau, 7, periodic=1, force=force)
+    with lbm.Lattice(nx, ny, dtype="f64", tau=tau, periodic=1, body_force=(*force, 0)) as L:
+        L.set_flags(a)
+        L.load_populations(f0)
+        L.set_launch(*shape)
+        L.step(5)
+        L.set_flags(b)
+        L.step(7)
+        got = L.retrieve_populations(np.float64)
+    assert np.max(np.abs(got - ref)) <= 1e-12
+    solid = b != 0
+    frozen = (a != 0) & solid
+    assert np.array_equal(got[:, frozen], f0[:, frozen])  # solid throughout: the initial values
