@@ -158,14 +158,16 @@ __device__ __forceinline__ uint32_t solid_cells(const uint32_t (&lw)[NW]) {
 // Update the vector of ld and store it to dst.  own(q) returns the raw pack of the vector's own
 // population q (bounce-back takes the opposite population of the cell itself).  Solid cells are
 // not written: no fluid cell reads their values (a pull from a solid cell is replaced by
-// bounce-back), and both buffers hold the same values there from the initialisation on, so a
-// vector without solid cells is stored whole, a mixed vector cell by cell, an all-solid one not
-// at all.
+// bounce-back), and both buffers hold the same values there (the initialisation and the population
+// upload write both, the link build copies every solid cell into the other buffer, a checkpoint is
+// restored into both), so a vector without solid cells is stored whole, a mixed vector cell by
+// cell, an all-solid one not at all.
 //
 // 16-bit storage assembles the pulled populations and applies the bounce-back on the raw pairs:
 // the x-shifted vectors are byte permutes of adjacent words, and a bounce-back is one select per
 // pair under a mask built from the link word.  The arithmetic values are then those of the float
-// path (a raw select followed by the conversion is the conversion followed by the select).
+// path (a raw select followed by the conversion is the conversion followed by the select); each
+// pair of cells is unpacked, collided and packed back in turn, so at most 18 FP32 values are live.
 template <class S, int V, bool FORCE, class I, int POL, class Own>
 __device__ __forceinline__ void finish_row(const RowLoad<S, V, I> &ld, Own own, S *__restrict__ dst, int x0, int nx,
                                            I plane, int periodic, const D2Q9Params &prm, uint64_t pol_st,

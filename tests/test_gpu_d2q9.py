@@ -420,7 +420,8 @@ def test_solid_cells_stay_frozen_across_flag_changes(shape):
     b[(xx - 30) ** 2 + (yy - 20) ** 2 <= 36] = 0
     b[(xx - 30) ** 2 + (yy - 20) ** 2 <= 9] = 1        # the old disk shrinks
     f0 = random_state(nx, ny, 4242)
-    tau, force = 0.7, (2e-6, 0.0)
+    # the library takes tau and the force as float: the oracle gets the same values
+    tau, force = float(np.float32(0.7)), (float(np.float32(2e-6)), 0.0)
     ref = oracle.d2q9_run(f0, a, tau, 5, periodic=1, force=force)
     ref = oracle.d2q9_run(ref, b, tau, 7, periodic=1, force=force)
     with lbm.Lattice(nx, ny, dtype="f64", tau=tau, periodic=1, body_force=(*force, 0)) as L:
