@@ -224,7 +224,12 @@ LBM_API lbm_status lbm_step_force_series(lbm_ctx *ctx, int32_t nsteps, float *ho
  * warp staging the populations each row of a 512-cell strip pulls into a ring of shared-memory
  * slots with cp.async.bulk, four warps updating the rows; for it l2_policy selects the ring (0: 4
  * slots and 5 blocks per SM, 1: 4 slots and 4 blocks, 2: 6 slots and 3 blocks).  Its waits are
- * bounded: if one gives up, the next call that synchronises the context returns LBM_ERR_TIMEOUT. */
+ * bounded: if one gives up, the next call that synchronises the context returns LBM_ERR_TIMEOUT.
+ * cells_per_thread -2 selects two time steps per launch on shared-memory tiles of block_threads x
+ * rows_per_block cells (64 x 8, 64 x 16 or 128 x 8; l2_policy 0; FP32 and 16-bit storage): each
+ * block loads its tile with a two-cell halo, computes the first step on the tile grown by one cell
+ * and the second into the destination, so the populations cross HBM once per two updates (an odd
+ * last step of a call runs the one-step kernel).  Every shape gives bit-identical populations. */
 LBM_API lbm_status lbm_autotune(lbm_ctx *ctx, int32_t retune);
 LBM_API lbm_status lbm_set_launch(lbm_ctx *ctx, int32_t cells_per_thread, int32_t block_threads,
                                   int32_t rows_per_block, int32_t l2_policy);

@@ -26,6 +26,7 @@
 #include "lbm_internal.h"
 #include "d2q9_core.cuh"
 #include "d2q9_bulk.cuh"
+#include "d2q9_tile2.cuh"
 #include "d2q9_vec.cuh"
 #include "reduce.cuh"
 
@@ -348,6 +349,52 @@ struct Shape {
     int v, tx, ty, pol;  // cells per thread, block shape, L2 policy of the vector path (0, 1, 2)
 };
 
+// v == TILE2: two steps per launch on shared-memory tiles of tx x ty cells (d2q9_tile2.cuh)
+constexpr int TILE2 = -2;
+
+template <class S, int TX, int TY, bool FORCE>
+__global__ void __launch_bounds__(d2q9::tile2::THREADS) tile2_kernel(const S *__restrict__ src, S *__restrict__ dst,
+                                                                    const uint16_t *__restrict__ links, int nx,
+                                                                    int ny, int pitch, int plane, int periodic,
+                                                                    D2Q9Params prm) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    d2q9::tile2::two_steps<S, TX, TY, FORCE>(src, dst, links, nx, ny, pitch, plane, periodic, prm, smem);
+}
+
+template <class S, int TX, int TY, bool FORCE>
+cudaError_t launch_tile2_t(lbm_ctx *ctx, const S *src, S *dst, const D2Q9Params &prm) {
+    constexpr size_t bytes = d2q9::tile2::Layout<S, TX, TY>::bytes;
+    static bool attr_set = false;  // per instantiation (the attribute is per function)
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(tile2_kernel<S, TX, TY, FORCE>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    const lbm_desc &d = ctx->desc;
+    const dim3 grid((unsigned)((d.nx + TX - 1) / TX), (unsigned)((d.ny + TY - 1) / TY));
+    tile2_kernel<S, TX, TY, FORCE><<<grid, d2q9::tile2::THREADS, bytes, ctx->stream>>>(
+        src, dst, ctx->links_d, d.nx, d.ny, (int)ctx->pitch, (int)ctx->plane, d.periodic, prm);
+    return cudaGetLastError();
+}
+
+// the tile shapes of the two-step kernel
+inline bool tile2_shape(int tx, int ty) { return (tx == 64 && (ty == 8 || ty == 16)) || (tx == 128 && ty == 8); }
+
+template <class S>
+cudaError_t launch_tile2(lbm_ctx *ctx, int tx, int ty, const S *src, S *dst) {
+    if constexpr (sizeof(S) > 4) {
+        return cudaErrorInvalidValue;
+    } else {
+        const D2Q9Params prm = d2q9_params(ctx->desc);
+        const bool f = prm.fx != 0.0f || prm.fy != 0.0f;
+        if (tx == 64 && ty == 8) return f ? launch_tile2_t<S, 64, 8, true>(ctx, src, dst, prm) : launch_tile2_t<S, 64, 8, false>(ctx, src, dst, prm);
+        if (tx == 64 && ty == 16) return f ? launch_tile2_t<S, 64, 16, true>(ctx, src, dst, prm) : launch_tile2_t<S, 64, 16, false>(ctx, src, dst, prm);
+        if (tx == 128 && ty == 8) return f ? launch_tile2_t<S, 128, 8, true>(ctx, src, dst, prm) : launch_tile2_t<S, 128, 8, false>(ctx, src, dst, prm);
+        return cudaErrorInvalidValue;
+    }
+}
+
 template <class S>
 constexpr bool vec_ok(int v) {
     return (sizeof(S) == 4 && (v == 2 || v == 4)) || (sizeof(S) == 2 && (v == 2 || v == 4 || v == 8)) ||
@@ -376,6 +423,7 @@ cudaError_t launch_one(lbm_ctx *ctx, const Shape &sh, const S *src, S *dst, int 
         }
         return cudaGetLastError();
     }
+    if (sh.v == TILE2) return launch_tile2<S>(ctx, sh.tx, sh.ty, src, dst);  // two steps
     const int pitch = (int)ctx->pitch, plane = (int)ctx->plane;
     if (sh.v == 0) {  // bulk-copy pipeline
         if constexpr (sizeof(S) == 2)
@@ -409,6 +457,8 @@ std::vector<Shape> candidates(const lbm_ctx *ctx) {
     if (!small_index(ctx)) return c;
     if (sizeof(S) == 2)  // the bulk-copy pipeline
         for (int pol : {0, 1, 2}) c.push_back({0, d2q9::bulk::threads<4>(), 1, pol});
+    if (sizeof(S) <= 4)  // two steps per launch on shared-memory tiles
+        for (const auto &t : {std::pair<int, int>{64, 8}, {64, 16}, {128, 8}}) c.push_back({TILE2, t.first, t.second, 0});
     for (int v : {2, 4, 8}) {
         if (!vec_ok<S>(v) || ctx->pitch % v) continue;
         const int per_row = (int)(ctx->pitch / v);
@@ -522,7 +572,7 @@ cudaError_t tune(lbm_ctx *ctx) {
         float t = 0.0f;
         cudaEventElapsedTime(&t, e0, e1);
         if (sh.v == 0 && d2q9_take_pipe_status(ctx) != 0) return cudaSuccess;  // a bounded wait gave up
-        ms = t;
+        ms = sh.v == TILE2 ? 0.5f * t : t;  // per time step: a two-step launch counts twice
         return cudaSuccess;
     };
     const std::vector<Shape> cands = candidates<S>(ctx);
@@ -581,6 +631,23 @@ cudaError_t launch_step(lbm_ctx *ctx, int nsteps) {
         if (e != cudaSuccess) return e;
     }
     const Shape sh{ctx->cells_per_thread, ctx->block_threads, ctx->rows_per_block, ctx->l2_policy};
+    if (sh.v == TILE2) {
+        // two steps per launch; an odd last step by the one-step vector kernel (bit-identical)
+        for (int s = 0; s + 1 < nsteps; s += 2) {
+            cudaError_t e = launch_one<S>(ctx, sh, static_cast<const S *>(ctx->f[ctx->cur]),
+                                          static_cast<S *>(ctx->f[ctx->cur ^ 1]), 0);
+            if (e != cudaSuccess) return e;
+            ctx->cur ^= 1;
+        }
+        if (nsteps & 1) {
+            const Shape one{2, 64, 1, 0};
+            cudaError_t e = launch_one<S>(ctx, one, static_cast<const S *>(ctx->f[ctx->cur]),
+                                          static_cast<S *>(ctx->f[ctx->cur ^ 1]), 0);
+            if (e != cudaSuccess) return e;
+            ctx->cur ^= 1;
+        }
+        return cudaSuccess;
+    }
     for (int s = 0; s < nsteps; ++s) {
         const S *src = static_cast<const S *>(ctx->f[ctx->cur]);
         S *dst = static_cast<S *>(ctx->f[ctx->cur ^ 1]);
@@ -652,6 +719,8 @@ cudaError_t d2q9_init_equilibrium(lbm_ctx *ctx, const float *rho_d, const float 
 }
 
 bool d2q9_shape_valid(const lbm_ctx *ctx, int v, int tx, int ty, int pol) {
+    if (v == TILE2)  // two-step tiles: FP32 and 16-bit storage
+        return ctx->desc.dtype != LBM_F64 && tile2_shape(tx, ty) && pol == 0 && small_index(ctx);
     if (v == 0)  // bulk-copy pipeline: 16-bit storage, fixed block shape, three ring variants
         return (ctx->desc.dtype == LBM_F16S || ctx->desc.dtype == LBM_BF16S) &&
                tx == d2q9::bulk::threads<4>() && ty == 1 &&

@@ -206,12 +206,13 @@ def test_steps_are_deterministic():
 # pipeline of 16-bit storage (160 threads, 4 cells per consumer thread, one row per task; the last
 # field the ring variant)
 SHAPES = [(1, 256, 1, 0), (1, 128, 2, 0), (2, 64, 1, 0), (2, 32, 4, 1), (4, 32, 1, 2), (4, 64, 2, 0),
-          (4, 128, 1, 1), (8, 32, 1, 1), (8, 64, 2, 2), (0, 160, 1, 0), (0, 160, 1, 1), (0, 160, 1, 2)]
+          (4, 128, 1, 1), (8, 32, 1, 1), (8, 64, 2, 2), (0, 160, 1, 0), (0, 160, 1, 1), (0, 160, 1, 2),
+          (-2, 64, 8, 0), (-2, 64, 16, 0), (-2, 128, 8, 0)]  # -2: two steps per launch on shared-memory tiles
 
 
 def shape_ok(dtype, v):
-    return v == 1 or (dtype == "f32" and v in (2, 4)) or (dtype in ("f16s", "bf16s") and v in (0, 2, 4, 8)) or \
-        (dtype == "f64" and v == 2)
+    return v == 1 or (dtype == "f32" and v in (2, 4, -2)) or (dtype in ("f16s", "bf16s") and v in (0, 2, 4, 8, -2)) \
+        or (dtype == "f64" and v == 2)
 
 
 @pytest.mark.parametrize("shape", SHAPES)
@@ -436,3 +437,32 @@ def test_solid_cells_stay_frozen_across_flag_changes(shape):
     solid = b != 0
     frozen = (a != 0) & solid
     assert np.array_equal(got[:, frozen], f0[:, frozen])  # solid throughout: the initial values
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f16s"])
+@pytest.mark.parametrize("periodic", [0, 1, 2, 3])
+def test_two_step_tiles_match_the_one_step_kernel(dtype, periodic):
+    """Two steps per launch on shared-memory tiles (walls, moving walls, solid cells on tile edges,
+    wrap in x and y, domains smaller than a tile, an odd step count) give the one-step vector
+    kernel's populations bit for bit."""
+    for nx, ny in ((777, 70), (5, 3), (64, 8), (130, 17)):
+        flags, _ = lbm.gen_channel(nx, ny, 4 if nx > 60 else 0, 2.0, 6.0, 13) if nx > 8 else \
+            (np.zeros((ny, nx), np.uint8), None)
+        if periodic & 2:
+            flags[0, :] = flags[-1, :] = 0
+        if nx > 64:
+            flags[:, 63:65] = np.where(np.arange(ny)[:, None] % 4 == 0, 1, flags[:, 63:65])  # solid on a tile edge
+            flags[ny // 3, ::5] = lbm.MOVING_WALL
+        f0 = random_state(nx, ny, 31 + periodic + nx)
+        outs = []
+        for shape in ((2, 64, 1, 0), (-2, 64, 8, 0), (-2, 64, 16, 0), (-2, 128, 8, 0)):
+            with lbm.Lattice(nx, ny, dtype=dtype, tau=0.57, periodic=periodic, body_force=(1e-5, -3e-6, 0),
+                             wall_velocity=(0.03, 0.01, 0)) as L:
+                L.set_flags(flags)
+                L.load_populations(f0)
+                L.set_launch(*shape)
+                L.step(6)
+                L.step(17)
+                outs.append(L.retrieve_populations())
+        for k, o in enumerate(outs[1:]):
+            assert np.array_equal(o, outs[0]), (nx, ny, k)

@@ -583,3 +583,60 @@ def test_d3q27_prefetch_stays_in_the_population_buffer(dims):
             e = 0 if e < 0 else (total - length if e > total - length else e)
             e &= ~3
             assert 0 <= e and e + length <= total and (e * 4) % 16 == 0
+
+
+CX = [0, 1, 0, -1, 0, 1, -1, -1, 1]  # c_x of the D2Q9 populations
+
+
+@pytest.mark.parametrize("elem,tx,ty", [(4, 64, 8), (4, 64, 16), (4, 128, 8), (2, 64, 8), (2, 64, 16), (2, 128, 8)])
+def test_two_step_tile_indexing(elem, tx, ty):
+    """d2q9_tile2.cuh: every global load and store lies in the planes, every shared-memory index in
+    its tile, for domains smaller and larger than a tile, periodic or not; the shared memory fits."""
+    iw, ih, mw, mh = tx + 4, ty + 4, tx + 2, ty + 2
+    n_in, n_mid = iw * ih, mw * mh
+    smem = 9 * n_in * elem + 9 * n_mid * elem + n_mid * 2
+    assert smem <= 227 * 1024
+    rng = np.random.default_rng(tx * 100 + ty + elem)
+    shapes = [(1, 1), (5, 3), (tx, ty), (tx + 1, ty + 3), (3 * tx + 7, 2 * ty + 1)] + \
+             [(int(rng.integers(1, 400)), int(rng.integers(1, 90))) for _ in range(4)]
+    for nx, ny in shapes:
+        pitch = (nx + 31) // 32 * 32
+        plane = pitch * ny
+        for periodic in range(4):
+            px, py = bool(periodic & 1), bool(periodic & 2)
+
+            def wc(g, n, per):
+                inside = (g >= 0) & (g < n)
+                w = np.where(per, np.mod(g, n), np.clip(g, 0, n - 1))
+                return np.where(inside, g, w), inside | per
+
+            for bx in range((nx + tx - 1) // tx):
+                for by in range((ny + ty - 1) // ty):
+                    x0, y0 = bx * tx, by * ty
+                    # loads of the two-cell halo tile
+                    j, i = np.divmod(np.arange(n_in), iw)
+                    gx, _ = wc(x0 - 2 + i, nx, px)
+                    gy, _ = wc(y0 - 2 + j, ny, py)
+                    g = gy * pitch + gx
+                    assert g.min() >= 0 and g.max() < plane
+                    # link words of the mid tile
+                    j, i = np.divmod(np.arange(n_mid), mw)
+                    gx, inx = wc(x0 - 1 + i, nx, px)
+                    gy, iny = wc(y0 - 1 + j, ny, py)
+                    assert (gy * pitch + gx).min() >= 0 and (gy * pitch + gx).max() < plane
+                    # first step: pulls from the in tile around (i + 1, j + 1)
+                    c = (j + 1) * iw + (i + 1)
+                    for q in range(9):
+                        s = c - CY[q] * iw - CX[q]
+                        assert s.min() >= 0 and s.max() < n_in
+                    # second step: pulls from the mid tile around (i + 1, j + 1), stores in the planes
+                    j, i = np.divmod(np.arange(tx * ty), tx)
+                    keep = (x0 + i < nx) & (y0 + j < ny)
+                    m = (j + 1) * mw + (i + 1)
+                    assert m.max() < n_mid
+                    for q in range(9):
+                        s = m - CY[q] * mw - CX[q]
+                        assert s.min() >= 0 and s.max() < n_mid
+                    gs = (y0 + j[keep]) * pitch + x0 + i[keep]
+                    if gs.size:
+                        assert gs.min() >= 0 and gs.max() < plane
