@@ -45,47 +45,80 @@ __device__ __forceinline__ int wrap_or_clamp(int g, int n, bool periodic, bool &
     return g < 0 ? 0 : n - 1;
 }
 
-// populations of the cell at (ci, cj) of a tile T[9][H][W] (row width W), its pulls from
-// (ci - c_x, cj - c_y), replaced by its own opposite population where link bit q - 1 is set (plus
-// the moving-wall term where bit q + 7 is)
-template <class S, class R, int W, int N>
-__device__ __forceinline__ void gather_tile(const S *T, int ci, int cj, uint32_t L, Vec2<R> uw, R h[9]) {
+// Populations of the cells (ci, cj) and (ci + 1, cj) of a tile T[9][H][W] (row width W, N cells a
+// plane) as FP32 pairs: their pulls from (ci - c_x, cj - c_y), replaced by the cell's own opposite
+// population where link bit q - 1 is set (plus the moving-wall term where bit q + 7 is).
+template <class S, int W, int N>
+__device__ __forceinline__ void gather_pair(const S *T, int ci, int cj, uint32_t L0, uint32_t L1, Vec2<float> uw,
+                                            float2 h[9]) {
     const int c = cj * W + ci;
 #pragma unroll
-    for (int q = 0; q < 9; ++q) h[q] = Store<S>::to(T[q * N + c - cy(q) * W - cx(q)]);
-    if (L) {
+    for (int q = 0; q < 9; ++q) {
+        const int s = q * N + c - cy(q) * W - cx(q);
+        h[q] = make_float2(Store<S>::to(T[s]), Store<S>::to(T[s + 1]));
+    }
+    if (L0 | L1) {
 #pragma unroll
         for (int q = 1; q < 9; ++q) {
-            if (L & (1u << (q - 1))) {
-                R v = Store<S>::to(T[opp(q) * N + c]);
-                if (L & (1u << (q + 7))) v = add_(v, wall_term<S, R>(q, uw));
-                h[q] = v;
+            const uint32_t b = 1u << (q - 1), wb = 1u << (q + 7);
+            if ((L0 | L1) & b) {
+                const int o = opp(q) * N + c;
+                if (L0 & b) {
+                    float v = Store<S>::to(T[o]);
+                    if (L0 & wb) v = add_(v, wall_term<S, float>(q, uw));
+                    h[q].x = v;
+                }
+                if (L1 & b) {
+                    float v = Store<S>::to(T[o + 1]);
+                    if (L1 & wb) v = add_(v, wall_term<S, float>(q, uw));
+                    h[q].y = v;
+                }
             }
         }
     }
 }
 
+// V consecutive storage elements as one access (2 for the pairs here)
+template <class S>
+struct PairRaw {
+    using T = typename RawPack<2 * sizeof(S)>::T;
+};
+
 template <class S, int TX, int TY, bool FORCE>
 __device__ __forceinline__ void two_steps(const S *__restrict__ src, S *__restrict__ dst,
                                           const uint16_t *__restrict__ links, int nx, int ny, int pitch,
                                           int plane, int periodic, const D2Q9Params &prm, unsigned char *smem) {
-    using R = typename Store<S>::R;
     using Lay = Layout<S, TX, TY>;
+    using P = typename PairRaw<S>::T;  // two elements of storage
+    static_assert(TX % 2 == 0 && Lay::IW % 2 == 0 && Lay::MW % 2 == 0, "cells go in pairs");
     S *in = reinterpret_cast<S *>(smem);
     S *mid = reinterpret_cast<S *>(smem + Lay::in_bytes);
     uint16_t *lk = reinterpret_cast<uint16_t *>(smem + Lay::in_bytes + Lay::mid_bytes);
     const int x0 = (int)blockIdx.x * TX, y0 = (int)blockIdx.y * TY;
     const bool px = periodic & 1, py = periodic & 2;
 
-    // the source tile with its two-cell halo (wrapped when periodic, clamped otherwise)
-    for (int k = (int)threadIdx.x; k < Lay::IN; k += THREADS) {
-        const int j = k / Lay::IW, i = k - j * Lay::IW;
-        bool inside = true;
-        const int gx = wrap_or_clamp(x0 - 2 + i, nx, px, inside);
-        const int gy = wrap_or_clamp(y0 - 2 + j, ny, py, inside);
-        const int g = gy * pitch + gx;
+    // the source tile with its two-cell halo, a pair of cells at a time (wrapped when periodic,
+    // clamped otherwise); a pair that is not two consecutive elements of one row goes one by one
+    for (int k = (int)threadIdx.x; k < Lay::IN / 2; k += THREADS) {
+        const int j = k / (Lay::IW / 2), i = 2 * (k - j * (Lay::IW / 2));
+        bool in0 = true, in1 = true, iny = true;
+        const int gx0 = wrap_or_clamp(x0 - 2 + i, nx, px, in0);
+        const int gx1 = wrap_or_clamp(x0 - 1 + i, nx, px, in1);
+        const int gy = wrap_or_clamp(y0 - 2 + j, ny, py, iny);
+        const int g = gy * pitch + gx0;
+        const int t = j * Lay::IW + i;
+        if (gx1 == gx0 + 1 && (gx0 & 1) == 0) {
 #pragma unroll
-        for (int q = 0; q < 9; ++q) in[q * Lay::IN + k] = __ldg(src + (size_t)q * plane + g);
+            for (int q = 0; q < 9; ++q)
+                *reinterpret_cast<P *>(in + q * Lay::IN + t) = __ldg(reinterpret_cast<const P *>(src + (size_t)q * plane + g));
+        } else {
+            const int g1 = gy * pitch + gx1;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                in[q * Lay::IN + t] = __ldg(src + (size_t)q * plane + g);
+                in[q * Lay::IN + t + 1] = __ldg(src + (size_t)q * plane + g1);
+            }
+        }
     }
     // the link words of the first step's tile; 0xFFFF marks a cell outside the domain
     for (int k = (int)threadIdx.x; k < Lay::MN; k += THREADS) {
@@ -97,35 +130,62 @@ __device__ __forceinline__ void two_steps(const S *__restrict__ src, S *__restri
     }
     __syncthreads();
 
-    const R om = omega<R>(prm);
-    const Vec2<R> F = force<R>(prm), uw = wall_u<R>(prm);
-    // first step: the tile grown by one cell (mid cell (i, j) is in-tile cell (i + 1, j + 1))
-    for (int k = (int)threadIdx.x; k < Lay::MN; k += THREADS) {
-        const uint32_t L = lk[k];
-        if (L == 0xFFFFu || L == LINK_SOLID) continue;  // outside the domain, or solid: never read
-        const int j = k / Lay::MW, i = k - j * Lay::MW;
-        R h[9];
-        gather_tile<S, R, Lay::IW, Lay::IN>(in, i + 1, j + 1, L, uw, h);
-        collide<S, R, FORCE>(h, om, F);
+    const float om = omega<float>(prm);
+    const Vec2<float> F = force<float>(prm), uw = wall_u<float>(prm);
+    // first step, two cells at a time: the tile grown by one cell (mid cell (i, j) is in-tile cell
+    // (i + 1, j + 1)).  A cell outside the domain or solid is computed from whatever its tile holds
+    // and its result never read.
+    for (int k = (int)threadIdx.x; k < Lay::MN / 2; k += THREADS) {
+        const int j = k / (Lay::MW / 2), i = 2 * (k - j * (Lay::MW / 2));
+        const int m = j * Lay::MW + i;
+        const uint32_t L0 = lk[m], L1 = lk[m + 1];
+        float2 h[9];
+        gather_pair<S, Lay::IW, Lay::IN>(in, i + 1, j + 1, L0 == LINK_SOLID ? 0u : L0, L1 == LINK_SOLID ? 0u : L1,
+                                         uw, h);
+        collide_t<S, float2, FORCE>(h, om, F);
 #pragma unroll
-        for (int q = 0; q < 9; ++q) mid[q * Lay::MN + k] = Store<S>::from(h[q]);
+        for (int q = 0; q < 9; ++q) {
+            const S a = Store<S>::from(h[q].x), b = Store<S>::from(h[q].y);
+            mid[q * Lay::MN + m] = a;
+            mid[q * Lay::MN + m + 1] = b;
+        }
     }
     __syncthreads();
 
-    // second step: the tile itself (output cell (i, j) is mid cell (i + 1, j + 1)), into dst
-    for (int k = (int)threadIdx.x; k < TX * TY; k += THREADS) {
-        const int j = k / TX, i = k - j * TX;
+    // second step, two cells at a time: the tile itself (output cell (i, j) is mid cell
+    // (i + 1, j + 1)), into dst; solid cells and cells beyond the domain are not written
+    for (int k = (int)threadIdx.x; k < TX * TY / 2; k += THREADS) {
+        const int j = k / (TX / 2), i = 2 * (k - j * (TX / 2));
         const int x = x0 + i, y = y0 + j;
         if (x >= nx || y >= ny) continue;
         const int m = (j + 1) * Lay::MW + (i + 1);
-        const uint32_t L = lk[m];
-        if (L == LINK_SOLID) continue;
-        R h[9];
-        gather_tile<S, R, Lay::MW, Lay::MN>(mid, i + 1, j + 1, L, uw, h);
-        collide<S, R, FORCE>(h, om, F);
+        const uint32_t L0 = lk[m], L1 = lk[m + 1];
+        const bool w0 = L0 != LINK_SOLID, w1 = x + 1 < nx && L1 != LINK_SOLID && L1 != 0xFFFFu;
+        if (!w0 && !w1) continue;
+        float2 h[9];
+        gather_pair<S, Lay::MW, Lay::MN>(mid, i + 1, j + 1, w0 ? L0 : 0u, w1 ? L1 : 0u, uw, h);
+        collide_t<S, float2, FORCE>(h, om, F);
         const int g = y * pitch + x;
+        if (w0 && w1) {
 #pragma unroll
-        for (int q = 0; q < 9; ++q) dst[(size_t)q * plane + g] = Store<S>::from(h[q]);
+            for (int q = 0; q < 9; ++q) {
+                P raw;
+                if constexpr (sizeof(S) == 2) {
+                    const typename Pair<S>::P p2 = Pair<S>::from(h[q].x, h[q].y);
+                    memcpy(&raw, &p2, sizeof(raw));
+                } else {
+                    const S e[2] = {Store<S>::from(h[q].x), Store<S>::from(h[q].y)};
+                    memcpy(&raw, e, sizeof(raw));
+                }
+                *reinterpret_cast<P *>(dst + (size_t)q * plane + g) = raw;
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                if (w0) dst[(size_t)q * plane + g] = Store<S>::from(h[q].x);
+                if (w1) dst[(size_t)q * plane + g + 1] = Store<S>::from(h[q].y);
+            }
+        }
     }
 }
 
