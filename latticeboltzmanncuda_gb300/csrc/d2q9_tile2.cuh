@@ -7,12 +7,14 @@
 // per two updates; the halo's first-step cells are computed by both neighbouring blocks.
 //
 // Per cell the update is scalar_cell()'s (d2q9_vec.cuh) -- the same pulls, bounce-back and
-// moving-wall terms, and the same collide() -- and the first step's values are held in the storage
+// moving-wall terms, and the same collision -- and the first step's values are held in the storage
 // type, rounded as the one-step kernel stores them, so two steps here are bit-identical to two
 // launches of the one-step kernels.  Solid cells are not written (their values are never read:
 // a pull from a solid cell is replaced by bounce-back).  Halo cells outside a non-periodic domain
-// are loaded from a clamped position and never computed: a cell at the domain edge replaces every
-// pull from outside by bounce-back.
+// are loaded from a clamped position; their first-step values are computed from whatever the tile
+// holds and never read: a cell at the domain edge replaces every pull from outside by bounce-back.
+// Cells go two at a time (adjacent in a row) through the packed FP32 collision, which rounds each
+// lane as the scalar one does.
 #pragma once
 
 #include "d2q9_core.cuh"
@@ -120,7 +122,8 @@ __device__ __forceinline__ void two_steps(const S *__restrict__ src, S *__restri
             }
         }
     }
-    // the link words of the first step's tile; 0xFFFF marks a cell outside the domain
+    // the link words of the first step's tile; 0xFFFF for a cell outside the domain (only the first
+    // step reads it there, and computes that cell from garbage that no output cell reads)
     for (int k = (int)threadIdx.x; k < Lay::MN; k += THREADS) {
         const int j = k / Lay::MW, i = k - j * Lay::MW;
         bool inside = true;
@@ -160,7 +163,8 @@ __device__ __forceinline__ void two_steps(const S *__restrict__ src, S *__restri
         if (x >= nx || y >= ny) continue;
         const int m = (j + 1) * Lay::MW + (i + 1);
         const uint32_t L0 = lk[m], L1 = lk[m + 1];
-        const bool w0 = L0 != LINK_SOLID, w1 = x + 1 < nx && L1 != LINK_SOLID && L1 != 0xFFFFu;
+        // (an output cell lies in the domain: its word is its link word, never the outside marker)
+        const bool w0 = L0 != LINK_SOLID, w1 = x + 1 < nx && L1 != LINK_SOLID;
         if (!w0 && !w1) continue;
         float2 h[9];
         gather_pair<S, Lay::MW, Lay::MN>(mid, i + 1, j + 1, w0 ? L0 : 0u, w1 ? L1 : 0u, uw, h);
