@@ -229,7 +229,9 @@ LBM_API lbm_status lbm_step_force_series(lbm_ctx *ctx, int32_t nsteps, float *ho
  * rows_per_block cells (64 x 8, 64 x 16 or 128 x 8; l2_policy 0; FP32 and 16-bit storage): each
  * block loads its tile with a two-cell halo, computes the first step on the tile grown by one cell
  * and the second into the destination, so the populations cross HBM once per two updates (an odd
- * last step of a call runs the one-step kernel).  Every shape gives bit-identical populations. */
+ * last step of a call runs the one-step kernel).  cells_per_thread -3 is the same with persistent
+ * blocks (64 x 4 or 64 x 8 tiles) that copy the next tile into a second buffer by cp.async while
+ * they compute the current one.  Every shape gives bit-identical populations. */
 LBM_API lbm_status lbm_autotune(lbm_ctx *ctx, int32_t retune);
 LBM_API lbm_status lbm_set_launch(lbm_ctx *ctx, int32_t cells_per_thread, int32_t block_threads,
                                   int32_t rows_per_block, int32_t l2_policy);

@@ -381,6 +381,61 @@ cudaError_t launch_tile2_t(lbm_ctx *ctx, const S *src, S *dst, const D2Q9Params 
 // the tile shapes of the two-step kernel
 inline bool tile2_shape(int tx, int ty) { return (tx == 64 && (ty == 8 || ty == 16)) || (tx == 128 && ty == 8); }
 
+// v == TILE2P: the persistent two-step kernel (the next tile's copies in flight while a tile is
+// computed), tiles of 64 x 4 or 64 x 8 cells
+constexpr int TILE2P = -3;
+inline bool tile2p_shape(int tx, int ty) { return tx == 64 && (ty == 4 || ty == 8); }
+
+// 256 threads a block (512 measured slower: FP32 81.8k against 83.3k MLUPS on 64 x 8 tiles)
+constexpr int TILE2P_THREADS = 256;
+
+template <class S, int TX, int TY, bool FORCE>
+__global__ void __launch_bounds__(TILE2P_THREADS) tile2p_kernel(const S *__restrict__ src, S *__restrict__ dst,
+                                                                     const uint16_t *__restrict__ links, int nx,
+                                                                     int ny, int pitch, int plane, int periodic,
+                                                                     D2Q9Params prm, int tiles_x, int ntiles) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    d2q9::tile2::two_steps_persistent<S, TX, TY, FORCE, TILE2P_THREADS>(src, dst, links, nx, ny, pitch, plane,
+                                                                        periodic, prm, smem, tiles_x, ntiles);
+}
+
+template <class S, int TX, int TY, bool FORCE>
+cudaError_t launch_tile2p_t(lbm_ctx *ctx, const S *src, S *dst, const D2Q9Params &prm) {
+    constexpr size_t bytes = d2q9::tile2::LayoutP<S, TX, TY>::bytes;
+    static int per_sm = 0;  // per instantiation: resident blocks per SM, from the occupancy calculator
+    if (per_sm == 0) {
+        cudaError_t e = cudaFuncSetAttribute(tile2p_kernel<S, TX, TY, FORCE>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tile2p_kernel<S, TX, TY, FORCE>,
+                                                              TILE2P_THREADS, bytes);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    }
+    int sms = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (e != cudaSuccess) return e;
+    const lbm_desc &d = ctx->desc;
+    const int tiles_x = (d.nx + TX - 1) / TX, ntiles = tiles_x * ((d.ny + TY - 1) / TY);
+    const int grid = std::min(ntiles, per_sm * sms);
+    tile2p_kernel<S, TX, TY, FORCE><<<grid, TILE2P_THREADS, bytes, ctx->stream>>>(
+        src, dst, ctx->links_d, d.nx, d.ny, (int)ctx->pitch, (int)ctx->plane, d.periodic, prm, tiles_x, ntiles);
+    return cudaGetLastError();
+}
+
+template <class S>
+cudaError_t launch_tile2p(lbm_ctx *ctx, int tx, int ty, const S *src, S *dst) {
+    if constexpr (sizeof(S) > 4) {
+        return cudaErrorInvalidValue;
+    } else {
+        const D2Q9Params prm = d2q9_params(ctx->desc);
+        const bool f = prm.fx != 0.0f || prm.fy != 0.0f;
+        if (tx == 64 && ty == 4) return f ? launch_tile2p_t<S, 64, 4, true>(ctx, src, dst, prm) : launch_tile2p_t<S, 64, 4, false>(ctx, src, dst, prm);
+        if (tx == 64 && ty == 8) return f ? launch_tile2p_t<S, 64, 8, true>(ctx, src, dst, prm) : launch_tile2p_t<S, 64, 8, false>(ctx, src, dst, prm);
+        return cudaErrorInvalidValue;
+    }
+}
+
 template <class S>
 cudaError_t launch_tile2(lbm_ctx *ctx, int tx, int ty, const S *src, S *dst) {
     if constexpr (sizeof(S) > 4) {
@@ -423,7 +478,8 @@ cudaError_t launch_one(lbm_ctx *ctx, const Shape &sh, const S *src, S *dst, int 
         }
         return cudaGetLastError();
     }
-    if (sh.v == TILE2) return launch_tile2<S>(ctx, sh.tx, sh.ty, src, dst);  // two steps
+    if (sh.v == TILE2) return launch_tile2<S>(ctx, sh.tx, sh.ty, src, dst);    // two steps
+    if (sh.v == TILE2P) return launch_tile2p<S>(ctx, sh.tx, sh.ty, src, dst);  // two steps, persistent
     const int pitch = (int)ctx->pitch, plane = (int)ctx->plane;
     if (sh.v == 0) {  // bulk-copy pipeline
         if constexpr (sizeof(S) == 2)
@@ -457,8 +513,10 @@ std::vector<Shape> candidates(const lbm_ctx *ctx) {
     if (!small_index(ctx)) return c;
     if (sizeof(S) == 2)  // the bulk-copy pipeline
         for (int pol : {0, 1, 2}) c.push_back({0, d2q9::bulk::threads<4>(), 1, pol});
-    if (sizeof(S) <= 4)  // two steps per launch on shared-memory tiles
+    if (sizeof(S) <= 4) {  // two steps per launch on shared-memory tiles
         for (const auto &t : {std::pair<int, int>{64, 8}, {64, 16}, {128, 8}}) c.push_back({TILE2, t.first, t.second, 0});
+        for (int ty : {4, 8}) c.push_back({TILE2P, 64, ty, 0});
+    }
     for (int v : {2, 4, 8}) {
         if (!vec_ok<S>(v) || ctx->pitch % v) continue;
         const int per_row = (int)(ctx->pitch / v);
@@ -572,7 +630,7 @@ cudaError_t tune(lbm_ctx *ctx) {
         float t = 0.0f;
         cudaEventElapsedTime(&t, e0, e1);
         if (sh.v == 0 && d2q9_take_pipe_status(ctx) != 0) return cudaSuccess;  // a bounded wait gave up
-        ms = sh.v == TILE2 ? 0.5f * t : t;  // per time step: a two-step launch counts twice
+        ms = (sh.v == TILE2 || sh.v == TILE2P) ? 0.5f * t : t;  // per time step: a two-step launch counts twice
         return cudaSuccess;
     };
     const std::vector<Shape> cands = candidates<S>(ctx);
@@ -631,7 +689,7 @@ cudaError_t launch_step(lbm_ctx *ctx, int nsteps) {
         if (e != cudaSuccess) return e;
     }
     const Shape sh{ctx->cells_per_thread, ctx->block_threads, ctx->rows_per_block, ctx->l2_policy};
-    if (sh.v == TILE2) {
+    if (sh.v == TILE2 || sh.v == TILE2P) {
         // two steps per launch; an odd last step by the one-step vector kernel (bit-identical)
         for (int s = 0; s + 1 < nsteps; s += 2) {
             cudaError_t e = launch_one<S>(ctx, sh, static_cast<const S *>(ctx->f[ctx->cur]),
@@ -721,6 +779,8 @@ cudaError_t d2q9_init_equilibrium(lbm_ctx *ctx, const float *rho_d, const float 
 bool d2q9_shape_valid(const lbm_ctx *ctx, int v, int tx, int ty, int pol) {
     if (v == TILE2)  // two-step tiles: FP32 and 16-bit storage
         return ctx->desc.dtype != LBM_F64 && tile2_shape(tx, ty) && pol == 0 && small_index(ctx);
+    if (v == TILE2P)  // persistent two-step tiles
+        return ctx->desc.dtype != LBM_F64 && tile2p_shape(tx, ty) && pol == 0 && small_index(ctx);
     if (v == 0)  // bulk-copy pipeline: 16-bit storage, fixed block shape, three ring variants
         return (ctx->desc.dtype == LBM_F16S || ctx->desc.dtype == LBM_BF16S) &&
                tx == d2q9::bulk::threads<4>() && ty == 1 &&

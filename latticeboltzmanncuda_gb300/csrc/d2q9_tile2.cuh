@@ -193,6 +193,136 @@ __device__ __forceinline__ void two_steps(const S *__restrict__ src, S *__restri
     }
 }
 
+// Persistent form: a block loops over tiles t = blockIdx.x, blockIdx.x + gridDim.x, ... and issues
+// the next tile's copies (`cp.async`: the populations and the link words of the loaded tile, two
+// aligned elements at a time) into the second of two input buffers before it computes the current
+// tile, so the copies overlap the arithmetic.  The link words are taken over the loaded tile (the
+// first step's cells are its interior); a cell outside a non-periodic domain carries the link word
+// of the clamped position, and like every other first-step cell outside the domain its result is
+// never read.
+template <class S, int TX, int TY>
+struct LayoutP {
+    using L = Layout<S, TX, TY>;
+    static constexpr size_t in_bytes = L::in_bytes;                             // one input buffer
+    static constexpr size_t lk_bytes = (size_t)L::IN * sizeof(uint16_t);        // its link words
+    static constexpr size_t buf_bytes = (in_bytes + lk_bytes + 15) / 16 * 16;   // one buffer
+    static constexpr size_t bytes = 2 * buf_bytes + L::mid_bytes;
+};
+
+template <int BYTES>
+__device__ __forceinline__ void copy_async(void *smem_dst, const void *gmem_src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(gmem_src), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void copy_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void copy_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+template <class S, int TX, int TY, int NT>
+__device__ __forceinline__ void issue_tile(const S *__restrict__ src, const uint16_t *__restrict__ links, int nx,
+                                           int ny, int pitch, int plane, bool px, bool py, int x0, int y0, S *in,
+                                           uint16_t *lk) {
+    using Lay = Layout<S, TX, TY>;
+    using P = typename PairRaw<S>::T;
+    for (int k = (int)threadIdx.x; k < Lay::IN / 2; k += NT) {
+        const int j = k / (Lay::IW / 2), i = 2 * (k - j * (Lay::IW / 2));
+        bool in0 = true, in1 = true, iny = true;
+        const int gx0 = wrap_or_clamp(x0 - 2 + i, nx, px, in0);
+        const int gx1 = wrap_or_clamp(x0 - 1 + i, nx, px, in1);
+        const int gy = wrap_or_clamp(y0 - 2 + j, ny, py, iny);
+        const int g = gy * pitch + gx0;
+        const int t = j * Lay::IW + i;
+        if (gx1 == gx0 + 1 && (gx0 & 1) == 0) {
+#pragma unroll
+            for (int q = 0; q < 9; ++q) copy_async<sizeof(P)>(in + q * Lay::IN + t, src + (size_t)q * plane + g);
+            copy_async<4>(lk + t, links + g);
+        } else {
+            const int g1 = gy * pitch + gx1;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                in[q * Lay::IN + t] = __ldg(src + (size_t)q * plane + g);
+                in[q * Lay::IN + t + 1] = __ldg(src + (size_t)q * plane + g1);
+            }
+            lk[t] = __ldg(links + g);
+            lk[t + 1] = __ldg(links + g1);
+        }
+    }
+}
+
+template <class S, int TX, int TY, bool FORCE, int NT>
+__device__ __forceinline__ void two_steps_persistent(const S *__restrict__ src, S *__restrict__ dst,
+                                                     const uint16_t *__restrict__ links, int nx, int ny, int pitch,
+                                                     int plane, int periodic, const D2Q9Params &prm,
+                                                     unsigned char *smem, int tiles_x, int ntiles) {
+    using Lay = Layout<S, TX, TY>;
+    using LP = LayoutP<S, TX, TY>;
+    static_assert(TX % 2 == 0 && Lay::IW % 2 == 0 && Lay::MW % 2 == 0, "cells go in pairs");
+    // input buffer b: its populations at b * buf_bytes, its link words behind them
+    auto inb = [&](int b) { return reinterpret_cast<S *>(smem + (size_t)b * LP::buf_bytes); };
+    auto lkb = [&](int b) { return reinterpret_cast<uint16_t *>(smem + (size_t)b * LP::buf_bytes + LP::in_bytes); };
+    S *mid = reinterpret_cast<S *>(smem + 2 * LP::buf_bytes);
+    const bool px = periodic & 1, py = periodic & 2;
+    const float om = omega<float>(prm);
+    const Vec2<float> F = force<float>(prm), uw = wall_u<float>(prm);
+
+    int t = (int)blockIdx.x, buf = 0;
+    if (t < ntiles)
+        issue_tile<S, TX, TY, NT>(src, links, nx, ny, pitch, plane, px, py, (t % tiles_x) * TX,
+                                  (t / tiles_x) * TY, inb(0), lkb(0));
+    copy_async_commit();
+    for (; t < ntiles; t += (int)gridDim.x) {
+        const int tn = t + (int)gridDim.x;
+        if (tn < ntiles)  // the next tile's copies, in flight while this tile is computed
+            issue_tile<S, TX, TY, NT>(src, links, nx, ny, pitch, plane, px, py, (tn % tiles_x) * TX,
+                                  (tn / tiles_x) * TY, inb(buf ^ 1), lkb(buf ^ 1));
+        copy_async_commit();
+        copy_async_wait<1>();  // this tile's copies (all but the group just issued)
+        __syncthreads();
+        const S *in = inb(buf);
+        const uint16_t *lk = lkb(buf);
+        const int x0 = (t % tiles_x) * TX, y0 = (t / tiles_x) * TY;
+        // first step on the tile grown by one cell, two adjacent cells at a time
+        for (int k = (int)threadIdx.x; k < Lay::MN / 2; k += NT) {
+            const int j = k / (Lay::MW / 2), i = 2 * (k - j * (Lay::MW / 2));
+            const int c = (j + 1) * Lay::IW + (i + 1);
+            const uint32_t L0 = lk[c], L1 = lk[c + 1];
+            float2 h[9];
+            gather_pair<S, Lay::IW, Lay::IN>(in, i + 1, j + 1, L0 == LINK_SOLID ? 0u : L0,
+                                             L1 == LINK_SOLID ? 0u : L1, uw, h);
+            collide_t<S, float2, FORCE>(h, om, F);
+            const int m = j * Lay::MW + i;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                mid[q * Lay::MN + m] = Store<S>::from(h[q].x);
+                mid[q * Lay::MN + m + 1] = Store<S>::from(h[q].y);
+            }
+        }
+        __syncthreads();
+        // second step on the tile itself, two adjacent cells at a time, into dst
+        for (int k = (int)threadIdx.x; k < TX * TY / 2; k += NT) {
+            const int j = k / (TX / 2), i = 2 * (k - j * (TX / 2));
+            const int x = x0 + i, y = y0 + j;
+            if (x >= nx || y >= ny) continue;
+            const int c = (j + 2) * Lay::IW + (i + 2);
+            const uint32_t L0 = lk[c], L1 = lk[c + 1];
+            const bool w0 = L0 != LINK_SOLID, w1 = x + 1 < nx && L1 != LINK_SOLID;
+            if (!w0 && !w1) continue;
+            float2 h[9];
+            gather_pair<S, Lay::MW, Lay::MN>(mid, i + 1, j + 1, w0 ? L0 : 0u, w1 ? L1 : 0u, uw, h);
+            collide_t<S, float2, FORCE>(h, om, F);
+            const int g = y * pitch + x;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                if (w0) dst[(size_t)q * plane + g] = Store<S>::from(h[q].x);
+                if (w1) dst[(size_t)q * plane + g + 1] = Store<S>::from(h[q].y);
+            }
+        }
+        __syncthreads();  // every thread is done with this buffer and with mid
+        buf ^= 1;
+    }
+    copy_async_wait<0>();  // nothing left in flight when the block ends
+}
+
 }  // namespace tile2
 }  // namespace d2q9
 }  // namespace lbm

@@ -207,12 +207,13 @@ def test_steps_are_deterministic():
 # field the ring variant)
 SHAPES = [(1, 256, 1, 0), (1, 128, 2, 0), (2, 64, 1, 0), (2, 32, 4, 1), (4, 32, 1, 2), (4, 64, 2, 0),
           (4, 128, 1, 1), (8, 32, 1, 1), (8, 64, 2, 2), (0, 160, 1, 0), (0, 160, 1, 1), (0, 160, 1, 2),
-          (-2, 64, 8, 0), (-2, 64, 16, 0), (-2, 128, 8, 0)]  # -2: two steps per launch on shared-memory tiles
+          (-2, 64, 8, 0), (-2, 64, 16, 0), (-2, 128, 8, 0),   # -2: two steps per launch on shared-memory tiles
+          (-3, 64, 4, 0), (-3, 64, 8, 0)]                       # -3: the same with persistent blocks
 
 
 def shape_ok(dtype, v):
-    return v == 1 or (dtype == "f32" and v in (2, 4, -2)) or (dtype in ("f16s", "bf16s") and v in (0, 2, 4, 8, -2)) \
-        or (dtype == "f64" and v == 2)
+    return v == 1 or (dtype == "f32" and v in (2, 4, -2, -3)) or \
+        (dtype in ("f16s", "bf16s") and v in (0, 2, 4, 8, -2, -3)) or (dtype == "f64" and v == 2)
 
 
 @pytest.mark.parametrize("shape", SHAPES)
@@ -302,6 +303,8 @@ def test_autotune_picks_a_valid_shape_and_keeps_state():
         v, tx, ty, pol = L.autotune(retune=True)
         if v == -2:  # two steps per launch on tiles of tx x ty cells
             assert (tx, ty) in ((64, 8), (64, 16), (128, 8)) and pol == 0
+        elif v == -3:  # the same with persistent blocks
+            assert (tx, ty) in ((64, 4), (64, 8)) and pol == 0
         else:
             assert v in (1, 2, 4) and tx % 32 == 0 and tx * ty <= 256 and pol in (0, 1, 2)
         assert L.info()["tuned"] == 1
@@ -458,7 +461,7 @@ def test_two_step_tiles_match_the_one_step_kernel(dtype, periodic):
             flags[ny // 3, ::5] = lbm.MOVING_WALL
         f0 = random_state(nx, ny, 31 + periodic + nx)
         outs = []
-        for shape in ((2, 64, 1, 0), (-2, 64, 8, 0), (-2, 64, 16, 0), (-2, 128, 8, 0)):
+        for shape in ((2, 64, 1, 0), (-2, 64, 8, 0), (-2, 64, 16, 0), (-2, 128, 8, 0), (-3, 64, 4, 0), (-3, 64, 8, 0)):
             with lbm.Lattice(nx, ny, dtype=dtype, tau=0.57, periodic=periodic, body_force=(1e-5, -3e-6, 0),
                              wall_velocity=(0.03, 0.01, 0)) as L:
                 L.set_flags(flags)

@@ -588,7 +588,8 @@ def test_d3q27_prefetch_stays_in_the_population_buffer(dims):
 CX = [0, 1, 0, -1, 0, 1, -1, -1, 1]  # c_x of the D2Q9 populations
 
 
-@pytest.mark.parametrize("elem,tx,ty", [(4, 64, 8), (4, 64, 16), (4, 128, 8), (2, 64, 8), (2, 64, 16), (2, 128, 8)])
+@pytest.mark.parametrize("elem,tx,ty", [(4, 64, 8), (4, 64, 16), (4, 128, 8), (2, 64, 8), (2, 64, 16), (2, 128, 8),
+                                         (4, 64, 4), (2, 64, 4)])
 def test_two_step_tile_indexing(elem, tx, ty):
     """d2q9_tile2.cuh: every global load and store lies in the planes, every shared-memory index in
     its tile, for domains smaller and larger than a tile, periodic or not; the shared memory fits."""
@@ -596,6 +597,9 @@ def test_two_step_tile_indexing(elem, tx, ty):
     n_in, n_mid = iw * ih, mw * mh
     smem = 9 * n_in * elem + 9 * n_mid * elem + n_mid * 2
     assert smem <= 227 * 1024
+    # the persistent form: two input buffers with the link words of the loaded tile, then mid
+    buf = (9 * n_in * elem + n_in * 2 + 15) // 16 * 16
+    assert 2 * buf + 9 * n_mid * elem <= 227 * 1024 and (9 * n_in * elem) % 16 == 0
     rng = np.random.default_rng(tx * 100 + ty + elem)
     shapes = [(1, 1), (5, 3), (tx, ty), (tx + 1, ty + 3), (3 * tx + 7, 2 * ty + 1)] + \
              [(int(rng.integers(1, 400)), int(rng.integers(1, 90))) for _ in range(4)]
