@@ -1,5 +1,6 @@
 // Batched D2Q9: many independent domains of uneven size, tau, forcing and obstacle mask advance
-// together, one kernel launch per time step for all of them.
+// together, one kernel launch per time step for all of them (a batch of few cells: one persistent
+// cooperative launch per step sequence, its blocks meeting after each step).
 //
 // Each domain (a "slot") owns one allocation -- its two population buffers, link words, flags and
 // fluid-cell count -- made when it is added, so slots come and go without moving anyone else's
@@ -10,10 +11,12 @@
 // one ended, on data still in L2).  Up to PARAM_SLOTS live slots (FP32, 16-bit storage) the slot
 // descriptors (size, buffer base, parity, step budget, relaxation rate, force, wall velocity,
 // periodicity) and the first tile of every slot travel in the kernel's parameter block, a block
-// finds its slot by a binary search over those, and a tile is a run of TX * TY * V consecutive
-// cells of the slot's padded cell array; beyond that, and for FP64, a device table of descriptors
-// and a tile list (slot, x-chunk, first row: TY rows x TX * V cells) do.  The tile shape (V, TX,
-// TY) is picked by the autotuner from timings on the batch itself.
+// finds its slot by a binary search over those; with 16-bit storage a tile is a run of TX * TY * V
+// consecutive cells of the slot's padded cell array (and its first thread prefetches into L2 the
+// tile 32k cells further along the slot), with FP32 a band of TY rows of TX * V cells; beyond that,
+// and for FP64, a device table of descriptors and a tile list (slot, x-chunk, first row: TY rows x
+// TX * V cells) do.  The tile shape (V, TX, TY) is picked by the autotuner from timings on the batch
+// itself.
 //
 // Nothing on the serving path waits for the device: adding a slot (flags upload, link words,
 // fluid-cell count, equilibrium), the table uploads before a launch sequence, freeing a slot and
