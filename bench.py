@@ -13,7 +13,8 @@ Arm "mine" (default) prints one JSON line with
              domain, no data-path collective)
   e2e        the same solve through the C ABI from pinned host buffers: flags + initial populations
              host->device, 10,000 steps, density/velocity device->host, every step
-  roofline   step kernel: algorithmic bytes per launch (72 B x cells) / average launch duration
+  roofline   step kernel: algorithmic bytes per launch (72 B x fluid cells: one read and one write of
+             each population) / average launch duration
   cpu_baseline  the CPU oracle (OpenMP, all host cores) on a bounded sample of the same workload
   batched_vs_plain / served_vs_plain (one GPU only; --no-legs skips them): the other half of the
              metric, each leg run once after the headline -- the 512-domain batch (2000 steps) in
@@ -24,6 +25,10 @@ Arm "mine" (default) prints one JSON line with
              results against FP64 solves of the same domains; details under "legs"
 Arm "reference" times the CPU restatement of the step on the host cores (the reference has no CPU
 implementation of its own) on the same workload and prints the same kind of line.
+
+Other workloads (--workload): batch, serve (the legs above on their own), tgv (Taylor-Green decay
+and errors per storage type), d3q27 (the reference-mode step on the 128^3 sphere model),
+persistent (small batches: one launch per step against one persistent launch per sequence).
 """
 from __future__ import annotations
 

@@ -1,7 +1,8 @@
 // D2Q9 kernels: fused pull step (streaming + half-way bounce-back + moving walls + periodic wrap +
 // BGK collision + Guo forcing in one pass: one read and one write of the nine populations per
-// cell update), link-word construction, equilibrium initialisation, moments, FP64 conservation
-// sums and host-layout conversion.
+// cell update) in scalar, vectorised (d2q9_vec.cuh), bulk-copy (d2q9_bulk.cuh) and two-steps-per-
+// launch (d2q9_tile2.cuh) forms chosen by an autotuner, link-word construction, equilibrium
+// initialisation, moments, FP64 conservation sums and host-layout conversion.
 //
 // Storage: structure of arrays, plane q holds population q of all cells, rows padded to `pitch`
 // elements (a multiple of 32) so each row starts 128-byte aligned in FP32.  Populations are
