@@ -306,7 +306,7 @@ def run_mine(args):
         L.step(args.lbm_steps)  # the first step runs the launch-shape autotuner
     torch.cuda.synchronize(dev)
     info = L.info()
-    two_step = info["cells_per_thread"] == -2  # two time steps per launch on shared-memory tiles
+    two_step = info["cells_per_thread"] in (-2, -3)  # two time steps per launch on shared-memory tiles
     if two_step:
         shape = f"two steps per launch, {info['block_threads']}x{info['rows_per_block']}-cell tiles"
     else:
