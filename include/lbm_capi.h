@@ -108,8 +108,9 @@ typedef struct lbm_info {
     int64_t bytes_per_update; /* algorithmic bytes per cell update: 2 * Q * sizeof(storage) */
     int64_t steps_done;
     int32_t block_threads;    /* D2Q9 step kernel launch shape: threads along x per block, */
-    int32_t cells_per_thread; /* consecutive cells per thread, */
-    int32_t rows_per_block;   /* rows per block */
+    int32_t cells_per_thread; /* consecutive cells per thread (0: bulk-copy pipeline; -2, -3: two */
+    int32_t rows_per_block;   /* steps per launch on tiles of block_threads x rows_per_block cells), */
+                              /* rows per block */
     int32_t tuned;            /* 1 once the shape has been chosen */
     int32_t l2_policy;        /* L2 eviction hints of the vectorised path (see lbm_set_launch) */
 } lbm_info;
