@@ -557,15 +557,27 @@ struct StepArgs {
     const int32_t *tgt_index;  // per cell: its row of `gathered`
 };
 
+// Programmatic dependent launch (PTX griddepcontrol, sm_90 and later).  The gather kernel lets the
+// fused kernel of the same step launch as soon as every gather block has started; the fused kernel
+// waits for the gather grid to complete (its memory visible) only in the threads that read a
+// gathered row, so the other cells' blocks take the SMs the gather blocks leave and the launch gap
+// between the two kernels disappears.  Without a prerequisite grid (a launch without the
+// programmatic attribute) the wait returns at once.
+__device__ __forceinline__ void allow_dependent_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void wait_prerequisite_grids() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // one cell of the fused step: pull (or, for a target of the gather lists, its gathered populations),
 // zero internal cells, collide, flow source, store
 template <int EQ>
 __device__ __forceinline__ bool fused_cell(const StepArgs &a, int64_t c, int x, int y, int z, uint8_t fl) {
     float v[27];
     if (a.cli && (fl & F_GATHER)) {
+        // the row was written by this step's gather grid, which may still run: wait for it, then read
+        // through L2 (not the read-only path: the row changed while this grid was resident)
+        wait_prerequisite_grids();
         const float *g = a.gathered + (int64_t)__ldg(a.tgt_index + c) * 27;
 #pragma unroll
-        for (int j = 0; j < 27; ++j) v[j] = __ldg(g + j);
+        for (int j = 0; j < 27; ++j) v[j] = __ldcg(g + j);
     } else {
         pull(a.src, a.d, c, x, y, z, v);
     }
@@ -623,6 +635,9 @@ __device__ __forceinline__ void prefetch_block_ahead(const StepArgs &a) {
 
 template <int EQ>
 __global__ void __launch_bounds__(FUSED_THREADS, fused_min_blocks(EQ)) fused_kernel(StepArgs a) {
+    // one thread of the last block waits for the gather grid whatever the flags say, so this grid
+    // never completes before it (work queued after the step sees the force the gather added)
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) wait_prerequisite_grids();
     if constexpr (EQ == EQ_F32) prefetch_block_ahead(a);
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= a.d.n) return;
@@ -684,6 +699,7 @@ constexpr int GATHER_THREADS = 512;
 
 template <int MODE>
 __global__ void __launch_bounds__(GATHER_THREADS) gather_kernel(StepArgs a, GatherArgs g) {
+    if (MODE == 0) allow_dependent_launch();  // the fused kernel may launch (it waits for the rows)
     // the direction tables in shared memory: each lane indexes them with its own direction
     __shared__ int s_dir[27][3];
     __shared__ float s_cs[27][3];
@@ -1096,17 +1112,29 @@ cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps, double *series_d) {
         cudaError_t e = cudaSuccess;
         double *copy = series_d ? series_d + 3 * (int64_t)s : nullptr;
         const bool reduced = a.cli && ctx->ntgt > 0 && ctx->force_on;  // the force changes this step
+        const bool gathered = a.cli && ctx->ntgt > 0;
         if (a.cli) {  // the targets of the gather lists first: the fused kernel collides them
             e = launch_gather(ctx, a, 0, copy);
             if (e != cudaSuccess) return e;
         }
+        // after a gather launch the fused kernel is its programmatic dependent (it overlaps the
+        // gather's tail); otherwise an ordinary stream-ordered launch
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(blocks_for(ctx->cells, threads));
+        cfg.blockDim = dim3(threads);
+        cfg.stream = ctx->stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = gathered ? 1 : 0;
         if (ctx->eq_mode == EQ_F64)
-            fused_kernel<EQ_F64><<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
+            e = cudaLaunchKernelEx(&cfg, fused_kernel<EQ_F64>, a);
         else if (ctx->eq_mode == EQ_F32)
-            fused_kernel<EQ_F32><<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
+            e = cudaLaunchKernelEx(&cfg, fused_kernel<EQ_F32>, a);
         else
-            fused_kernel<EQ_FF><<<blocks_for(ctx->cells, threads), threads, 0, ctx->stream>>>(a);
-        e = cudaGetLastError();
+            e = cudaLaunchKernelEx(&cfg, fused_kernel<EQ_FF>, a);
+        if (e == cudaSuccess) e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         if (copy && !reduced) {
             e = cudaMemcpyAsync(copy, ctx->force_acc_d, 3 * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
