@@ -29,6 +29,7 @@
 #include "d2q9_bulk.cuh"
 #include "d2q9_tile2.cuh"
 #include "d2q9_vec.cuh"
+#include "pdl.cuh"
 #include "reduce.cuh"
 
 namespace lbm {
@@ -135,6 +136,10 @@ __global__ void __launch_bounds__(256, vec_min_blocks(V)) step_vec_kernel(const 
                                                        const uint16_t *__restrict__ links, int nx, int ny,
                                                        int pitch, int plane, int periodic, D2Q9Params prm,
                                                        int reverse) {
+    // launched as the programmatic dependent of the step before: nothing is read before that step
+    // has completed, and the next step's blocks may be scheduled as this one's last blocks finish
+    wait_prerequisite_grids();
+    allow_dependent_launch();
     const int row = blockIdx.y * blockDim.y + threadIdx.y;
     if (row >= ny) return;  // uniform per warp: warps never straddle rows
     const int y = reverse ? ny - 1 - row : row;
@@ -488,18 +493,24 @@ cudaError_t launch_one(lbm_ctx *ctx, const Shape &sh, const S *src, S *dst, int 
                          : launch_bulk_variant<S, false>(ctx, sh.pol, src, dst, reverse);
         return cudaErrorInvalidValue;
     }
+    // the vector kernels: programmatic dependents of the launch before (back-to-back steps overlap
+    // one step's last blocks with the next one's launch)
 #define LBM_VEC_LAUNCH(VV, PP)                                                                                  \
-    if (force) step_vec_kernel<S, VV, true, PP><<<grid, block, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, reverse); \
-    else step_vec_kernel<S, VV, false, PP><<<grid, block, 0, st>>>(src, dst, ctx->links_d, d.nx, d.ny, pitch, plane, d.periodic, prm, reverse);
+    e = force ? launch_maybe_dependent(true, step_vec_kernel<S, VV, true, PP>, grid, block, 0, st, src, dst,    \
+                                       links, d.nx, d.ny, pitch, plane, d.periodic, prm, reverse)               \
+              : launch_maybe_dependent(true, step_vec_kernel<S, VV, false, PP>, grid, block, 0, st, src, dst,   \
+                                       links, d.nx, d.ny, pitch, plane, d.periodic, prm, reverse);
 #define LBM_VEC_CASE(VV)                                                                                        \
     if constexpr (vec_ok<S>(VV)) {                                                                              \
         if (sh.v == VV) {                                                                                       \
+            cudaError_t e;                                                                                      \
             if (sh.pol == 1) { LBM_VEC_LAUNCH(VV, 1) }                                                          \
             else if (sh.pol == 2) { LBM_VEC_LAUNCH(VV, 2) }                                                     \
             else { LBM_VEC_LAUNCH(VV, 0) }                                                                      \
-            return cudaGetLastError();                                                                          \
+            return e != cudaSuccess ? e : cudaGetLastError();                                                   \
         }                                                                                                       \
     }
+    const uint16_t *links = ctx->links_d;
     LBM_VEC_CASE(2)
     LBM_VEC_CASE(4)
     LBM_VEC_CASE(8)

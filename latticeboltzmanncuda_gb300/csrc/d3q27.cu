@@ -24,6 +24,7 @@
 #include <type_traits>
 
 #include "lbm_internal.h"
+#include "pdl.cuh"
 #include "reduce.cuh"
 
 namespace lbm {
@@ -557,14 +558,10 @@ struct StepArgs {
     const int32_t *tgt_index;  // per cell: its row of `gathered`
 };
 
-// Programmatic dependent launch (PTX griddepcontrol, sm_90 and later).  The gather kernel lets the
-// fused kernel of the same step launch as soon as every gather block has started; the fused kernel
-// waits for the gather grid to complete (its memory visible) only in the threads that read a
-// gathered row, so the other cells' blocks take the SMs the gather blocks leave and the launch gap
-// between the two kernels disappears.  Without a prerequisite grid (a launch without the
-// programmatic attribute) the wait returns at once.
-__device__ __forceinline__ void allow_dependent_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-__device__ __forceinline__ void wait_prerequisite_grids() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// The fused kernel is launched as the gather kernel's programmatic dependent (pdl.cuh): it may launch
+// as soon as every gather block has started and waits for the gather grid only in the threads that
+// read a gathered row, so the other cells' blocks take the SMs the gather blocks leave and the
+// launch gap between the two kernels disappears.
 
 // one cell of the fused step: pull (or, for a target of the gather lists, its gathered populations),
 // zero internal cells, collide, flow source, store
@@ -1119,21 +1116,13 @@ cudaError_t d3q27_step(lbm_ctx *ctx, int nsteps, double *series_d) {
         }
         // after a gather launch the fused kernel is its programmatic dependent (it overlaps the
         // gather's tail); otherwise an ordinary stream-ordered launch
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(blocks_for(ctx->cells, threads));
-        cfg.blockDim = dim3(threads);
-        cfg.stream = ctx->stream;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        attr[0].val.programmaticStreamSerializationAllowed = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = gathered ? 1 : 0;
+        const dim3 grid(blocks_for(ctx->cells, threads)), block(threads);
         if (ctx->eq_mode == EQ_F64)
-            e = cudaLaunchKernelEx(&cfg, fused_kernel<EQ_F64>, a);
+            e = launch_maybe_dependent(gathered, fused_kernel<EQ_F64>, grid, block, 0, ctx->stream, a);
         else if (ctx->eq_mode == EQ_F32)
-            e = cudaLaunchKernelEx(&cfg, fused_kernel<EQ_F32>, a);
+            e = launch_maybe_dependent(gathered, fused_kernel<EQ_F32>, grid, block, 0, ctx->stream, a);
         else
-            e = cudaLaunchKernelEx(&cfg, fused_kernel<EQ_FF>, a);
+            e = launch_maybe_dependent(gathered, fused_kernel<EQ_FF>, grid, block, 0, ctx->stream, a);
         if (e == cudaSuccess) e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         if (copy && !reduced) {
