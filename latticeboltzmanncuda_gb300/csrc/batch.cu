@@ -35,6 +35,7 @@
 
 #include "d2q9_vec.cuh"
 #include "lbm_internal.h"
+#include "pdl.cuh"
 
 namespace lbm {
 lbm_status set_thread_error(lbm_status s, const std::string &msg);
@@ -118,6 +119,8 @@ template <class S, int V>
 __global__ void __launch_bounds__(256) batch_step_kernel(const SlotDesc *__restrict__ slots,
                                                          const Tile *__restrict__ tiles, int ntiles, int step,
                                                          int reverse) {
+    wait_prerequisite_grids();  // a programmatic dependent of the launch before (launch_v)
+    allow_dependent_launch();
     batch_tile<S, V>(slots, tiles, ntiles, step, reverse);
 }
 
@@ -128,6 +131,8 @@ template <class S, int V>
 __global__ void __launch_bounds__(256, 4) batch_step_kernel_occ(const SlotDesc *__restrict__ slots,
                                                                 const Tile *__restrict__ tiles, int ntiles, int step,
                                                                 int reverse) {
+    wait_prerequisite_grids();  // a programmatic dependent of the launch before (launch_v)
+    allow_dependent_launch();
     batch_tile<S, V>(slots, tiles, ntiles, step, reverse);
 }
 
@@ -279,12 +284,16 @@ __device__ __forceinline__ int launch_tile(int ntiles, int reverse) {
 template <class S, int V>
 __global__ void __launch_bounds__(256, batch_min_blocks(V)) batch_step_kernel_p(const __grid_constant__ BatchParams p,
                                                                                int step, int reverse) {
+    wait_prerequisite_grids();  // a programmatic dependent of the launch before (launch_v)
+    allow_dependent_launch();
     batch_tile_p<S, V>(p, launch_tile(p.ntiles, reverse), step, reverse ? -1 : 1);
 }
 
 template <class S, int V>
 __global__ void __launch_bounds__(256, 4) batch_step_kernel_p_occ(const __grid_constant__ BatchParams p, int step,
                                                                   int reverse) {
+    wait_prerequisite_grids();  // a programmatic dependent of the launch before (launch_v)
+    allow_dependent_launch();
     batch_tile_p<S, V>(p, launch_tile(p.ntiles, reverse), step, reverse ? -1 : 1);
 }
 
@@ -644,20 +653,29 @@ lbm_status rebuild(lbm_batch *b, int64_t nsteps) {
 
 template <class S, int V>
 cudaError_t launch_v(lbm_batch *b, int step, int reverse) {
-    dim3 block(b->tx, b->ty);
-    dim3 grid((unsigned)b->ntiles);
+    // every step kernel is the programmatic dependent of the launch before it: its blocks wait for
+    // that grid at entry and may be scheduled while its last blocks finish
+    const dim3 block(b->tx, b->ty);
+    const dim3 grid((unsigned)b->ntiles);
+    cudaError_t e = cudaErrorInvalidValue;
     if (b->use_params) {
         if constexpr (sizeof(S) == 2 && V == 4)
-            batch_step_kernel_p_occ<S, V><<<grid, block, 0, b->stream>>>(b->params, step, reverse);
+            e = launch_maybe_dependent(true, batch_step_kernel_p_occ<S, V>, grid, block, 0, b->stream, b->params, step,
+                                       reverse);
         else if constexpr (sizeof(S) <= 4)
-            batch_step_kernel_p<S, V><<<grid, block, 0, b->stream>>>(b->params, step, reverse);
-        return cudaGetLastError();
+            e = launch_maybe_dependent(true, batch_step_kernel_p<S, V>, grid, block, 0, b->stream, b->params, step,
+                                       reverse);
+        return e != cudaSuccess ? e : cudaGetLastError();
     }
+    const SlotDesc *descs = b->desc_d;
+    const Tile *tiles = b->tiles_d;
     if constexpr (sizeof(S) == 2 && V == 4)
-        batch_step_kernel_occ<S, V><<<grid, block, 0, b->stream>>>(b->desc_d, b->tiles_d, b->ntiles, step, reverse);
+        e = launch_maybe_dependent(true, batch_step_kernel_occ<S, V>, grid, block, 0, b->stream, descs, tiles,
+                                   b->ntiles, step, reverse);
     else
-        batch_step_kernel<S, V><<<grid, block, 0, b->stream>>>(b->desc_d, b->tiles_d, b->ntiles, step, reverse);
-    return cudaGetLastError();
+        e = launch_maybe_dependent(true, batch_step_kernel<S, V>, grid, block, 0, b->stream, descs, tiles, b->ntiles,
+                                   step, reverse);
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 // batches of at most this many live cells run a step sequence as one persistent launch (measured
