@@ -310,8 +310,9 @@ LBM_API lbm_status lbm_batch_synchronize(lbm_batch *b);
 /* Persistent launches: a step sequence of lbm_batch_step (two steps or more) runs as one
  * cooperative launch whose blocks meet after each step, instead of one launch per step.  With
  * 4-wide tiles (the default shape of batches below the tuning threshold), for FP32 and 16-bit
- * storage.  mode 0: never; 1 (default): batches of at most 2^19 live cells, where a launch per step
- * costs more than the step; 2: whenever the shape allows.  Each meeting waits at most wait_ns
+ * storage.  mode 0 (default): never; 1: batches of at most 2^19 live cells; 2: whenever the shape
+ * allows.  One launch per step, each launch allowed to start while the one before finishes, measured
+ * faster than the persistent launch on batches of 2e4 to 1.6e6 cells.  Each meeting waits at most wait_ns
  * (default 1e9) for the other blocks, then the launch ends and lbm_batch_synchronize reports
  * LBM_ERR_TIMEOUT.  skip_block >= 0 is a diagnostic: that block does not arrive at the first
  * meeting, so the wait runs out (no counterpart in the reference). */

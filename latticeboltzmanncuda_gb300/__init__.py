@@ -444,9 +444,9 @@ class Batch:
         self._chk(capi.lib().lbm_batch_synchronize(self._b))
 
     def set_persistent(self, mode=1, wait_ns=1_000_000_000, skip_block=-1):
-        """Step sequences as one persistent launch: mode 0 never, 1 batches of at most 2^19 live
-        cells (default), 2 whenever the tile shape allows; skip_block >= 0 is a diagnostic that
-        makes the launch's wait run out (synchronize then raises LBM_ERR_TIMEOUT)."""
+        """Step sequences as one persistent launch: mode 0 never (the batch's default), 1 batches of
+        at most 2^19 live cells, 2 whenever the tile shape allows; skip_block >= 0 is a diagnostic
+        that makes the launch's wait run out (synchronize then raises LBM_ERR_TIMEOUT)."""
         self._chk(capi.lib().lbm_batch_set_persistent(self._b, int(mode), int(wait_ns), int(skip_block)))
 
     @property

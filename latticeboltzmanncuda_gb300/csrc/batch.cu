@@ -403,9 +403,11 @@ struct lbm_batch {
     bool use_params = false;             // the launch takes the descriptors in its parameter block
     BatchParams params{};
     int64_t next_ticket = 1;
-    // persistent launches: mode (0 never, 1 batches of at most PERSIST_CELLS live cells, 2 whenever
-    // the launch allows it), the limit of their waits, a block that does not arrive (diagnostic)
-    int persist = 1;
+    // persistent launches: mode (0 never, the default: one launch per step, each the programmatic
+    // dependent of the one before, measured faster at every batch size; 1 batches of at most
+    // PERSIST_CELLS live cells; 2 whenever the launch allows it), the limit of their waits, a block
+    // that does not arrive (diagnostic)
+    int persist = 0;
     int64_t persist_wait_ns = 1000000000;
     int persist_skip = -1;
     GridSync *sync_d = nullptr;
@@ -678,9 +680,11 @@ cudaError_t launch_v(lbm_batch *b, int step, int reverse) {
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 
-// batches of at most this many live cells run a step sequence as one persistent launch (measured
-// on FP16 batches of 64^2-256^2 domains, 200-step sequences: 1.48x at 2e4-7e4 cells, 1.05x at
-// 3.8e5, 0.91x at 1.6e6, where the per-step kernel's higher occupancy wins)
+// mode 1: batches of at most this many live cells run a step sequence as one persistent launch.
+// Measured on FP16 batches of 64^2-256^2 domains, 200-step sequences, against one launch per step:
+// 1.48x at 2e4-7e4 cells, 1.05x at 3.8e5, 0.91x at 1.6e6 when every launch waited for the one
+// before to drain; 0.82-0.87x at every size once each step launch is the programmatic dependent
+// of the one before, hence mode 0 by default.
 constexpr int64_t PERSIST_CELLS = (int64_t)1 << 19;
 
 bool persistent_ok(const lbm_batch *b, int nsteps) {
