@@ -1,6 +1,7 @@
 // Batched D2Q9: many independent domains of uneven size, tau, forcing and obstacle mask advance
-// together, one kernel launch per time step for all of them (a batch of few cells: one persistent
-// cooperative launch per step sequence, its blocks meeting after each step).
+// together, one kernel launch per time step for all of them, each launch the programmatic dependent
+// of the one before (lbm_batch_set_persistent: one persistent cooperative launch per step sequence
+// instead, its blocks meeting after each step).
 //
 // Each domain (a "slot") owns one allocation -- its two population buffers, link words, flags and
 // fluid-cell count -- made when it is added, so slots come and go without moving anyone else's

@@ -2,7 +2,9 @@
 // BGK collision + Guo forcing in one pass: one read and one write of the nine populations per
 // cell update) in scalar, vectorised (d2q9_vec.cuh), bulk-copy (d2q9_bulk.cuh) and two-steps-per-
 // launch (d2q9_tile2.cuh) forms chosen by an autotuner, link-word construction, equilibrium
-// initialisation, moments, FP64 conservation sums and host-layout conversion.
+// initialisation, moments, FP64 conservation sums and host-layout conversion.  The vectorised step
+// is launched as the programmatic dependent of the launch before it (pdl.cuh), so back-to-back
+// steps overlap one step's last wave with the next step's first blocks.
 //
 // Storage: structure of arrays, plane q holds population q of all cells, rows padded to `pitch`
 // elements (a multiple of 32) so each row starts 128-byte aligned in FP32.  Populations are
