@@ -635,6 +635,7 @@ __global__ void __launch_bounds__(FUSED_THREADS, fused_min_blocks(EQ)) fused_ker
     // one thread of the last block waits for the gather grid whatever the flags say, so this grid
     // never completes before it (work queued after the step sees the force the gather added)
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) wait_prerequisite_grids();
+    allow_dependent_launch();  // the next step's gather kernel may launch (it waits for this grid)
     if constexpr (EQ == EQ_F32) prefetch_block_ahead(a);
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= a.d.n) return;
@@ -696,7 +697,10 @@ constexpr int GATHER_THREADS = 512;
 
 template <int MODE>
 __global__ void __launch_bounds__(GATHER_THREADS) gather_kernel(StepArgs a, GatherArgs g) {
-    if (MODE == 0) allow_dependent_launch();  // the fused kernel may launch (it waits for the rows)
+    // mode 0 is the programmatic dependent of the step before (its populations are read here) and
+    // lets this step's fused kernel launch, which waits for the rows
+    wait_prerequisite_grids();
+    if (MODE == 0) allow_dependent_launch();
     // the direction tables in shared memory: each lane indexes them with its own direction
     __shared__ int s_dir[27][3];
     __shared__ float s_cs[27][3];
@@ -1000,11 +1004,14 @@ cudaError_t launch_gather(lbm_ctx *ctx, const StepArgs &a, int mode, double *for
     const int threads = GATHER_THREADS;
     const unsigned nb = (unsigned)d3q27_gather_blocks(ctx->ntgt);  // one warp per target cell
     static_assert(GATHER_THREADS == 16 * 32, "d3q27_gather_blocks assumes sixteen warps per block");
-    if (mode != 0)
+    if (mode != 0) {
         gather_kernel<1><<<nb, threads, 0, ctx->stream>>>(a, g);
-    else
-        gather_kernel<0><<<nb, threads, 0, ctx->stream>>>(a, g);
-    return cudaGetLastError();  // the force, when accumulated, was added by the kernel's last block
+        return cudaGetLastError();
+    }
+    // the step's gather: the programmatic dependent of the launch before (the previous step's fused
+    // kernel), its blocks waiting for that grid at entry
+    const cudaError_t e = launch_maybe_dependent(true, gather_kernel<0>, dim3(nb), dim3(threads), 0, ctx->stream, a, g);
+    return e != cudaSuccess ? e : cudaGetLastError();  // the force, when accumulated, was added by the kernel's last block
 }
 
 // Both equilibrium evaluations on n pseudo-random (rho, u) samples, all directions: counts the

@@ -6,9 +6,12 @@ stores anything that grid reads or writes.  The contract per kernel:
 
 * the D2Q9 vector step and the four batch step kernels: the wait is the first statement of the
   kernel, before any early return, and allow_dependent_launch() follows it;
+* the D3Q27 gather kernel (the programmatic dependent of the previous step's fused kernel): the
+  wait is its first statement;
 * the D3Q27 fused kernel: the wait precedes the read of a gathered row (the only data the gather
   grid before it writes), and one thread of the last block waits unconditionally, so the fused
-  grid never completes before the gather grid;
+  grid never completes before the gather grid; the gather kernel allows its launch only after its
+  own wait, so the fused kernel starts after the previous step's fused kernel has completed;
 * every kernel named in a launch_maybe_dependent call is one of those above.
 """
 import os
@@ -66,7 +69,7 @@ def test_dependent_kernels_wait_first(fname):
 @pytest.mark.parametrize("fname", ["d2q9.cu", "batch.cu", "d3q27.cu"])
 def test_only_contracted_kernels_are_launched_as_dependents(fname):
     src = source(fname)
-    allowed = WAIT_FIRST.get(fname, set()) | ({"fused_kernel"} if fname == "d3q27.cu" else set())
+    allowed = WAIT_FIRST.get(fname, set()) | ({"fused_kernel", "gather_kernel"} if fname == "d3q27.cu" else set())
     launched = launched_dependent(src)
     assert launched, f"no dependent launch found in {fname}"
     assert launched <= allowed, launched - allowed
@@ -82,8 +85,11 @@ def test_fused_kernel_waits_before_reading_gathered_rows():
     assert "__ldg(g + j)" not in branch and "__ldcg(g + j)" in branch
     body = statements(kernel_body(src, "fused_kernel"))
     assert body[0] == "if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) wait_prerequisite_grids()", body[0]
-    # the gather kernel allows the launch of its dependent
-    assert "allow_dependent_launch()" in kernel_body(src, "gather_kernel")
+    # the gather kernel waits first, then allows the launch of its dependent
+    gather = statements(kernel_body(src, "gather_kernel"))
+    assert gather[0] == "wait_prerequisite_grids()", gather[0]
+    assert gather[1] == "if (MODE == 0) allow_dependent_launch()", gather[1]
+    assert "allow_dependent_launch()" in body[1], body[1]
 
 
 def test_contract_check_catches_a_load_before_the_wait():
